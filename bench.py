@@ -1,0 +1,335 @@
+#!/usr/bin/env python
+"""Benchmark of COMMIT's operator pair A*x + A'*y on one GB300 (or N replicas).
+
+Workload (default ``hcp_1m``): seeded synthetic full-brain dictionary -- 145x174x145 grid,
+600k-voxel mask, 1M streamlines (~1.2e8 segments), stick-zeppelin-ball model with 1 IC,
+1 EC and 2 ISO responses, 18 b0 + 3 shells x 90 directions (nS = 288), 500 LUT
+directions, FP32 LUT and lengths, FP64 vectors.  A step is one operator pair
+y = A x, g = A' y over the whole workload; ``value`` is pairs/s with the inputs resident
+in HBM (y is 1.38 GB, far larger than the 129 MB L2, so no L2 flush is needed).
+``e2e`` is the same metric through LinearOperator.dot on pinned host buffers, host
+copies included.  ``--impl reference`` times the reference's own compiled CPU operator
+(oracle/_ref, or the C restatement when the reference was not compiled) on a bounded
+voxel-slab sample of the same workload, scaled to the full workload by segment count.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'A·x+Aᵀx operator pairs/s (1M-streamline workload)'
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument('--gpus', type=int, default=1)
+    p.add_argument('--steps', type=int, default=10)
+    p.add_argument('--warmup', type=int, default=3)
+    p.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    p.add_argument('--workload', default='hcp_1m')
+    p.add_argument('--fibers', type=int, default=0, help='override the number of streamlines (smaller runs)')
+    p.add_argument('--arith', default='ff', choices=['ff', 'f64'])
+    p.add_argument('--sample-frac', type=float, default=1.0 / 16.0, help='CPU sample: fraction of the segments')
+    p.add_argument('--no-e2e', action='store_true')
+    p.add_argument('--no-cpu', action='store_true')
+    return p.parse_args()
+
+
+# ------------------------------------------------------------------ environment helpers
+def dist_env():
+    ws = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+    FIELDS = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+              'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+              'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix='.csv')
+            os.close(fd)
+            self.f = open(self.path, 'w')
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.gpu), f'--query-gpu={self.FIELDS}',
+                                          '--format=csv,noheader,nounits', '-lms', '200'], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = [r.split(',') for r in open(self.path).read().strip().splitlines() if r.strip()]
+        os.unlink(self.path)
+        sm, mx, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for r in rows:
+            r = [c.strip() for c in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, r[5:9]):
+                if val.lower().startswith('active'):
+                    reasons.add(nm)
+        return {'sm_mhz': statistics.median(sm) if sm else None, 'sm_max_mhz': max(mx) if mx else None,
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return {'hbm_gbs': d.get('hbm_gbs', 6800.0), 'src': 'measured'}
+    return {'hbm_gbs': 6800.0, 'src': 'fallback'}
+
+
+def algorithmic(D, K) -> tuple:
+    """Compulsory bytes and FMAs of one product (A or A'), LUT bytes excluded (on-chip)."""
+    n, nE, nI = D['IC']['n'], D['EC']['n'], D['ISO']['n']
+    nIC, nEC, nISO = K['wmr'].shape[0], K['wmh'].shape[0], K['iso'].shape[0]
+    nS = K['wmr'].shape[2]
+    nrows = D['IC']['nVOX'] * nS
+    ncols = D['IC']['nSTR'] * nIC + nE * nEC + nI * nISO
+    b = n * (4 + 4 + 2 + 4) + (nE * (4 + 2) if nEC else 0) + (nI * 4 if nISO else 0) + ncols * 8 + nrows * 8
+    f = n * nS * nIC + nE * nS * nEC + nI * nS * nISO
+    return b, f, nrows, ncols
+
+
+def sample_slab(D, K, frac: float):
+    """Central slab of voxels holding about `frac` of the IC segments (voxel-sorted)."""
+    vox = D['IC']['vox']
+    nV = D['IC']['nVOX']
+    counts = np.bincount(vox, minlength=nV)
+    c = np.cumsum(counts)
+    n = int(c[-1])
+    mid = int(np.searchsorted(c, n // 2))
+    lo, hi = mid, mid
+    target = max(1, int(frac * n))
+    while (int(c[hi - 1]) if hi > 0 else 0) - (int(c[lo - 1]) if lo > 0 else 0) < target and (lo > 0 or hi < nV):
+        lo = max(0, lo - max(1, (hi - lo) // 2 + 16))
+        hi = min(nV, hi + max(1, (hi - lo) // 2 + 16))
+    s0 = int(c[lo - 1]) if lo > 0 else 0
+    s1 = int(c[hi - 1]) if hi > 0 else 0
+    IC = {k: np.ascontiguousarray(D['IC'][k][s0:s1]) for k in ('str', 'vox', 'dir', 'len')}
+    IC['vox'] = (IC['vox'] - lo).astype(np.uint32)
+    IC['n'] = s1 - s0
+    IC['nSTR'] = D['IC']['nSTR']
+    IC['nVOX'] = hi - lo
+    IC['eval'] = np.ones(IC['nSTR'] * K['wmr'].shape[0], np.uint32)
+    ev = D['EC']['vox']
+    e0, e1 = np.searchsorted(ev, lo), np.searchsorted(ev, hi)
+    EC = {'vox': (ev[e0:e1] - lo).astype(np.uint32), 'dir': np.ascontiguousarray(D['EC']['dir'][e0:e1]),
+          'n': int(e1 - e0)}
+    iv = D['ISO']['vox']
+    i0, i1 = np.searchsorted(iv, lo), np.searchsorted(iv, hi)
+    ISO = {'vox': (iv[i0:i1] - lo).astype(np.uint32), 'n': int(i1 - i0)}
+    return {'IC': IC, 'EC': EC, 'ISO': ISO}, (s1 - s0) / n, (lo, hi)
+
+
+def cpu_reference(D, K, frac, steps, warmup):
+    """Time the reference CPU operator (oracle/_ref if compiled for this host, else the
+    C restatement) on a voxel-slab sample; returns a cpu_baseline dict (pairs/s scaled
+    to the full workload by segment count)."""
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    import oracle as O
+    import build_ref
+    cores = os.cpu_count() or 1
+    Ds, share, (lo, hi) = sample_slab(D, K, frac)
+    kind = 'port'
+    try:
+        if build_ref.generate() and build_ref.compile_operator() and O.ref_available():
+            kind = 'reference'
+    except Exception:
+        kind = 'port'
+    threads = min(cores, 255)
+    if kind == 'reference':
+        A = O.RefOperator(Ds, K, O.set_threads(Ds, threads))
+    else:
+        A = O.PortOperator(Ds, K, None, nthreads=threads)
+    x = np.random.default_rng(11).uniform(0.0, 1.0, size=A.nCOLS)
+    for _ in range(max(1, warmup)):
+        y = A.dot(x)
+        A.T.dot(y)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        y = A.dot(x)
+        A.T.dot(y)
+    dt = time.perf_counter() - t0
+    rate_sample = steps / dt
+    return {'value': rate_sample * share, 'unit': 'pairs/s', 'cores': threads, 'kind': kind,
+            'sample': (f'central voxel slab [{lo},{hi}) = {share * 100:.2f}% of the IC segments '
+                       f'({Ds["IC"]["n"]} segments, {Ds["EC"]["n"]} EC, {Ds["ISO"]["n"]} ISO); {steps} pairs in '
+                       f'{dt:.2f} s on {threads} threads, rate scaled by segment share'),
+            'sample_pairs_per_s': rate_sample}
+
+
+def build_workload(args, device):
+    from commit_gb300 import synth
+    spec = synth.SPECS[args.workload]
+    if args.fibers:
+        spec = synth.scaled_spec(args.workload, n_fibers=args.fibers)
+    t0 = time.perf_counter()
+    D, K = synth.make_dictionary(spec, device=device)
+    D['IC']['eval'] = np.ones(D['IC']['nSTR'] * K['wmr'].shape[0], np.uint32)
+    return spec, D, K, time.perf_counter() - t0
+
+
+def workload_config(spec, D, K, args):
+    nS = K['wmr'].shape[2]
+    return {'workload': f'{args.workload}: {spec.n_fibers} synthetic streamlines, grid {"x".join(map(str, spec.dim))}, '
+                        f'{spec.n_mask} mask voxels, SZB 1 IC / {K["wmh"].shape[0]} EC / {K["iso"].shape[0]} ISO, '
+                        f'nS={nS}, ndirs={spec.ndirs}',
+            'n_segments': int(D['IC']['n']), 'n_voxels': int(D['IC']['nVOX']), 'n_ec': int(D['EC']['n']),
+            'n_iso': int(D['ISO']['n']), 'nS': int(nS), 'vectors': 'f64', 'lut': 'f32',
+            'arith': args.arith, 'l2': 'inputs larger than L2 (y is nV*nS f64), no flush'}
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return 0
+    import torch
+    dev = 'cuda' if torch.cuda.is_available() else 'cpu'
+    spec, D, K, _ = build_workload(args, dev)
+    cb = cpu_reference(D, K, args.sample_frac, args.steps, args.warmup)
+    out = {'metric': METRIC, 'value': cb['value'], 'unit': 'pairs/s', 'impl': 'reference', 'n_gpus': args.gpus,
+           'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': 1000.0 / cb['value'],
+           'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
+           'config': workload_config(spec, D, K, args), 'cpu_baseline': cb,
+           'e2e': {'value': cb['value'], 'unit': 'pairs/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(out))
+    return 0
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group('nccl')
+    dev = torch.device('cuda', torch.cuda.current_device())
+    from commit_gb300 import synth
+    from commit_gb300.operator import LinearOperator
+    spec, D, K, tgen = build_workload(args, 'cuda')
+    A = LinearOperator(D, K, None, arith=args.arith, device=dev.index)
+    At = A.T
+    nbytes, nfma, nrows, ncols = algorithmic(D, K)
+    x = torch.from_numpy(synth.make_x(ncols, spec.seed + 1)).to(dev)
+    y = torch.empty(nrows, dtype=torch.float64, device=dev)
+    g = torch.empty(ncols, dtype=torch.float64, device=dev)
+    st = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        A.dot(x, out=y)
+        At.dot(y, out=g)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+        torch.cuda.synchronize()
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e_start.record(st)
+    for k in range(args.steps):
+        ev[k][0].record(st)
+        A.dot(x, out=y)
+        ev[k][1].record(st)
+        At.dot(y, out=g)
+        ev[k][2].record(st)
+    e_end.record(st)
+    torch.cuda.synchronize()
+    ms = e_start.elapsed_time(e_end)
+    if ws > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.barrier()
+        ms = float(t.item())
+    clk = clocks.stop()
+    fwd_ms = statistics.mean(a.elapsed_time(b) for a, b, _ in ev)
+    adj_ms = statistics.mean(b.elapsed_time(c) for _, b, c in ev)
+    value = args.steps * ws / (ms / 1000.0)
+    peaks = measured_peaks()
+    dom, dom_ms = ('adjoint (voxel pass + fibre sum)', adj_ms) if adj_ms >= fwd_ms else ('forward k_forward', fwd_ms)
+    achieved = nbytes / (dom_ms / 1000.0) / 1e9
+    out = {'metric': METRIC, 'value': value, 'unit': 'pairs/s', 'n_gpus': ws, 'steps': args.steps,
+           'warmup': args.warmup, 'ms_per_step': ms / args.steps, 'higher_is_better': True, 'scaling': 'weak',
+           'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'config': workload_config(spec, D, K, args),
+           'roofline': {'bound': 'hbm', 'kernel': dom, 'achieved': achieved, 'peak': peaks['hbm_gbs'],
+                        'unit': 'GB/s', 'frac': achieved / peaks['hbm_gbs'], 'peak_src': peaks['src'],
+                        'traffic': None, 'algorithmic_bytes_per_launch': nbytes,
+                        'forward_ms': fwd_ms, 'adjoint_ms': adj_ms,
+                        'fma_per_product': nfma, 'achieved_gfma_s': nfma / (dom_ms / 1000.0) / 1e9},
+           'clocks': clk, 'gpu_launches': args.steps * (1 + 2), 'setup_s': {'generate': tgen}}
+    # end to end through the public API on pinned host buffers
+    if not args.no_e2e:
+        xh = torch.empty(ncols, dtype=torch.float64, pin_memory=True).numpy()
+        xh[:] = x.cpu().numpy()
+        yh = torch.empty(nrows, dtype=torch.float64, pin_memory=True).numpy()
+        gh = torch.empty(ncols, dtype=torch.float64, pin_memory=True).numpy()
+        for _ in range(max(1, args.warmup)):
+            A.dot(xh, out=yh)
+            At.dot(yh, out=gh)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            A.dot(xh, out=yh)
+            At.dot(yh, out=gh)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        if ws > 1:
+            t = torch.tensor([dt], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            dt = float(t.item())
+        out['e2e'] = {'value': args.steps * ws / dt, 'unit': 'pairs/s', 'h2d_bytes_per_step': (ncols + nrows) * 8,
+                      'd2h_bytes_per_step': (nrows + ncols) * 8}
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        out['cpu_baseline'] = cpu_reference(D, K, args.sample_frac, 3, 1)
+    if rank == 0:
+        print(json.dumps(out))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == 'reference':
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == '__main__':
+    sys.exit(main())

@@ -1,0 +1,102 @@
+// Internal declarations shared by the commit_gb300 CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include <string>
+
+#include "../../include/commit_gb300.h"
+
+namespace cgb {
+
+// ------------------------------------------------------------------ errors
+void set_error(const std::string &msg);
+int fail(int code, const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+
+#define CGB_CUDA(call)                                                  \
+    do {                                                                \
+        cudaError_t e__ = (call);                                       \
+        if (e__ != cudaSuccess) return ::cgb::cuda_fail(e__, #call);    \
+    } while (0)
+
+#define CGB_TRY(call)                         \
+    do {                                      \
+        int rc__ = (call);                    \
+        if (rc__ != CGB_OK) return rc__;      \
+    } while (0)
+
+// ------------------------------------------------------------------ sizes
+constexpr int kMaxChunks = 16;       // samples per lane: nS <= 32 * kMaxChunks
+constexpr int kMaxSamples = 32 * kMaxChunks;
+constexpr int kBlock = 256;          // threads per block of the voxel kernels
+constexpr int kRedSlots = 16;        // doubles reduced per block in the FISTA partial sums
+
+// ------------------------------------------------------------------ device view of a handle
+struct OpDev {
+    int nS, ndirs, nF, nE, nV, nISOv, nIC, nEC, nISO;
+    int64_t n;
+    int64_t ec_base, iso_base;      // first EC / ISO column
+    const float *lutIC, *lutEC, *lutISO;          // float32 LUTs
+    const void *lutIC_r, *lutEC_r;                // reduced-precision LUT copies (bf16/fp16) or null
+    const uint32_t *vox_ptr;        // [nV+1] IC segments of voxel v: [vox_ptr[v], vox_ptr[v+1])
+    const uint32_t *seg_f;          // [n] voxel-ordered fibre index
+    const uint16_t *seg_o;          // [n] voxel-ordered orientation
+    const float *seg_l;             // [n] voxel-ordered length
+    const __half *seg_l16;          // [n] FP16 lengths (reduced path) or null
+    const uint32_t *eval;           // [nF*nIC]
+    const uint32_t *fib_ptr;        // [nF+1] fibre f owns fib_perm[fib_ptr[f] .. fib_ptr[f+1])
+    const uint32_t *fib_perm;       // [n] voxel-order positions grouped by fibre
+    const uint32_t *ec_ptr;         // [nV+1]
+    const uint32_t *ec_col;         // [nE] EC element (column) of each voxel-ordered entry
+    const uint16_t *ec_o;           // [nE]
+    const uint32_t *iso_ptr;        // [nV+1]
+    const uint32_t *iso_col;        // [nISOv]
+};
+
+}  // namespace cgb
+
+struct cgb_op {
+    int device;
+    int nS, ndirs, nF, nE, nV, nISOv, nIC, nEC, nISO, nolut;
+    int64_t n, nrows, ncols;
+    int arith;
+    int lpv;                        // lanes per voxel (1..32)
+    // device buffers (owned)
+    float *lutIC, *lutEC, *lutISO;
+    void *lutIC_r, *lutEC_r;        // reduced-precision LUT copies
+    int lut_r_kind;                 // CGB_ARITH_BF16 / CGB_ARITH_FP16 / 0
+    __half *seg_l16;
+    uint32_t *vox_ptr, *seg_f, *eval, *fib_ptr, *fib_perm, *ec_ptr, *ec_col, *iso_ptr, *iso_col;
+    uint16_t *seg_o, *ec_o;
+    float *seg_l;
+    double *scratch;                // [nIC*n] per-segment adjoint terms (FP64 path)
+    float *scratch32;               // [nIC*n] per-segment adjoint terms (FP32 path), on demand
+    double *partials;               // block partial sums
+    double *dscal;                  // device scalars
+    double *h_scal;                 // pinned host scalars
+    double *d_in, *d_out;           // staging for cgb_op_apply_host
+    int64_t d_in_len, d_out_len;
+    size_t bytes;
+    int nsm;
+    cgb::OpDev dev() const;
+};
+
+namespace cgb {
+// operator launches (operator.cu); `grid` returns the number of blocks that wrote partials
+int launch_forward(cgb_op *op, const double *x, double *y, cudaStream_t st, int arith);
+int launch_adjoint(cgb_op *op, const double *y, double *x, cudaStream_t st, int arith);
+// |sqw*(A x - y)|^2 partial sums (y, sqw may be null); ax_out (optional) receives A x
+int launch_resnorm_grid(cgb_op *op, const double *x, const double *y, const double *sqw, double *partials,
+                        double *ax_out, cudaStream_t st, int arith, int *grid);
+// grad = A'(sqw * r), r = sqw*(A x - y), |r|^2 partial sums; with ax_a non-null, A x is
+// taken as ca*ax_a + cb*ax_b instead of being recomputed
+int launch_gradient_grid(cgb_op *op, const double *x, const double *y, const double *sqw, double *grad,
+                         double *partials, const double *ax_a, const double *ax_b, double ca, double cb,
+                         cudaStream_t st, int arith, int *grid);
+int reduction_blocks(const cgb_op *op);
+}  // namespace cgb

@@ -1,0 +1,747 @@
+// FISTA solver (commit/solvers.py:244-391) and proximal maps (commit/proximals.pyx:13-186)
+// on the device.
+//
+// One solver iteration is: the smooth + proximal step fused into one elementwise pass
+// (x = prox(xhat - step*grad, step), per-compartment maps of init_regularisation,
+// solvers.py:16-206), the group-lasso prox as level-scheduled warp-per-group passes, one
+// statistics pass giving <x-xhat,grad>, |x-xhat|^2, |x-prev_x|^2, |x|^2 and the l1 parts
+// of Omega, the objective pass |sqrt(W)(A x - y)|^2 (voxel kernel with a norm epilogue,
+// no y-sized write), and after the stopping tests the momentum pass and the fused
+// gradient pass (A xhat - y formed per voxel in registers and fed straight into the
+// adjoint).  All reductions are two-level (per block, then one block per quantity) in a
+// fixed order, so a run is bitwise reproducible.  The host only reads back a handful of
+// FP64 scalars once per objective evaluation to take the backtracking and stopping
+// decisions exactly as the reference does.
+#include <math.h>
+
+#include <vector>
+
+#include "cgb_internal.cuh"
+
+namespace cgb {
+namespace {
+
+constexpr int kStatSlots = 8;
+
+struct RegDev {
+    int64_t sIC, nIC, sEC, nEC, sISO, nISO;
+    int reg_ic, reg_ec, reg_iso, nn_ic, nn_ec, nn_iso;
+    double lam_ic, lam_ec, lam_iso;  // already multiplied by the prox scaling
+    const double *w;
+    int weighted_ic, weighted_iso;
+};
+
+struct L1Term {
+    int64_t a, b;      // range [a, b)
+    const double *w;   // weights or null
+};
+
+struct L1Terms {
+    L1Term t[4];
+    int n;
+};
+
+template <int NV>
+__device__ __forceinline__ void block_sum_store_n(double (&v)[NV], double *dst) {
+    __shared__ double red[NV][kBlock / 32];
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+#pragma unroll
+        for (int o = 16; o; o >>= 1) v[j] += __shfl_xor_sync(0xffffffffu, v[j], o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int j = 0; j < NV; ++j) red[j][threadIdx.x >> 5] = v[j];
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+#pragma unroll
+        for (int j = 0; j < NV; ++j) {
+            double t = threadIdx.x < kBlock / 32 ? red[j][threadIdx.x] : 0.0;
+#pragma unroll
+            for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+            if (threadIdx.x == 0) dst[j] = t;
+        }
+    }
+}
+
+__device__ __forceinline__ double soft(double v, double lam) {
+    // proximals.pyx:25-39
+    if (v > lam) return v - lam;
+    if (v < -lam) return v + lam;
+    return 0.0;
+}
+
+// x_out = prox(x_in - a*grad, s) for the elementwise parts of the regulariser
+__global__ void k_prox_elem(double *__restrict__ xo, const double *__restrict__ xi, const double *__restrict__ grad,
+                            double a, RegDev R, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double v = grad ? __dsub_rn(xi[i], __dmul_rn(a, grad[i])) : xi[i];
+        if (i >= R.sISO && i < R.sISO + R.nISO) {
+            if (R.reg_iso == CGB_REG_LASSO) v = soft(v, R.weighted_iso ? R.w[i] * R.lam_iso : R.lam_iso);
+            if (R.nn_iso && v <= 0.0) v = 0.0;
+        } else if (i >= R.sEC && i < R.sEC + R.nEC) {
+            if (R.reg_ec == CGB_REG_LASSO) v = soft(v, R.lam_ec);
+            if (R.nn_ec && v <= 0.0) v = 0.0;
+        } else if (i >= R.sIC && i < R.sIC + R.nIC) {
+            if (R.reg_ic == CGB_REG_LASSO || R.reg_ic == CGB_REG_SPARSE_GROUP_LASSO)
+                v = soft(v, R.weighted_ic ? R.w[i] * R.lam_ic : R.lam_ic);
+            if (R.nn_ic && (R.reg_ic == CGB_REG_NONE || R.reg_ic == CGB_REG_LASSO) && v <= 0.0) v = 0.0;
+        }
+        xo[i] = v;
+    }
+}
+
+__global__ void k_nonneg(double *__restrict__ x, int64_t a, int64_t b) {
+    for (int64_t i = a + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < b; i += (int64_t)gridDim.x * blockDim.x)
+        if (x[i] <= 0.0) x[i] = 0.0;
+}
+
+__global__ void k_soft(double *__restrict__ x, const double *__restrict__ w, double lam, int64_t a, int64_t b) {
+    for (int64_t i = a + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < b; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] = soft(x[i], w ? w[i] * lam : lam);
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// proximals.pyx:103-134 for the pairwise-disjoint groups [g0, g1): warp per group
+__global__ void k_group_prox(double *__restrict__ x, int64_t nx, const int32_t *__restrict__ gidx,
+                             const int64_t *__restrict__ gptr, const double *__restrict__ gw, int64_t g0, int64_t g1,
+                             double lam) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t g = g0 + warp; g < g1; g += nw) {
+        const int64_t beg = gptr[g], end = gptr[g + 1];
+        double s = 0.0;
+        for (int64_t k = beg + lane; k < end; k += 32) {
+            const int64_t i = gidx[k];
+            const double v = (i >= 0 && i < nx) ? x[i] : 0.0;
+            s = fma(v, v, s);
+        }
+        s = warp_sum(s);
+        const double gn = sqrt(s);
+        const double wl = gw[g] * lam;
+        if (gn <= wl) {
+            for (int64_t k = beg + lane; k < end; k += 32) {
+                const int64_t i = gidx[k];
+                if (i >= 0 && i < nx) x[i] = 0.0;
+            }
+        } else {
+            const double f = (gn - wl) / gn;
+            for (int64_t k = beg + lane; k < end; k += 32) {
+                const int64_t i = gidx[k];
+                if (i >= 0 && i < nx) x[i] *= f;
+            }
+        }
+    }
+}
+
+// per-group w_g*|x_g| (proximals.pyx:80-99), reduced per block into partials slot 0
+__global__ void k_group_norms(const double *__restrict__ x, int64_t nx, const int32_t *__restrict__ gidx,
+                              const int64_t *__restrict__ gptr, const double *__restrict__ gw, int64_t G,
+                              double *__restrict__ partials) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    double acc = 0.0;
+    for (int64_t g = warp; g < G; g += nw) {
+        double s = 0.0;
+        for (int64_t k = gptr[g] + lane; k < gptr[g + 1]; k += 32) {
+            const int64_t i = gidx[k];
+            const double v = (i >= 0 && i < nx) ? x[i] : 0.0;
+            s = fma(v, v, s);
+        }
+        s = warp_sum(s);
+        if (lane == 0) acc += gw[g] * sqrt(s);
+    }
+    double v[1] = {acc};
+    block_sum_store_n<1>(v, partials + (size_t)blockIdx.x * kRedSlots);
+}
+
+// FISTA statistics: slots 0 <x-xh,g>, 1 |x-xh|^2, 2 |x-p|^2, 3 |x|^2, 4.. l1 terms
+__global__ void k_stats(const double *__restrict__ x, const double *__restrict__ xh, const double *__restrict__ g,
+                        const double *__restrict__ p, int64_t n, L1Terms T, double *__restrict__ partials) {
+    double v[kStatSlots] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double xi = x[i];
+        if (xh) {
+            const double d = xi - xh[i];
+            v[0] = fma(d, g[i], v[0]);
+            v[1] = fma(d, d, v[1]);
+        }
+        if (p) {
+            const double e = xi - p[i];
+            v[2] = fma(e, e, v[2]);
+        }
+        v[3] = fma(xi, xi, v[3]);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k < T.n && i >= T.t[k].a && i < T.t[k].b) v[4 + k] += fabs(T.t[k].w ? T.t[k].w[i] * xi : xi);
+    }
+    block_sum_store_n<kStatSlots>(v, partials + (size_t)blockIdx.x * kRedSlots);
+}
+
+__global__ void k_dot(const double *__restrict__ a, const double *__restrict__ b, int64_t n,
+                      double *__restrict__ partials) {
+    double v[1] = {0.0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        v[0] = fma(a[i], b[i], v[0]);
+    block_sum_store_n<1>(v, partials + (size_t)blockIdx.x * kRedSlots);
+}
+
+__global__ void k_scale_range(double *__restrict__ x, int64_t a, int64_t b, double f) {
+    for (int64_t i = a + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < b; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] = f == 0.0 ? 0.0 : x[i] * f;
+}
+
+// out[j] = sum over blocks of partials[b*kRedSlots + j], j = blockIdx.x, fixed order
+__global__ void k_finalize(const double *__restrict__ partials, int nblocks, double *__restrict__ out) {
+    double v[1] = {0.0};
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) v[0] += partials[(size_t)b * kRedSlots + blockIdx.x];
+    double tmp[1];
+    block_sum_store_n<1>(v, tmp);
+    if (threadIdx.x == 0) out[blockIdx.x] = tmp[0];
+}
+
+// xhat = x + c*(x - prev); prev = x
+__global__ void k_momentum(double *__restrict__ xh, const double *__restrict__ x, double *__restrict__ p, double c,
+                           int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double xi = x[i];
+        xh[i] = __dadd_rn(xi, __dmul_rn(c, __dsub_rn(xi, p[i])));
+        p[i] = xi;
+    }
+}
+
+int elem_grid(const cgb_op *op, int64_t n) {
+    int64_t g = (n + kBlock - 1) / kBlock;
+    const int64_t cap = (int64_t)op->nsm * 4;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+int finalize(const double *partials, int nblocks, int nslots, double *out, cudaStream_t st) {
+    k_finalize<<<nslots, kBlock, 0, st>>>(partials, nblocks, out);
+    CGB_CUDA(cudaGetLastError());
+    return CGB_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ solver workspace
+struct FistaWS {
+    int64_t ncols = 0, nrows = 0;
+    double *xhat = nullptr, *prev = nullptr, *grad = nullptr, *ax[2] = {nullptr, nullptr};
+    double *pstats = nullptr, *pgrp = nullptr, *pres = nullptr;
+    ~FistaWS() {
+        double *ps[] = {xhat, prev, grad, ax[0], ax[1], pstats, pgrp, pres};
+        for (double *p : ps)
+            if (p) cudaFree(p);
+    }
+};
+
+namespace {
+
+int ws_alloc(double **p, size_t n) {
+    CGB_CUDA(cudaMalloc((void **)p, (n ? n : 1) * sizeof(double)));
+    return CGB_OK;
+}
+
+struct Solver {
+    cgb_op *op;
+    const double *y, *sqw;
+    const cgb_reg *reg;
+    const cgb_fista_params *prm;
+    cudaStream_t st;
+    FistaWS ws;
+    L1Terms terms;
+    double l1coef[4];
+    int has_group_prox = 0, group_in_omega = 0;
+    double group_omega_coef = 0.0;
+    int calls = 0;
+
+    int init() {
+        const int64_t nc = op->ncols, nr = op->nrows;
+        const int rb = reduction_blocks(op);
+        CGB_TRY(ws_alloc(&ws.xhat, nc));
+        CGB_TRY(ws_alloc(&ws.prev, nc));
+        CGB_TRY(ws_alloc(&ws.grad, nc));
+        if (prm->momentum_reuse) {
+            CGB_TRY(ws_alloc(&ws.ax[0], nr));
+            CGB_TRY(ws_alloc(&ws.ax[1], nr));
+        }
+        CGB_TRY(ws_alloc(&ws.pstats, (size_t)rb * kRedSlots));
+        CGB_TRY(ws_alloc(&ws.pgrp, (size_t)rb * kRedSlots));
+        CGB_TRY(ws_alloc(&ws.pres, (size_t)rb * kRedSlots));
+        // l1 parts of Omega with the reference's slicing (solvers.py:68, 150, 183)
+        terms.n = 0;
+        auto clamp = [&](int64_t v) { return v < 0 ? 0 : (v > nc ? nc : v); };
+        auto add = [&](int64_t a, int64_t b, const double *w, double c) {
+            a = clamp(a);
+            b = clamp(b);
+            if (b <= a || c == 0.0) return;
+            terms.t[terms.n] = L1Term{a, b, w};
+            l1coef[terms.n] = c;
+            terms.n++;
+        };
+        const cgb_reg &R = *reg;
+        if (R.reg_ic == CGB_REG_LASSO) {
+            // x[startIC:sizeIC]
+            add(R.start_ic, R.size_ic, R.weighted_ic ? R.coeff_weights : nullptr, R.lambda_ic);
+        } else if (R.reg_ic == CGB_REG_SPARSE_GROUP_LASSO) {
+            // whole x (proximals.pyx:150, 177-178); weighted with all_coeff_weights
+            if (R.lambda_ic != 0.0 || R.lambda_ic_group != 0.0)
+                add(0, nc, R.weighted_ic ? R.coeff_weights : nullptr, R.lambda_ic);
+        }
+        if (R.reg_ec == CGB_REG_LASSO) add(R.start_ec, R.start_ec + R.size_ec, nullptr, R.lambda_ec);
+        if (R.reg_iso == CGB_REG_LASSO) {
+            if (R.weighted_iso) add(R.start_iso, R.size_iso, R.coeff_weights, R.lambda_iso);  // [startISO:sizeISO]
+            else add(R.start_iso, R.start_iso + R.size_iso, nullptr, R.lambda_iso);
+        }
+        if (R.reg_ic == CGB_REG_GROUP_LASSO || R.reg_ic == CGB_REG_SPARSE_GROUP_LASSO) {
+            const double lg = R.reg_ic == CGB_REG_GROUP_LASSO ? R.lambda_ic : R.lambda_ic_group;
+            has_group_prox = R.ngroups > 0;
+            if (R.reg_ic == CGB_REG_GROUP_LASSO) {
+                group_in_omega = lg != 0.0;
+                group_omega_coef = lg;
+            } else {
+                group_in_omega = (R.lambda_ic != 0.0 || lg != 0.0);
+                group_omega_coef = lg;
+            }
+            if (R.ngroups > 0 && (!R.group_idx || !R.group_ptr || !R.group_w))
+                return fail(CGB_ERR_INVALID, "group arrays are NULL");
+        }
+        if ((R.weighted_ic || R.weighted_iso) && !R.coeff_weights)
+            return fail(CGB_ERR_INVALID, "weighted regulariser without coeff_weights");
+        return CGB_OK;
+    }
+
+    RegDev regdev(double s) const {
+        const cgb_reg &R = *reg;
+        RegDev d;
+        d.sIC = R.start_ic; d.nIC = R.size_ic; d.sEC = R.start_ec; d.nEC = R.size_ec;
+        d.sISO = R.start_iso; d.nISO = R.size_iso;
+        d.reg_ic = R.reg_ic; d.reg_ec = R.reg_ec; d.reg_iso = R.reg_iso;
+        d.nn_ic = R.nn_ic; d.nn_ec = R.nn_ec; d.nn_iso = R.nn_iso;
+        d.lam_ic = s * R.lambda_ic;
+        d.lam_ec = s * R.lambda_ec;
+        d.lam_iso = s * R.lambda_iso;
+        d.w = R.coeff_weights;
+        d.weighted_ic = R.weighted_ic; d.weighted_iso = R.weighted_iso;
+        return d;
+    }
+
+    // x_out = prox(x_in - a*grad, s) (grad may be null), in place allowed
+    int prox(double *xo, const double *xi, const double *grad, double a, double s) {
+        const int64_t nc = op->ncols;
+        if (nc == 0) return CGB_OK;
+        k_prox_elem<<<elem_grid(op, nc), kBlock, 0, st>>>(xo, xi, grad, a, regdev(s), nc);
+        CGB_CUDA(cudaGetLastError());
+        const cgb_reg &R = *reg;
+        if (has_group_prox) {
+            const double lam = s * (R.reg_ic == CGB_REG_GROUP_LASSO ? R.lambda_ic : R.lambda_ic_group);
+            if (lam != 0.0) {
+                for (int64_t k = 0; k < R.nlevels; ++k) {
+                    const int64_t g0 = R.level_ptr[k], g1 = R.level_ptr[k + 1];
+                    if (g1 <= g0) continue;
+                    int64_t blocks = ((g1 - g0) * 32 + kBlock - 1) / kBlock;
+                    if (blocks > op->nsm * 8) blocks = op->nsm * 8;
+                    k_group_prox<<<(int)blocks, kBlock, 0, st>>>(xo, op->ncols, R.group_idx, R.group_ptr, R.group_w, g0, g1,
+                                                                lam);
+                    CGB_CUDA(cudaGetLastError());
+                }
+            }
+        }
+        if (R.nn_ic && (R.reg_ic == CGB_REG_GROUP_LASSO || R.reg_ic == CGB_REG_SPARSE_GROUP_LASSO) && R.size_ic > 0) {
+            k_nonneg<<<elem_grid(op, R.size_ic), kBlock, 0, st>>>(xo, R.start_ic, R.start_ic + R.size_ic);
+            CGB_CUDA(cudaGetLastError());
+        }
+        return CGB_OK;
+    }
+
+    // statistics of x (and omega pieces) into dscal[1..8], group omega into dscal[9]
+    int stats(const double *x, const double *xh, const double *g, const double *p) {
+        const int64_t nc = op->ncols;
+        const int gb = elem_grid(op, nc);
+        k_stats<<<gb, kBlock, 0, st>>>(x, xh, g, p, nc, terms, ws.pstats);
+        CGB_CUDA(cudaGetLastError());
+        CGB_TRY(finalize(ws.pstats, gb, kStatSlots, op->dscal + 1, st));
+        if (group_in_omega) {
+            int64_t blocks = (reg->ngroups * 32 + kBlock - 1) / kBlock;
+            if (blocks > op->nsm * 4) blocks = op->nsm * 4;
+            if (blocks < 1) blocks = 1;
+            k_group_norms<<<(int)blocks, kBlock, 0, st>>>(x, op->ncols, reg->group_idx, reg->group_ptr, reg->group_w,
+                                                         reg->ngroups, ws.pgrp);
+            CGB_CUDA(cudaGetLastError());
+            CGB_TRY(finalize(ws.pgrp, (int)blocks, 1, op->dscal + 9, st));
+        } else {
+            CGB_CUDA(cudaMemsetAsync(op->dscal + 9, 0, sizeof(double), st));
+        }
+        return CGB_OK;
+    }
+
+    double omega_from(const double *h) const {
+        double om = 0.0;
+        for (int k = 0; k < terms.n; ++k) om += l1coef[k] * h[5 + k];
+        if (group_in_omega) om += group_omega_coef * h[9];
+        return om;
+    }
+
+    // |sqw*(A x - y)|^2 -> dscal[0]; optionally A x -> ax
+    int objective(const double *x, double *ax) {
+        int g = 0;
+        CGB_TRY(launch_resnorm_grid(op, x, y, sqw, op->partials, ax, st, prm->arith, &g));
+        calls++;
+        if (g > 0) {
+            CGB_TRY(finalize(op->partials, g, 1, op->dscal + 0, st));
+        } else {
+            CGB_CUDA(cudaMemsetAsync(op->dscal, 0, sizeof(double), st));
+        }
+        return CGB_OK;
+    }
+
+    // grad = A'(W (A x - y)) (or from the A x combination), |r|^2 -> dscal[10]
+    int gradient(const double *x, double *grad, const double *ax_a, const double *ax_b, double ca, double cb) {
+        int g = 0;
+        CGB_TRY(launch_gradient_grid(op, x, y, sqw, grad, ws.pres, ax_a, ax_b, ca, cb, st, prm->arith, &g));
+        calls += ax_a ? 1 : 2;
+        if (g > 0) {
+            CGB_TRY(finalize(ws.pres, g, 1, op->dscal + 10, st));
+        } else {
+            CGB_CUDA(cudaMemsetAsync(op->dscal + 10, 0, sizeof(double), st));
+        }
+        return CGB_OK;
+    }
+
+    int fetch(double *h) {
+        CGB_CUDA(cudaMemcpyAsync(h, op->dscal, 16 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CGB_CUDA(cudaStreamSynchronize(st));
+        return CGB_OK;
+    }
+
+    int run(double *x, cgb_fista_result *res) {
+        const int64_t nc = op->ncols;
+        const double eps = 2.220446049250313e-16;
+        double *h = op->h_scal;
+        const double beta = 0.9;
+        int backtracks = 0;
+        // initialisation (solvers.py:260-286)
+        CGB_CUDA(cudaMemcpyAsync(ws.xhat, x, nc * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        CGB_TRY(gradient(ws.xhat, ws.grad, nullptr, nullptr, 0.0, 0.0));
+        CGB_TRY(prox(ws.xhat, ws.xhat, nullptr, 0.0, 1.0));
+        CGB_TRY(stats(ws.xhat, nullptr, nullptr, nullptr));
+        CGB_TRY(fetch(h));
+        double res_norm = sqrt(h[10]);
+        double reg_term = omega_from(h);
+        double prev_obj = 0.5 * res_norm * res_norm + reg_term;
+        double told = 1.0;
+        CGB_CUDA(cudaMemcpyAsync(ws.prev, ws.xhat, nc * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        double qfval = prev_obj;
+        // step size from one Rayleigh quotient of grad (solvers.py:282-286)
+        {
+            int g = 0;
+            k_dot<<<elem_grid(op, nc), kBlock, 0, st>>>(ws.grad, ws.grad, nc, ws.pstats);
+            CGB_CUDA(cudaGetLastError());
+            CGB_TRY(finalize(ws.pstats, elem_grid(op, nc), 1, op->dscal + 11, st));
+            CGB_TRY(launch_resnorm_grid(op, ws.grad, nullptr, sqw, op->partials, nullptr, st, prm->arith, &g));
+            calls++;
+            if (g > 0) {
+                CGB_TRY(finalize(op->partials, g, 1, op->dscal + 12, st));
+            } else {
+                CGB_CUDA(cudaMemsetAsync(op->dscal + 12, 0, sizeof(double), st));
+            }
+            CGB_TRY(fetch(h));
+        }
+        const double Ln = sqrt(h[12]) / sqrt(h[11]);
+        const double L = Ln * Ln;
+        double step = 1.9 / L;
+        if (prm->verbose == 4) {
+            printf("\n      |  1/2||Ax-y||^2      Omega      |  Cost function    Abs error      Rel error    |"
+                   "      Abs x          Rel x    \n");
+            printf("------|--------------------------------|-----------------------------------------------|"
+                   "------------------------------\n");
+        }
+        int it = 1;
+        int cur = 0;          // ax buffer written by objective(x)
+        int have_prev_ax = 0; // ax[1-cur] holds A*prev_x
+        double curr_obj = 0, reg_term_x = 0, abs_obj = 0, rel_obj = 0, abs_x = 0, rel_x = 0;
+        int crit = 4;
+        while (true) {
+            auto eval_x = [&](double s) -> int {
+                CGB_TRY(prox(x, ws.xhat, ws.grad, s, s));
+                CGB_TRY(stats(x, ws.xhat, ws.grad, ws.prev));
+                CGB_TRY(objective(x, prm->momentum_reuse ? ws.ax[cur] : nullptr));
+                return fetch(h);
+            };
+            CGB_TRY(eval_x(step));
+            qfval = 0.5 * sqrt(h[10]) * sqrt(h[10]);
+            if (it == 1) qfval = prev_obj;
+            reg_term_x = omega_from(h);
+            double q = qfval + h[1] + 0.5 / step * (sqrt(h[2]) * sqrt(h[2])) + reg_term_x;
+            res_norm = sqrt(h[0]);
+            curr_obj = 0.5 * res_norm * res_norm + reg_term_x;
+            while (curr_obj > q) {
+                step = beta * step;
+                backtracks++;
+                CGB_TRY(eval_x(step));
+                reg_term_x = omega_from(h);
+                q = qfval + h[1] + 0.5 / step * (sqrt(h[2]) * sqrt(h[2])) + reg_term_x;
+                res_norm = sqrt(h[0]);
+                curr_obj = 0.5 * res_norm * res_norm + reg_term_x;
+            }
+            abs_obj = fabs(curr_obj - prev_obj);
+            rel_obj = abs_obj / curr_obj;
+            abs_x = sqrt(h[3]);
+            rel_x = abs_x / (sqrt(h[4]) + eps);
+            if (prm->verbose == 4)
+                printf("%4d  |  %13.7e  %13.7e  |  %13.7e  %13.7e  %13.7e  |  %13.7e  %13.7e\n", it,
+                       0.5 * res_norm * res_norm, reg_term_x, curr_obj, abs_obj, rel_obj, abs_x, rel_x);
+            if (abs_obj < eps) { crit = 0; break; }
+            if (rel_obj < prm->tol_fun) { crit = 1; break; }
+            if (abs_x < eps) { crit = 2; break; }
+            if (rel_x < prm->tol_x) { crit = 3; break; }
+            if (it >= prm->max_iter) { crit = 4; break; }
+            // FISTA update (solvers.py:359-368)
+            const double t = 0.5 * (1.0 + sqrt(1.0 + 4.0 * told * told));
+            const double c = (told - 1.0) / t;
+            k_momentum<<<elem_grid(op, nc), kBlock, 0, st>>>(ws.xhat, x, ws.prev, c, nc);
+            CGB_CUDA(cudaGetLastError());
+            if (prm->momentum_reuse && (c == 0.0 || have_prev_ax)) {
+                // A*xhat = (1+c) A*x - c A*prev_x
+                CGB_TRY(gradient(ws.xhat, ws.grad, ws.ax[cur], have_prev_ax ? ws.ax[1 - cur] : ws.ax[cur], 1.0 + c,
+                                 -c));
+            } else {
+                CGB_TRY(gradient(ws.xhat, ws.grad, nullptr, nullptr, 0.0, 0.0));
+            }
+            if (prm->momentum_reuse) {
+                cur = 1 - cur;
+                have_prev_ax = 1;
+            }
+            it += 1;
+            prev_obj = curr_obj;
+            told = t;
+        }
+        if (prm->verbose == 4) {
+            static const char *names[] = {"Absolute tolerance on the objective", "Relative tolerance on the objective",
+                                          "Absolute tolerance on the unknowns", "Relative tolerance on the unknowns",
+                                          "Maximum number of iterations"};
+            printf("< Stopping criterion: %s >\n", names[crit]);
+        }
+        res->residual = 0.5 * res_norm * res_norm;
+        res->regterm = reg_term_x;
+        res->cost_function = curr_obj;
+        res->abs_cost = abs_obj;
+        res->rel_cost = rel_obj;
+        res->abs_x = abs_x;
+        res->rel_x = rel_x;
+        res->iterations = it;
+        res->stopping_criterion = crit;
+        res->backtracks = backtracks;
+        res->operator_calls = calls;
+        CGB_CUDA(cudaStreamSynchronize(st));
+        return CGB_OK;
+    }
+};
+
+}  // namespace
+}  // namespace cgb
+
+using namespace cgb;
+
+struct DevGuard {
+    int prev = -1;
+    explicit DevGuard(int d) {
+        cudaGetDevice(&prev);
+        if (prev != d) cudaSetDevice(d);
+    }
+    ~DevGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+extern "C" {
+
+int cgb_fista_run(cgb_op *op, const double *y, const double *sqrt_w, const cgb_reg *reg,
+                  const cgb_fista_params *params, double *x, cgb_fista_result *result, void *stream) {
+    if (!op || !y || !reg || !params || !x || !result) return fail(CGB_ERR_INVALID, "null argument");
+    if (params->arith != CGB_ARITH_F64 && params->arith != CGB_ARITH_FF)
+        return fail(CGB_ERR_INVALID, "FISTA arith must be F64 or FF");
+    if (reg->reg_ec > CGB_REG_LASSO || reg->reg_iso > CGB_REG_LASSO)
+        return fail(CGB_ERR_INVALID, "EC/ISO regularisers must be none or lasso");
+    if ((reg->reg_ic == CGB_REG_GROUP_LASSO || reg->reg_ic == CGB_REG_SPARSE_GROUP_LASSO) && reg->ngroups > 0 &&
+        (!reg->level_ptr || reg->nlevels < 1))
+        return fail(CGB_ERR_INVALID, "group regulariser needs a level schedule");
+    DevGuard g(op->device);
+    Solver S;
+    S.op = op;
+    S.y = y;
+    S.sqw = sqrt_w;
+    S.reg = reg;
+    S.prm = params;
+    S.st = (cudaStream_t)stream;
+    CGB_TRY(S.init());
+    return S.run(x, result);
+}
+
+// ------------------------------------------------------------------ standalone proximal maps
+static int grid_n(int64_t n) {
+    int64_t g = (n + kBlock - 1) / kBlock;
+    if (g > 4096) g = 4096;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+int cgb_prox_non_negativity(double *x, int64_t start, int64_t size, void *stream) {
+    if (size <= 0) return CGB_OK;
+    if (!x || start < 0) return fail(CGB_ERR_INVALID, "bad argument");
+    k_nonneg<<<grid_n(size), kBlock, 0, (cudaStream_t)stream>>>(x, start, start + size);
+    CGB_CUDA(cudaGetLastError());
+    return CGB_OK;
+}
+
+int cgb_prox_soft_thresholding(double *x, double lam, int64_t start, int64_t size, void *stream) {
+    if (size <= 0) return CGB_OK;
+    if (!x || start < 0) return fail(CGB_ERR_INVALID, "bad argument");
+    k_soft<<<grid_n(size), kBlock, 0, (cudaStream_t)stream>>>(x, nullptr, lam, start, start + size);
+    CGB_CUDA(cudaGetLastError());
+    return CGB_OK;
+}
+
+int cgb_prox_w_soft_thresholding(double *x, const double *w, double lam, int64_t start, int64_t size,
+                                 void *stream) {
+    if (size <= 0) return CGB_OK;
+    if (!x || !w || start < 0) return fail(CGB_ERR_INVALID, "bad argument");
+    k_soft<<<grid_n(size), kBlock, 0, (cudaStream_t)stream>>>(x, w, lam, start, start + size);
+    CGB_CUDA(cudaGetLastError());
+    return CGB_OK;
+}
+
+static int sum_sq_range(const double *x, int64_t start, int64_t size, double *out, cudaStream_t st) {
+    const int g = grid_n(size) > 1024 ? 1024 : grid_n(size);
+    double *part = nullptr, *dres = nullptr;
+    CGB_CUDA(cudaMallocAsync((void **)&part, (size_t)g * kRedSlots * sizeof(double), st));
+    CGB_CUDA(cudaMallocAsync((void **)&dres, sizeof(double), st));
+    k_dot<<<g, kBlock, 0, st>>>(x + start, x + start, size, part);
+    k_finalize<<<1, kBlock, 0, st>>>(part, g, dres);
+    cudaError_t e = cudaMemcpyAsync(out, dres, sizeof(double), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    cudaFreeAsync(part, st);
+    cudaFreeAsync(dres, st);
+    CGB_CUDA(e);
+    CGB_CUDA(cudaGetLastError());
+    return CGB_OK;
+}
+
+int cgb_prox_projection_onto_l2_ball(double *x, double lam, int64_t start, int64_t size, void *stream) {
+    // proximals.pyx:59-77
+    if (size <= 0) return CGB_OK;
+    if (!x || start < 0) return fail(CGB_ERR_INVALID, "bad argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    double s2 = 0.0;
+    CGB_TRY(sum_sq_range(x, start, size, &s2, st));
+    const double xn = sqrt(s2);
+    const double f = xn > lam ? 1.0 - lam / xn : 0.0;
+    k_scale_range<<<grid_n(size), kBlock, 0, st>>>(x, start, start + size, f);
+    CGB_CUDA(cudaGetLastError());
+    return CGB_OK;
+}
+
+int cgb_prox_group_lasso(double *x, int64_t nx, const int32_t *group_idx, const int64_t *group_ptr, const double *group_w,
+                         int64_t ngroups, const int64_t *level_ptr, int64_t nlevels, double lam, void *stream) {
+    if (lam == 0.0 || ngroups <= 0) return CGB_OK;
+    if (!x || !group_idx || !group_ptr || !group_w || !level_ptr) return fail(CGB_ERR_INVALID, "bad argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    for (int64_t k = 0; k < nlevels; ++k) {
+        const int64_t g0 = level_ptr[k], g1 = level_ptr[k + 1];
+        if (g1 <= g0) continue;
+        int64_t blocks = ((g1 - g0) * 32 + kBlock - 1) / kBlock;
+        if (blocks > 4096) blocks = 4096;
+        k_group_prox<<<(int)blocks, kBlock, 0, st>>>(x, nx, group_idx, group_ptr, group_w, g0, g1, lam);
+        CGB_CUDA(cudaGetLastError());
+    }
+    return CGB_OK;
+}
+
+static int group_omega(const double *x, int64_t nx, const int32_t *gidx, const int64_t *gptr, const double *gw, int64_t G,
+                       double *out, cudaStream_t st) {
+    int64_t blocks = (G * 32 + kBlock - 1) / kBlock;
+    if (blocks > 1024) blocks = 1024;
+    if (blocks < 1) blocks = 1;
+    double *part = nullptr, *dres = nullptr;
+    CGB_CUDA(cudaMallocAsync((void **)&part, (size_t)blocks * kRedSlots * sizeof(double), st));
+    CGB_CUDA(cudaMallocAsync((void **)&dres, sizeof(double), st));
+    k_group_norms<<<(int)blocks, kBlock, 0, st>>>(x, nx, gidx, gptr, gw, G, part);
+    k_finalize<<<1, kBlock, 0, st>>>(part, (int)blocks, dres);
+    cudaError_t e = cudaMemcpyAsync(out, dres, sizeof(double), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    cudaFreeAsync(part, st);
+    cudaFreeAsync(dres, st);
+    CGB_CUDA(e);
+    CGB_CUDA(cudaGetLastError());
+    return CGB_OK;
+}
+
+int cgb_omega_group_lasso(const double *x, int64_t nx, const int32_t *group_idx, const int64_t *group_ptr,
+                          const double *group_w, int64_t ngroups, double lam, double *out, void *stream) {
+    if (!out) return fail(CGB_ERR_INVALID, "out is NULL");
+    *out = 0.0;
+    if (lam == 0.0 || ngroups <= 0) return CGB_OK;
+    double s = 0.0;
+    CGB_TRY(group_omega(x, nx, group_idx, group_ptr, group_w, ngroups, &s, (cudaStream_t)stream));
+    *out = lam * s;
+    return CGB_OK;
+}
+
+static int l1_sum(const double *x, const double *w, int64_t a, int64_t b, double *out, cudaStream_t st) {
+    *out = 0.0;
+    if (b <= a) return CGB_OK;
+    const int g = grid_n(b - a) > 1024 ? 1024 : grid_n(b - a);
+    double *part = nullptr, *dres = nullptr;
+    CGB_CUDA(cudaMallocAsync((void **)&part, (size_t)g * kRedSlots * sizeof(double), st));
+    CGB_CUDA(cudaMallocAsync((void **)&dres, 8 * sizeof(double), st));
+    L1Terms T;
+    T.n = 1;
+    T.t[0] = L1Term{a, b, w};
+    k_stats<<<g, kBlock, 0, st>>>(x, nullptr, nullptr, nullptr, b, T, part);
+    k_finalize<<<kStatSlots, kBlock, 0, st>>>(part, g, dres);
+    double h[8];
+    cudaError_t e = cudaMemcpyAsync(h, dres, 8 * sizeof(double), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    cudaFreeAsync(part, st);
+    cudaFreeAsync(dres, st);
+    CGB_CUDA(e);
+    CGB_CUDA(cudaGetLastError());
+    *out = h[4];
+    return CGB_OK;
+}
+
+int cgb_omega_l1(const double *x, const double *w, int64_t start, int64_t size, double lam, double *out,
+                 void *stream) {
+    if (!out || !x) return fail(CGB_ERR_INVALID, "null argument");
+    double s = 0.0;
+    CGB_TRY(l1_sum(x, w, start, start + size, &s, (cudaStream_t)stream));
+    *out = lam * s;
+    return CGB_OK;
+}
+
+int cgb_omega_sparse_group_lasso(const double *x, int64_t nx, const double *w, const int32_t *group_idx,
+                                 const int64_t *group_ptr, const double *group_w, int64_t ngroups, double lam1,
+                                 double lam2, double *out, void *stream) {
+    if (!out || !x) return fail(CGB_ERR_INVALID, "null argument");
+    *out = 0.0;
+    if (lam1 == 0.0 && lam2 == 0.0) return CGB_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    double o1 = 0.0, o2 = 0.0;
+    CGB_TRY(l1_sum(x, w, 0, nx, &o1, st));
+    if (ngroups > 0) CGB_TRY(group_omega(x, nx, group_idx, group_ptr, group_w, ngroups, &o2, st));
+    *out = lam1 * o1 + lam2 * o2;
+    return CGB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,181 @@
+// Launch layer of the FP64-accurate operator: chooses the arithmetic policy, runs the
+// LUT-free kernels (setup_operator.py:713-915) and the per-fibre second pass of A'.
+#include "operator_kernels.cuh"
+
+namespace cgb {
+
+int forward_f64(cgb_op *op, const double *x, double *y, double *ax, const double *yobs, const double *sqw,
+                double *partials, cudaStream_t st, int *grid);
+int adjoint_f64(cgb_op *op, const double *yin, int in_mode, const double *x, const double *yobs,
+                const double *sqw, const double *ax_a, const double *ax_b, double ca, double cb, double *xout,
+                double *partials, cudaStream_t st, int *grid);
+int forward_ff(cgb_op *op, const double *x, double *y, double *ax, const double *yobs, const double *sqw,
+               double *partials, cudaStream_t st, int *grid);
+int adjoint_ff(cgb_op *op, const double *yin, int in_mode, const double *x, const double *yobs,
+               const double *sqw, const double *ax_a, const double *ax_b, double ca, double cb, double *xout,
+               double *partials, cudaStream_t st, int *grid);
+
+namespace detail {
+// second A' pass: per-fibre sums of the voxel-ordered segment terms
+__global__ void k_fibre_sum(const OpDev P, const double *__restrict__ scratch, double *__restrict__ xout) {
+    const int64_t total = (int64_t)P.nF * P.nIC;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(q / P.nF);
+        const uint32_t f = (uint32_t)(q - (int64_t)i * P.nF);
+        const uint32_t beg = P.fib_ptr[f], end = P.fib_ptr[f + 1];
+        const double *S = scratch + (size_t)i * P.n;
+        double s = 0.0;
+        for (uint32_t k = beg; k < end; ++k) s += S[P.fib_perm[k]];
+        xout[q] = s * (double)P.eval[q];
+    }
+}
+
+// ------------------------------------------------------------------ LUT-free operator (nS == 1)
+__global__ void k_forward_nolut(const OpDev P, const double *__restrict__ x, double *__restrict__ yout,
+                                double *__restrict__ axout, const double *__restrict__ yobs,
+                                const double *__restrict__ sqw, double *__restrict__ partials) {
+    double nrm = 0.0;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < P.nV; v += gridDim.x * blockDim.x) {
+        double a = 0.0;
+        if (P.nIC > 0)
+            for (uint32_t j = P.vox_ptr[v]; j < P.vox_ptr[v + 1]; ++j) {
+                const uint32_t f = P.seg_f[j];
+                const double x0 = x[f] * (double)P.eval[f];
+                if (x0 != 0) a += (double)P.seg_l[j] * x0;
+            }
+        if (P.nISO > 0)
+            for (uint32_t j = P.iso_ptr[v]; j < P.iso_ptr[v + 1]; ++j) {
+                const double x0 = x[P.iso_base + P.iso_col[j]];
+                if (x0 != 0) a += x0;
+            }
+        if (yout) yout[v] = a;
+        if (axout) axout[v] = a;
+        if (partials) {
+            double r = yobs ? a - yobs[v] : a;
+            if (sqw) r *= sqw[v];
+            nrm = fma(r, r, nrm);
+        }
+    }
+    if (partials) block_sum_store(nrm, partials + (size_t)blockIdx.x * kRedSlots);
+}
+
+__global__ void k_adjoint_nolut(const OpDev P, const double *__restrict__ yin, int in_mode,
+                                const double *__restrict__ x, const double *__restrict__ yobs,
+                                const double *__restrict__ sqw, const double *__restrict__ ax_a,
+                                const double *__restrict__ ax_b, double ca, double cb, double *__restrict__ scratch,
+                                double *__restrict__ xout, double *__restrict__ partials) {
+    double nrm = 0.0;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < P.nV; v += gridDim.x * blockDim.x) {
+        double z;
+        if (in_mode == 0) {
+            z = yin[v];
+        } else {
+            double a = 0.0;
+            if (in_mode == 1) {
+                if (P.nIC > 0)
+                    for (uint32_t j = P.vox_ptr[v]; j < P.vox_ptr[v + 1]; ++j) {
+                        const uint32_t f = P.seg_f[j];
+                        const double x0 = x[f] * (double)P.eval[f];
+                        if (x0 != 0) a += (double)P.seg_l[j] * x0;
+                    }
+                if (P.nISO > 0)
+                    for (uint32_t j = P.iso_ptr[v]; j < P.iso_ptr[v + 1]; ++j) {
+                        const double x0 = x[P.iso_base + P.iso_col[j]];
+                        if (x0 != 0) a += x0;
+                    }
+            } else {
+                a = ca * ax_a[v] + cb * ax_b[v];
+            }
+            double r = a - yobs[v];
+            if (sqw) r *= sqw[v];
+            nrm = fma(r, r, nrm);
+            z = sqw ? sqw[v] * r : r;
+        }
+        if (P.nIC > 0)
+            for (uint32_t j = P.vox_ptr[v]; j < P.vox_ptr[v + 1]; ++j) scratch[j] = (double)P.seg_l[j] * z;
+        if (P.nISO > 0)
+            for (uint32_t j = P.iso_ptr[v]; j < P.iso_ptr[v + 1]; ++j) xout[P.iso_base + P.iso_col[j]] = z;
+    }
+    if (partials) block_sum_store(nrm, partials + (size_t)blockIdx.x * kRedSlots);
+}
+
+}  // namespace detail
+
+using namespace detail;
+
+int fibre_sum(cgb_op *op, double *xout, cudaStream_t st) {
+    if (op->nIC > 0 && op->nF > 0) {
+        const OpDev P = op->dev();
+        const int64_t total = (int64_t)op->nF * op->nIC;
+        int gb = (int)((total + 255) / 256);
+        if (gb > op->nsm * 16) gb = op->nsm * 16;
+        k_fibre_sum<<<gb, 256, 0, st>>>(P, op->scratch, xout);
+        CGB_CUDA(cudaGetLastError());
+    }
+    return CGB_OK;
+}
+
+static int run_forward(cgb_op *op, const double *x, double *y, double *ax, const double *yobs, const double *sqw,
+                       double *partials, cudaStream_t st, int arith, int *grid_out) {
+    if (grid_out) *grid_out = 0;
+    if (op->nV == 0) return CGB_OK;
+    if (op->nolut) {
+        const OpDev P = op->dev();
+        int g = (op->nV + kBlock - 1) / kBlock;
+        if (g > reduction_blocks(op)) g = reduction_blocks(op);
+        k_forward_nolut<<<g, kBlock, 0, st>>>(P, x, y, ax, yobs, sqw, partials);
+        CGB_CUDA(cudaGetLastError());
+        if (grid_out) *grid_out = g;
+        return CGB_OK;
+    }
+    if (arith == CGB_ARITH_F64) return forward_f64(op, x, y, ax, yobs, sqw, partials, st, grid_out);
+    return forward_ff(op, x, y, ax, yobs, sqw, partials, st, grid_out);
+}
+
+static int run_adjoint(cgb_op *op, const double *yin, int in_mode, const double *x, const double *yobs,
+                       const double *sqw, const double *ax_a, const double *ax_b, double ca, double cb, double *xout,
+                       double *partials, cudaStream_t st, int arith, int *grid_out) {
+    if (grid_out) *grid_out = 0;
+    if (op->nV == 0) {
+        if (op->ncols > 0) CGB_CUDA(cudaMemsetAsync(xout, 0, op->ncols * sizeof(double), st));
+        return CGB_OK;
+    }
+    if (op->nolut) {
+        const OpDev P = op->dev();
+        int g = (op->nV + kBlock - 1) / kBlock;
+        if (g > reduction_blocks(op)) g = reduction_blocks(op);
+        k_adjoint_nolut<<<g, kBlock, 0, st>>>(P, yin, in_mode, x, yobs, sqw, ax_a, ax_b, ca, cb, op->scratch, xout,
+                                              partials);
+        CGB_CUDA(cudaGetLastError());
+        if (grid_out) *grid_out = g;
+    } else if (arith == CGB_ARITH_F64) {
+        CGB_TRY(adjoint_f64(op, yin, in_mode, x, yobs, sqw, ax_a, ax_b, ca, cb, xout, partials, st, grid_out));
+    } else {
+        CGB_TRY(adjoint_ff(op, yin, in_mode, x, yobs, sqw, ax_a, ax_b, ca, cb, xout, partials, st, grid_out));
+    }
+    return fibre_sum(op, xout, st);
+}
+
+int launch_forward(cgb_op *op, const double *x, double *y, cudaStream_t st, int arith) {
+    return run_forward(op, x, y, nullptr, nullptr, nullptr, nullptr, st, arith, nullptr);
+}
+
+int launch_adjoint(cgb_op *op, const double *y, double *x, cudaStream_t st, int arith) {
+    return run_adjoint(op, y, 0, nullptr, nullptr, nullptr, nullptr, nullptr, 0.0, 0.0, x, nullptr, st, arith,
+                       nullptr);
+}
+
+int launch_resnorm_grid(cgb_op *op, const double *x, const double *y, const double *sqw, double *partials,
+                        double *ax_out, cudaStream_t st, int arith, int *grid) {
+    return run_forward(op, x, nullptr, ax_out, y, sqw, partials, st, arith, grid);
+}
+
+int launch_gradient_grid(cgb_op *op, const double *x, const double *y, const double *sqw, double *grad,
+                         double *partials, const double *ax_a, const double *ax_b, double ca, double cb,
+                         cudaStream_t st, int arith, int *grid) {
+    const int mode = ax_a ? 2 : 1;
+    return run_adjoint(op, nullptr, mode, x, y, sqw, ax_a, ax_b, ca, cb, grad, partials, st, arith, grid);
+}
+
+}  // namespace cgb

@@ -1,0 +1,388 @@
+#pragma once
+// A*x and A'*y kernels of the FP64-accurate path (templates; instantiated per arithmetic).
+//
+// Reference semantics: setup_operator.py:50-218 (A: COMMIT_A__block) and :370-563
+// (A': COMMIT_At__block), :713-871 (LUT-free variants).  For a voxel v with IC segments
+// (f, o, l), EC elements (o) and ISO elements:
+//   y[v,s] = sum_seg l * sum_i x[i*nF+f]*eval[i*nF+f] * LUT_IC[i,o,s]
+//          + sum_ec  sum_i x[ec_base + i*nE + e] * LUT_EC[i,o,s]
+//          + sum_iso sum_i x[iso_base + i*nISO + j] * LUT_ISO[i,s]
+//   x[i*nF+f] = eval[i*nF+f] * sum_{seg of f} l * <LUT_IC[i,o,:], y[v,:]>     (A')
+//
+// GB300 mapping.  A group of LPV lanes (a warp for long sample vectors) owns one voxel at
+// a time and each lane owns NCH samples; segment metadata is loaded cooperatively
+// (coalesced), the coefficient c = l*x*eval is formed once by the loading lane and
+// broadcast with shuffles, and every lane streams its slice of the LUT row.  Output rows
+// are written once, so A needs no zero fill and no atomics.  A' runs the same voxel pass:
+// each lane accumulates partial dot products for a batch of LPV segments, a shared-memory
+// transpose hands lane t the LPV partials of segment t, and the per-segment terms l*<L,y>
+// go to a scratch stream in voxel order; a second pass sums them per fibre through the
+// fibre-ordered index (deterministic, no atomics).  EC/ISO outputs are owned by one voxel
+// and are written directly by the first pass.
+//
+// Arithmetic.  GB300 issues FP64 FMAs at ~1/58 of the FP32 rate, so besides native FP64
+// (ArF64) the kernels run a float-float policy (ArFF): FP64 inputs are split into two
+// FP32 words, products are made exact with an FMA (two-product), sums are error-free
+// (two-sum), giving ~48-bit significands -- far inside the 1e-10 parity bound -- on the
+// FP32 pipe.  Reductions of residual norms stay in FP64.
+#include "cgb_internal.cuh"
+
+namespace cgb {
+namespace detail {
+
+// ------------------------------------------------------------------ arithmetic policies
+struct ArF64 {
+    using Acc = double;
+    using Coef = double;
+    __device__ static __forceinline__ void zero(Acc &a) { a = 0.0; }
+    __device__ static __forceinline__ Coef coef(double c) { return c; }
+    __device__ static __forceinline__ bool nz(const Coef &c) { return c != 0.0; }
+    __device__ static __forceinline__ Coef shfl(unsigned m, const Coef &c, int src, int w) {
+        return __shfl_sync(m, c, src, w);
+    }
+    __device__ static __forceinline__ void fma_(Acc &a, const Coef &c, float L) { a = fma(c, (double)L, a); }
+    __device__ static __forceinline__ void add(Acc &a, const Acc &b) { a += b; }
+    __device__ static __forceinline__ double val(const Acc &a) { return a; }
+};
+
+struct ArFF {
+    struct Acc {
+        float s, e;
+    };
+    struct Coef {
+        float h, l;
+    };
+    __device__ static __forceinline__ void zero(Acc &a) { a.s = 0.f; a.e = 0.f; }
+    __device__ static __forceinline__ Coef coef(double c) {
+        Coef r;
+        r.h = __double2float_rn(c);
+        r.l = __double2float_rn(c - (double)r.h);
+        return r;
+    }
+    __device__ static __forceinline__ bool nz(const Coef &c) { return c.h != 0.f || c.l != 0.f; }
+    __device__ static __forceinline__ Coef shfl(unsigned m, const Coef &c, int src, int w) {
+        Coef r;
+        r.h = __shfl_sync(m, c.h, src, w);
+        r.l = __shfl_sync(m, c.l, src, w);
+        return r;
+    }
+    // a += (c.h + c.l) * L with an exact two-product of the high word and a two-sum
+    __device__ static __forceinline__ void fma_(Acc &a, const Coef &c, float L) {
+        const float p = __fmul_rn(c.h, L);
+        float e = __fmaf_rn(c.h, L, -p);
+        e = __fmaf_rn(c.l, L, e);
+        const float s = __fadd_rn(a.s, p);
+        const float bb = __fsub_rn(s, a.s);
+        const float err = __fadd_rn(__fsub_rn(a.s, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+        a.s = s;
+        a.e = __fadd_rn(a.e, __fadd_rn(err, e));
+    }
+    __device__ static __forceinline__ void add(Acc &a, const Acc &b) {
+        const float s = __fadd_rn(a.s, b.s);
+        const float bb = __fsub_rn(s, a.s);
+        const float err = __fadd_rn(__fsub_rn(a.s, __fsub_rn(s, bb)), __fsub_rn(b.s, bb));
+        a.s = s;
+        a.e = __fadd_rn(a.e, __fadd_rn(b.e, err));
+    }
+    __device__ static __forceinline__ double val(const Acc &a) { return (double)a.s + (double)a.e; }
+};
+
+template <int LPV>
+struct Group {
+    int sub;
+    unsigned mask;
+    __device__ __forceinline__ Group() {
+        const int lane = threadIdx.x & 31;
+        sub = lane & (LPV - 1);
+        mask = (LPV == 32) ? 0xffffffffu : (((1u << LPV) - 1u) << (lane & ~(LPV - 1)));
+    }
+};
+
+__device__ __forceinline__ void block_sum_store(double v, double *dst) {
+    __shared__ double red[kBlock / 32];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        v = threadIdx.x < kBlock / 32 ? red[threadIdx.x] : 0.0;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) *dst = v;
+    }
+}
+
+// ------------------------------------------------------------------ forward accumulation
+// Accumulates row v of A*x into acc[NCH] (lane owns samples sub + k*LPV).
+template <int LPV, int NCH, class AR>
+__device__ __forceinline__ void forward_row(const OpDev &P, const Group<LPV> &G, int v, const double *__restrict__ x,
+                                            typename AR::Acc (&acc)[NCH]) {
+    const int nS = P.nS;
+#pragma unroll
+    for (int k = 0; k < NCH; ++k) AR::zero(acc[k]);
+    // IC segments
+    if (P.nIC > 0) {
+        const uint32_t beg = P.vox_ptr[v], end = P.vox_ptr[v + 1];
+        for (uint32_t b = beg; b < end; b += LPV) {
+            const uint32_t j = b + G.sub;
+            const bool valid = j < end;
+            uint32_t f = 0, o = 0;
+            float l = 0.f;
+            if (valid) {
+                f = P.seg_f[j];
+                o = P.seg_o[j];
+                l = P.seg_l[j];
+            }
+            const int cnt = min((int)(end - b), LPV);
+            for (int i = 0; i < P.nIC; ++i) {
+                double c = 0.0;
+                if (valid) {
+                    const size_t col = (size_t)i * P.nF + f;
+                    c = (double)l * (x[col] * (double)P.eval[col]);
+                }
+                const typename AR::Coef cf = AR::coef(c);
+                const uint32_t row = ((uint32_t)i * P.ndirs + o) * (uint32_t)nS;
+                for (int t = 0; t < cnt; ++t) {
+                    const typename AR::Coef ct = AR::shfl(G.mask, cf, t, LPV);
+                    const uint32_t rt = __shfl_sync(G.mask, row, t, LPV);
+                    if (AR::nz(ct)) {
+                        const float *L = P.lutIC + rt;
+#pragma unroll
+                        for (int k = 0; k < NCH; ++k) {
+                            const int s = G.sub + k * LPV;
+                            if (s < nS) AR::fma_(acc[k], ct, __ldg(L + s));
+                        }
+                    }
+                }
+            }
+        }
+    }
+    // EC elements
+    if (P.nEC > 0) {
+        const uint32_t beg = P.ec_ptr[v], end = P.ec_ptr[v + 1];
+        for (uint32_t b = beg; b < end; b += LPV) {
+            const uint32_t j = b + G.sub;
+            const bool valid = j < end;
+            uint32_t col = 0, o = 0;
+            if (valid) {
+                col = P.ec_col[j];
+                o = P.ec_o[j];
+            }
+            const int cnt = min((int)(end - b), LPV);
+            for (int i = 0; i < P.nEC; ++i) {
+                const double c = valid ? x[P.ec_base + (size_t)i * P.nE + col] : 0.0;
+                const typename AR::Coef cf = AR::coef(c);
+                const uint32_t row = ((uint32_t)i * P.ndirs + o) * (uint32_t)nS;
+                for (int t = 0; t < cnt; ++t) {
+                    const typename AR::Coef ct = AR::shfl(G.mask, cf, t, LPV);
+                    const uint32_t rt = __shfl_sync(G.mask, row, t, LPV);
+                    if (AR::nz(ct)) {
+                        const float *L = P.lutEC + rt;
+#pragma unroll
+                        for (int k = 0; k < NCH; ++k) {
+                            const int s = G.sub + k * LPV;
+                            if (s < nS) AR::fma_(acc[k], ct, __ldg(L + s));
+                        }
+                    }
+                }
+            }
+        }
+    }
+    // ISO elements
+    if (P.nISO > 0) {
+        const uint32_t beg = P.iso_ptr[v], end = P.iso_ptr[v + 1];
+        for (uint32_t b = beg; b < end; b += LPV) {
+            const uint32_t j = b + G.sub;
+            const bool valid = j < end;
+            const uint32_t col = valid ? P.iso_col[j] : 0;
+            const int cnt = min((int)(end - b), LPV);
+            for (int i = 0; i < P.nISO; ++i) {
+                const double c = valid ? x[P.iso_base + (size_t)i * P.nISOv + col] : 0.0;
+                const typename AR::Coef cf = AR::coef(c);
+                for (int t = 0; t < cnt; ++t) {
+                    const typename AR::Coef ct = AR::shfl(G.mask, cf, t, LPV);
+                    if (AR::nz(ct)) {
+                        const float *L = P.lutISO + (size_t)i * nS;
+#pragma unroll
+                        for (int k = 0; k < NCH; ++k) {
+                            const int s = G.sub + k * LPV;
+                            if (s < nS) AR::fma_(acc[k], ct, __ldg(L + s));
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
+// y = A x ; optionally ax_out = A x ; optionally partial sums of |sqw*(Ax - yobs)|^2
+template <int LPV, int NCH, class AR>
+__global__ void __launch_bounds__(kBlock) k_forward(const OpDev P, const double *__restrict__ x,
+                                                    double *__restrict__ yout, double *__restrict__ axout,
+                                                    const double *__restrict__ yobs, const double *__restrict__ sqw,
+                                                    double *__restrict__ partials) {
+    const Group<LPV> G;
+    const int gpb = kBlock / LPV;
+    const int ngroups = gridDim.x * gpb;
+    double nrm = 0.0;
+    for (int v = blockIdx.x * gpb + (int)threadIdx.x / LPV; v < P.nV; v += ngroups) {
+        typename AR::Acc acc[NCH];
+        forward_row<LPV, NCH, AR>(P, G, v, x, acc);
+#pragma unroll
+        for (int k = 0; k < NCH; ++k) {
+            const int s = G.sub + k * LPV;
+            if (s < P.nS) {
+                const size_t idx = (size_t)v * P.nS + s;
+                const double a = AR::val(acc[k]);
+                if (yout) yout[idx] = a;
+                if (axout) axout[idx] = a;
+                if (partials) {
+                    double r = yobs ? a - yobs[idx] : a;
+                    if (sqw) r *= sqw[idx];
+                    nrm = fma(r, r, nrm);
+                }
+            }
+        }
+    }
+    if (partials) block_sum_store(nrm, partials + (size_t)blockIdx.x * kRedSlots);
+}
+
+// ------------------------------------------------------------------ adjoint
+// Group-wide dot products <LUT row of item t, z> for up to LPV items; lane `sub` returns
+// the total of item `sub`.  red: this group's LPV x (LPV+1) shared-memory tile.
+template <int LPV, int NCH, class AR>
+__device__ __forceinline__ typename AR::Acc batch_dots(const Group<LPV> &G, const float *__restrict__ lut,
+                                                       uint32_t row, int cnt, int nS,
+                                                       const typename AR::Coef (&z)[NCH],
+                                                       typename AR::Acc *__restrict__ red) {
+    typename AR::Acc part[LPV];
+#pragma unroll
+    for (int t = 0; t < LPV; ++t) {
+        AR::zero(part[t]);
+        if (t < cnt) {
+            const uint32_t rt = __shfl_sync(G.mask, row, t, LPV);
+            const float *L = lut + rt;
+#pragma unroll
+            for (int k = 0; k < NCH; ++k) {
+                const int s = G.sub + k * LPV;
+                if (s < nS) AR::fma_(part[t], z[k], __ldg(L + s));
+            }
+        }
+    }
+    if (LPV == 1) return part[0];
+#pragma unroll
+    for (int t = 0; t < LPV; ++t) red[t * (LPV + 1) + G.sub] = part[t];
+    __syncwarp(G.mask);
+    typename AR::Acc tot = red[G.sub * (LPV + 1)];
+#pragma unroll
+    for (int q = 1; q < LPV; ++q) AR::add(tot, red[G.sub * (LPV + 1) + q]);
+    __syncwarp(G.mask);
+    return tot;
+}
+
+// in_mode 0: z = yin[v,:]
+// in_mode 1: z = sqw*r with r = sqw*(A x - yobs) (gradient of 1/2|sqw(Ax-y)|^2), |r|^2 partials
+// in_mode 2: as 1 with A x replaced by ca*ax_a + cb*ax_b
+template <int LPV, int NCH, class AR>
+__global__ void __launch_bounds__(kBlock) k_adjoint(const OpDev P, const double *__restrict__ yin, int in_mode,
+                                                    const double *__restrict__ x, const double *__restrict__ yobs,
+                                                    const double *__restrict__ sqw, const double *__restrict__ ax_a,
+                                                    const double *__restrict__ ax_b, double ca, double cb,
+                                                    double *__restrict__ scratch, double *__restrict__ xout,
+                                                    double *__restrict__ partials) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    typename AR::Acc *red =
+        reinterpret_cast<typename AR::Acc *>(smem_raw) + ((int)threadIdx.x / LPV) * LPV * (LPV + 1);
+    const Group<LPV> G;
+    const int gpb = kBlock / LPV;
+    const int ngroups = gridDim.x * gpb;
+    const int nS = P.nS;
+    double nrm = 0.0;
+    for (int v = blockIdx.x * gpb + (int)threadIdx.x / LPV; v < P.nV; v += ngroups) {
+        typename AR::Coef z[NCH];
+        if (in_mode == 0) {
+#pragma unroll
+            for (int k = 0; k < NCH; ++k) {
+                const int s = G.sub + k * LPV;
+                z[k] = AR::coef(s < nS ? yin[(size_t)v * nS + s] : 0.0);
+            }
+        } else {
+            double a[NCH];
+            if (in_mode == 1) {
+                typename AR::Acc acc[NCH];
+                forward_row<LPV, NCH, AR>(P, G, v, x, acc);
+#pragma unroll
+                for (int k = 0; k < NCH; ++k) a[k] = AR::val(acc[k]);
+            } else {
+#pragma unroll
+                for (int k = 0; k < NCH; ++k) {
+                    const int s = G.sub + k * LPV;
+                    const size_t idx = (size_t)v * nS + s;
+                    a[k] = s < nS ? ca * ax_a[idx] + cb * ax_b[idx] : 0.0;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < NCH; ++k) {
+                const int s = G.sub + k * LPV;
+                double zz = 0.0;
+                if (s < nS) {
+                    const size_t idx = (size_t)v * nS + s;
+                    double r = a[k] - yobs[idx];
+                    if (sqw) r *= sqw[idx];
+                    nrm = fma(r, r, nrm);
+                    zz = sqw ? sqw[idx] * r : r;
+                }
+                z[k] = AR::coef(zz);
+            }
+        }
+        // IC segments -> per-segment terms in voxel order
+        if (P.nIC > 0) {
+            const uint32_t beg = P.vox_ptr[v], end = P.vox_ptr[v + 1];
+            for (uint32_t b = beg; b < end; b += LPV) {
+                const uint32_t j = b + G.sub;
+                const bool valid = j < end;
+                const uint32_t o = valid ? P.seg_o[j] : 0;
+                const float l = valid ? P.seg_l[j] : 0.f;
+                const int cnt = min((int)(end - b), LPV);
+                for (int i = 0; i < P.nIC; ++i) {
+                    const uint32_t row = ((uint32_t)i * P.ndirs + o) * (uint32_t)nS;
+                    const typename AR::Acc tot = batch_dots<LPV, NCH, AR>(G, P.lutIC, row, cnt, nS, z, red);
+                    if (valid) scratch[(size_t)i * P.n + j] = (double)l * AR::val(tot);
+                }
+            }
+        }
+        if (P.nEC > 0) {
+            const uint32_t beg = P.ec_ptr[v], end = P.ec_ptr[v + 1];
+            for (uint32_t b = beg; b < end; b += LPV) {
+                const uint32_t j = b + G.sub;
+                const bool valid = j < end;
+                const uint32_t o = valid ? P.ec_o[j] : 0;
+                const uint32_t col = valid ? P.ec_col[j] : 0;
+                const int cnt = min((int)(end - b), LPV);
+                for (int i = 0; i < P.nEC; ++i) {
+                    const uint32_t row = ((uint32_t)i * P.ndirs + o) * (uint32_t)nS;
+                    const typename AR::Acc tot = batch_dots<LPV, NCH, AR>(G, P.lutEC, row, cnt, nS, z, red);
+                    if (valid) xout[P.ec_base + (size_t)i * P.nE + col] = AR::val(tot);
+                }
+            }
+        }
+        if (P.nISO > 0) {
+            const uint32_t beg = P.iso_ptr[v], end = P.iso_ptr[v + 1];
+            for (uint32_t b = beg; b < end; b += LPV) {
+                const uint32_t j = b + G.sub;
+                const bool valid = j < end;
+                const uint32_t col = valid ? P.iso_col[j] : 0;
+                const int cnt = min((int)(end - b), LPV);
+                for (int i = 0; i < P.nISO; ++i) {
+                    const typename AR::Acc tot =
+                        batch_dots<LPV, NCH, AR>(G, P.lutISO, (uint32_t)(i * nS), cnt, nS, z, red);
+                    if (valid) xout[P.iso_base + (size_t)i * P.nISOv + col] = AR::val(tot);
+                }
+            }
+        }
+    }
+    if (partials) block_sum_store(nrm, partials + (size_t)blockIdx.x * kRedSlots);
+}
+
+}  // namespace detail
+}  // namespace cgb

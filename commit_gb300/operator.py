@@ -1,0 +1,163 @@
+"""GB300 drop-in for commit/operator/operator.pyx:10-184 (``LinearOperator``).
+
+``LinearOperator(DICTIONARY, KERNELS, THREADS, nolut=False)`` takes the same dicts the
+reference takes (THREADS is accepted and ignored: the device re-layout done once at
+construction replaces the CPU partitions of Evaluation.set_threads).  ``dot`` accepts a
+float64 numpy vector (copied to the device and back, like the reference's host call) or
+a CUDA float64 torch tensor (kept on the device, enqueued on torch's current stream).
+``T`` returns the adjoint sharing the same device dictionary; ``shape``, ``nROWS``,
+``nCOLS`` and ``adjoint`` are as in the reference.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import check, lib
+
+
+def _host(a, dtype) -> np.ndarray:
+    a = np.ascontiguousarray(np.asarray(a, dtype=dtype))
+    return a
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p) if a.size else None
+
+
+class _Handle:
+    """Owns one cgb_op (device copy of the dictionary)."""
+
+    def __init__(self, ptr, device):
+        self.ptr = ptr
+        self.device = device
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                lib().cgb_op_destroy(self.ptr)
+                self.ptr = None
+        except Exception:
+            pass
+
+
+class LinearOperator:
+    """Implicit COMMIT dictionary operator A (and A' via ``.T``) on a GB300."""
+
+    def __init__(self, DICTIONARY, KERNELS, THREADS=None, nolut=False, arith: str = 'ff', device=None):
+        self.DICTIONARY = DICTIONARY
+        self.KERNELS = KERNELS
+        self.THREADS = THREADS
+        IC, EC, ISO = DICTIONARY['IC'], DICTIONARY['EC'], DICTIONARY['ISO']
+        self.ICn = int(IC['n'])
+        self.ICnSTR = int(IC['nSTR'])
+        self.ICnRF = int(KERNELS['wmr'].shape[0])
+        self.ICnVOX = int(IC['nVOX'])
+        self.ECn = int(EC['n'])
+        self.ECnRF = int(KERNELS['wmh'].shape[0])
+        self.ISOn = int(ISO['n'])
+        self.ISOnRF = int(KERNELS['iso'].shape[0])
+        # number of samples and directions as operator.pyx:56-63
+        if KERNELS['wmr'].size > 0:
+            self.nSAMPLES = int(KERNELS['wmr'].shape[2])
+        elif KERNELS['wmh'].size > 0:
+            self.nSAMPLES = int(KERNELS['wmh'].shape[2])
+        else:
+            self.nSAMPLES = int(KERNELS['wmr'].shape[1])
+        self.ndirs = int(KERNELS['wmr'].shape[1])
+        self.nolut = bool(nolut)
+        self.adjoint = 0
+        self.nROWS = self.ICnVOX * self.nSAMPLES
+        self.nCOLS = self.ICnSTR * self.ICnRF + self.ECn * self.ECnRF + self.ISOn * self.ISOnRF
+        if arith not in ('ff', 'f64'):
+            raise ValueError("arith must be 'ff' (float-float, FP64-accurate) or 'f64' (native FP64)")
+        self.arith = arith
+        if device is None:
+            device = torch.cuda.current_device() if torch.cuda.is_available() else 0
+        self.device = int(device)
+
+        f = _host(IC['str'], np.uint32)
+        v = _host(IC['vox'], np.uint32)
+        o = _host(IC['dir'], np.uint16)
+        ln = _host(IC['len'], np.float32)
+        ev = IC.get('eval')
+        ev = _host(ev if ev is not None else np.ones(self.ICnSTR * self.ICnRF, np.uint32), np.uint32)
+        if ev.size < self.ICnSTR * self.ICnRF:
+            raise ValueError('DICTIONARY["IC"]["eval"] is shorter than nSTR * nIC')
+        ecv = _host(EC['vox'], np.uint32)
+        eco = _host(EC['dir'], np.uint16)
+        isov = _host(ISO['vox'], np.uint32)
+        lic = _host(KERNELS['wmr'], np.float32)
+        lec = _host(KERNELS['wmh'], np.float32)
+        liso = _host(KERNELS['iso'], np.float32)
+        if f.size != self.ICn or v.size != self.ICn or ln.size != self.ICn or (not nolut and o.size != self.ICn):
+            raise ValueError('IC arrays do not match DICTIONARY["IC"]["n"]')
+        if ecv.size != self.ECn or isov.size != self.ISOn:
+            raise ValueError('EC/ISO arrays do not match their "n"')
+        out = ctypes.c_void_p()
+        check(lib().cgb_op_create(self.device, self.nSAMPLES, max(self.ndirs, 1), self.ICnSTR, self.ICn, self.ECn,
+                                  self.ICnVOX, self.ISOn, _ptr(f), _ptr(ev), _ptr(v), _ptr(o), _ptr(ln), _ptr(ecv),
+                                  _ptr(eco), _ptr(isov), _ptr(lic), _ptr(lec), _ptr(liso), self.ICnRF, self.ECnRF,
+                                  self.ISOnRF, int(self.nolut), _lib.ARITH[arith], ctypes.byref(out)))
+        self._h = _Handle(out, self.device)
+
+    # ------------------------------------------------------------------ reference surface
+    @property
+    def T(self):
+        """Adjoint operator (shares the device dictionary)."""
+        C = object.__new__(LinearOperator)
+        C.__dict__.update(self.__dict__)
+        C.adjoint = 1 - self.adjoint
+        return C
+
+    @property
+    def shape(self):
+        return (self.nROWS, self.nCOLS) if not self.adjoint else (self.nCOLS, self.nROWS)
+
+    @property
+    def handle(self):
+        return self._h.ptr
+
+    def device_bytes(self) -> int:
+        b = ctypes.c_size_t()
+        check(lib().cgb_op_device_bytes(self._h.ptr, ctypes.byref(b)))
+        return int(b.value)
+
+    def dot(self, v_in, out=None, arith: str | None = None):
+        """A @ v_in (or A' @ v_in for the adjoint).
+
+        numpy float64 in -> numpy float64 out (host copies inside the call);
+        torch CUDA float64 in -> torch CUDA float64 out (no host round-trip).
+        """
+        ar = _lib.ARITH[arith or self.arith]
+        if isinstance(v_in, torch.Tensor) and v_in.is_cuda:
+            if v_in.dtype != torch.float64:
+                raise TypeError('LinearOperator.dot expects float64 tensors')
+            v_in = v_in.contiguous()
+            if v_in.numel() != self.shape[1]:
+                raise RuntimeError("A.dot(): dimensions do not match")
+            if out is None:
+                out = torch.empty(self.shape[0], dtype=torch.float64, device=v_in.device)
+            st = torch.cuda.current_stream(v_in.device).cuda_stream
+            check(lib().cgb_op_apply(self._h.ptr, self.adjoint, ctypes.c_void_p(v_in.data_ptr()), v_in.numel(),
+                                     ctypes.c_void_p(out.data_ptr()), out.numel(), _lib.DTYPE_F64, ar,
+                                     ctypes.c_void_p(st)))
+            return out
+        v = np.ascontiguousarray(v_in, dtype=np.float64)
+        if v.size != self.shape[1]:
+            raise RuntimeError("A.dot(): dimensions do not match")
+        res = np.empty(self.shape[0], dtype=np.float64) if out is None else out
+        if arith is not None and ar != _lib.ARITH[self.arith]:
+            check(lib().cgb_op_set_arith(self._h.ptr, ar))
+        try:
+            check(lib().cgb_op_apply_host(self._h.ptr, self.adjoint, _ptr(v), v.size, _ptr(res), res.size))
+        finally:
+            if arith is not None and ar != _lib.ARITH[self.arith]:
+                check(lib().cgb_op_set_arith(self._h.ptr, _lib.ARITH[self.arith]))
+        return res
+
+    def __matmul__(self, v):
+        return self.dot(v)

@@ -1,0 +1,281 @@
+"""GB300 drop-in for commit/solvers.py (init_regularisation, evaluate_model, solve, fista).
+
+``init_regularisation`` accepts the dict ``Evaluation.set_regularisation`` builds
+(commit/core.pyx:1030-1046 and solvers.py:16-206) and returns it with ``omega`` and
+``prox`` entries, as the reference does; here they are device-backed callables that also
+carry the regulariser description, which ``solve``/``fista`` hand to the CUDA solver
+(``cgb_fista_run``).  FISTA itself runs on the GPU with the reference's step-size rule,
+backtracking, stopping criteria and returned ``opt_details`` (solvers.py:244-391).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import check, lib
+from .operator import LinearOperator
+
+eps = np.finfo(float).eps
+list_regularizers = [None, 'lasso', 'group_lasso', 'sparse_group_lasso']
+
+
+def _dev(a, dtype, device):
+    return torch.as_tensor(np.ascontiguousarray(a), dtype=dtype).to(device)
+
+
+def level_schedule(groups):
+    """Order groups into levels of pairwise-disjoint groups that reproduce the sequential
+    prox_group_lasso loop (proximals.pyx:103-134): a group's level is one more than the
+    highest level of any earlier group it overlaps, so overlapping groups keep their
+    relative order and disjoint ones run together.  Returns (order, level_ptr)."""
+    ng = len(groups)
+    if ng == 0:
+        return np.zeros(0, np.int64), np.zeros(1, np.int64)
+    top = max((int(g.max()) for g in groups if g.size), default=-1) + 1
+    touch = np.full(max(top, 1), -1, dtype=np.int64)
+    level = np.zeros(ng, dtype=np.int64)
+    for k, g in enumerate(groups):
+        lv = int(touch[g].max()) + 1 if g.size else 0
+        level[k] = lv
+        if g.size:
+            touch[g] = lv
+    order = np.argsort(level, kind='stable')
+    counts = np.bincount(level, minlength=int(level.max()) + 1)
+    return order, np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+
+
+class RegSpec:
+    """Device description of a regularisation dict (the omega/prox pair of the reference)."""
+
+    def __init__(self, rp: dict):
+        self.rp = rp
+        self.sIC, self.nIC = int(rp.get('startIC') or 0), int(rp.get('sizeIC') or 0)
+        self.sEC, self.nEC = int(rp.get('startEC') or 0), int(rp.get('sizeEC') or 0)
+        self.sISO, self.nISO = int(rp.get('startISO') or 0), int(rp.get('sizeISO') or 0)
+        self.ncols = self.nIC + self.nEC + self.nISO
+        self.reg_ic, self.reg_ec, self.reg_iso = rp.get('regIC'), rp.get('regEC'), rp.get('regISO')
+        # nn flags: `== True` when no regulariser is set, truthiness otherwise (solvers.py:54-206)
+        self.nn_ic = bool(rp.get('nnIC') == True) if self.reg_ic is None else bool(rp.get('nnIC'))  # noqa: E712
+        self.nn_ec = bool(rp.get('nnEC') == True) if self.reg_ec is None else bool(rp.get('nnEC'))  # noqa: E712
+        self.nn_iso = bool(rp.get('nnISO') == True) if self.reg_iso is None else bool(rp.get('nnISO'))  # noqa: E712
+        dIC = rp.get('dictIC_params')
+        dISO = rp.get('dictISO_params')
+        acw = np.ones(self.ncols, dtype=np.float64)
+        self.weighted_ic = False
+        self.weighted_iso = False
+        if dIC is not None and 'coeff_weights_kept' in dIC:
+            acw[self.sIC:self.sIC + self.nIC] = dIC['coeff_weights_kept']
+            self.weighted_ic = self.reg_ic in ('lasso', 'sparse_group_lasso')
+        if dISO is not None and 'coeff_weights' in dISO:
+            acw[self.sISO:self.sISO + self.nISO] = dISO['coeff_weights']
+            self.weighted_iso = self.reg_iso == 'lasso'
+        self.acw = acw
+        self.lam_ic = self.lam_ic_group = self.lam_ec = self.lam_iso = 0.0
+        if self.reg_ic == 'lasso':
+            self.lam_ic = float(rp['lambdaIC'])
+        elif self.reg_ic == 'group_lasso':
+            self.lam_ic = float(rp['lambdaIC'])
+        elif self.reg_ic == 'sparse_group_lasso':
+            self.lam_ic, self.lam_ic_group = float(rp['lambdaIC'][0]), float(rp['lambdaIC'][1])
+        if self.reg_ec == 'lasso':
+            self.lam_ec = float(rp.get('lambdaEC'))
+        if self.reg_iso == 'lasso':
+            self.lam_iso = float(rp.get('lambdaISO'))
+        self.groups = None
+        if self.reg_ic in ('group_lasso', 'sparse_group_lasso'):
+            if not len(dIC['group_idx_kept']) == len(dIC['group_weights']):
+                raise ValueError('Number of groups and weights do not match')
+            groups = [np.asarray(g, dtype=np.int64).ravel() for g in dIC['group_idx_kept']]
+            order, level_ptr = level_schedule(groups)
+            gw = np.asarray(dIC['group_weights'], dtype=np.float64)
+            og = [groups[k] for k in order]
+            sizes = np.array([g.size for g in og], dtype=np.int64)
+            self.group_idx = np.concatenate(og).astype(np.int32) if og else np.zeros(0, np.int32)
+            self.group_ptr = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+            self.group_w = gw[order]
+            self.level_ptr = level_ptr
+            self.groups = groups
+        self._dev = {}
+
+    def device_arrays(self, device):
+        key = str(device)
+        if key not in self._dev:
+            d = {'acw': _dev(self.acw, torch.float64, device)}
+            if self.groups is not None:
+                d['gidx'] = _dev(self.group_idx, torch.int32, device)
+                d['gptr'] = _dev(self.group_ptr, torch.int64, device)
+                d['gw'] = _dev(self.group_w, torch.float64, device)
+            self._dev[key] = d
+        return self._dev[key]
+
+    def cstruct(self, device) -> tuple:
+        d = self.device_arrays(device)
+        r = _lib.CgbReg()
+        r.start_ic, r.size_ic, r.start_ec, r.size_ec = self.sIC, self.nIC, self.sEC, self.nEC
+        r.start_iso, r.size_iso = self.sISO, self.nISO
+        r.reg_ic, r.reg_ec, r.reg_iso = _lib.REG[self.reg_ic], _lib.REG[self.reg_ec], _lib.REG[self.reg_iso]
+        r.nn_ic, r.nn_ec, r.nn_iso = int(self.nn_ic), int(self.nn_ec), int(self.nn_iso)
+        r.lambda_ic, r.lambda_ic_group = self.lam_ic, self.lam_ic_group
+        r.lambda_ec, r.lambda_iso = self.lam_ec, self.lam_iso
+        r.coeff_weights = d['acw'].data_ptr()
+        r.weighted_ic, r.weighted_iso = int(self.weighted_ic), int(self.weighted_iso)
+        keep = [d]
+        if self.groups is not None:
+            r.group_idx, r.group_ptr, r.group_w = d['gidx'].data_ptr(), d['gptr'].data_ptr(), d['gw'].data_ptr()
+            r.ngroups = len(self.groups)
+            lp = np.ascontiguousarray(self.level_ptr, dtype=np.int64)
+            keep.append(lp)
+            r.level_ptr = lp.ctypes.data
+            r.nlevels = lp.size - 1
+        return r, keep
+
+
+def _no_reg_spec(ncols: int) -> RegSpec:
+    return RegSpec({'startIC': 0, 'sizeIC': ncols, 'startEC': ncols, 'sizeEC': 0, 'startISO': ncols, 'sizeISO': 0,
+                    'regIC': None, 'regEC': None, 'regISO': None, 'nnIC': False, 'nnEC': False, 'nnISO': False})
+
+
+class _Omega:
+    """omega(x) of init_regularisation, evaluated on the device."""
+
+    def __init__(self, spec: RegSpec):
+        self.spec = spec
+
+    def __call__(self, x) -> float:
+        from . import proximals as P
+        s = self.spec
+        xt, _ = P._as_device(x)
+        total = 0.0
+        acw = s.device_arrays(xt.device)['acw']
+        if s.reg_ic == 'lasso':
+            total += P._l1(xt, acw if s.weighted_ic else None, s.sIC, s.nIC - s.sIC) * s.lam_ic
+        elif s.reg_ic == 'group_lasso':
+            total += P._omega_groups(xt, s, s.lam_ic)
+        elif s.reg_ic == 'sparse_group_lasso':
+            if s.lam_ic != 0 or s.lam_ic_group != 0:
+                total += s.lam_ic * P._l1(xt, acw if s.weighted_ic else None, 0, xt.numel())
+                total += P._omega_groups(xt, s, s.lam_ic_group, force=True)
+        if s.reg_ec == 'lasso':
+            total += s.lam_ec * P._l1(xt, None, s.sEC, s.nEC)
+        if s.reg_iso == 'lasso':
+            if s.weighted_iso:
+                total += s.lam_iso * P._l1(xt, acw, s.sISO, min(s.nISO, xt.numel()) - s.sISO)
+            else:
+                total += s.lam_iso * P._l1(xt, None, s.sISO, s.nISO)
+        return float(total)
+
+
+class _Prox:
+    """prox(x, scaling) of init_regularisation: in place on a numpy array or CUDA tensor."""
+
+    def __init__(self, spec: RegSpec):
+        self.spec = spec
+
+    def __call__(self, x, scaling):
+        from . import proximals as P
+        return P._apply_spec(x, self.spec, float(scaling))
+
+
+def init_regularisation(regularisation_params: dict) -> dict:
+    """commit/solvers.py:16-206: adds 'omega' and 'prox' to the regularisation dict."""
+    rp = regularisation_params
+    if rp['regIC'] not in list_regularizers or rp['regEC'] not in list_regularizers or \
+            rp['regISO'] not in list_regularizers:
+        raise ValueError('Regularisation not in the list')
+    if rp['regEC'] not in (None, 'lasso') or rp['regISO'] not in (None, 'lasso'):
+        raise ValueError('EC and ISO compartments support only None or "lasso"')
+    spec = RegSpec(rp)
+    rp['omega'] = _Omega(spec)
+    rp['prox'] = _Prox(spec)
+    rp['_spec'] = spec
+    return rp
+
+
+def evaluate_model(y, A, x, regularisation=None):
+    """solvers.py:209-215."""
+    omega = (lambda x: 0.0) if regularisation is None else init_regularisation(regularisation)['omega']
+    r = A.dot(x)
+    if isinstance(r, torch.Tensor):
+        return 0.5 * float(torch.linalg.norm(r - torch.as_tensor(y, device=r.device))) ** 2 + omega(x)
+    return 0.5 * np.linalg.norm(r - y) ** 2 + omega(x)
+
+
+def solve(y, A, At, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, verbose=True, x0=None, regularisation=None,
+          confidence_array=None, arith=None, momentum_reuse=True):
+    """solvers.py:218-241: regularised least squares by FISTA, on the GPU."""
+    if regularisation is None:
+        spec = _no_reg_spec(A.shape[1])
+    else:
+        spec = regularisation.get('_spec') if isinstance(regularisation, dict) else None
+        if spec is None:
+            spec = init_regularisation(regularisation)['_spec']
+    sqrt_W = None
+    if confidence_array is not None:
+        sqrt_W = np.sqrt(np.asarray(confidence_array)) if not isinstance(confidence_array, torch.Tensor) \
+            else torch.sqrt(confidence_array)
+    return _fista(y, A, spec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, arith, momentum_reuse)
+
+
+def fista(y, A, At, omega, prox, sqrt_W=None, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, verbose=False, x0=None,
+          arith=None, momentum_reuse=True):
+    """solvers.py:244-391.  omega/prox must come from init_regularisation (or be the
+    no-regulariser pair of ``solve``)."""
+    spec = getattr(prox, 'spec', None)
+    if spec is None:
+        spec = _no_reg_spec(A.shape[1])
+        if not (callable(prox) and _is_identity(prox, A.shape[1])):
+            raise TypeError('commit_gb300 fista needs omega/prox from commit_gb300.solvers.init_regularisation')
+    return _fista(y, A, spec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, arith, momentum_reuse)
+
+
+def _is_identity(prox, n) -> bool:
+    probe = np.linspace(-1.0, 1.0, 7)
+    try:
+        out = prox(probe.copy(), 1.0)
+    except Exception:
+        return False
+    return out is not None and np.array_equal(np.asarray(out), probe)
+
+
+def _fista(y, A, spec: RegSpec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, arith, momentum_reuse):
+    if not isinstance(A, LinearOperator):
+        raise TypeError('A must be a commit_gb300.operator.LinearOperator')
+    if A.adjoint:
+        raise ValueError('A must be the forward operator')
+    dev = torch.device('cuda', A.device)
+    host = not isinstance(y, torch.Tensor)
+    yd = torch.as_tensor(np.ascontiguousarray(y, dtype=np.float64) if host else y, dtype=torch.float64).to(dev)
+    yd = yd.contiguous()
+    if yd.numel() != A.nROWS:
+        raise RuntimeError("A.dot(): dimensions do not match")
+    if x0 is None:
+        xd = torch.zeros(A.nCOLS, dtype=torch.float64, device=dev)
+    else:
+        xd = torch.as_tensor(np.asarray(x0, dtype=np.float64) if not isinstance(x0, torch.Tensor) else x0,
+                             dtype=torch.float64).to(dev).clone()
+    sw = None
+    if sqrt_W is not None:
+        sw = torch.as_tensor(np.asarray(sqrt_W, dtype=np.float64) if not isinstance(sqrt_W, torch.Tensor) else sqrt_W,
+                             dtype=torch.float64).to(dev).contiguous()
+    if spec.ncols != A.nCOLS:
+        raise ValueError('regularisation sizes do not match the operator')
+    reg, keep = spec.cstruct(dev)
+    prm = _lib.CgbFistaParams(float(tol_fun), float(tol_x), int(max_iter), int(verbose) if verbose is not True else 1,
+                              _lib.ARITH[arith or A.arith], int(bool(momentum_reuse)))
+    res = _lib.CgbFistaResult()
+    st = torch.cuda.current_stream(dev).cuda_stream
+    check(lib().cgb_fista_run(A.handle, ctypes.c_void_p(yd.data_ptr()),
+                              ctypes.c_void_p(sw.data_ptr()) if sw is not None else None, ctypes.byref(reg),
+                              ctypes.byref(prm), ctypes.c_void_p(xd.data_ptr()), ctypes.byref(res),
+                              ctypes.c_void_p(st)))
+    del keep
+    details = {'residual': res.residual, 'regterm': res.regterm, 'cost_function': res.cost_function,
+               'abs_cost': res.abs_cost, 'rel_cost': res.rel_cost, 'abs_x': res.abs_x, 'rel_x': res.rel_x,
+               'iterations': int(res.iterations), 'stopping_criterion': _lib.CRITERIA[res.stopping_criterion]}
+    details['backtracks'] = int(res.backtracks)
+    details['operator_calls'] = int(res.operator_calls)
+    x = xd.cpu().numpy() if host else xd
+    return x, details

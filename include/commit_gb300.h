@@ -1,0 +1,187 @@
+/*
+ * commit_gb300 -- C ABI of the GB300 (sm_103a) implementation of COMMIT's implicit
+ * dictionary operator A / A' and of its FISTA solver.
+ *
+ * Every entry point returns a status code (CGB_OK on success); the message of the last
+ * failure on the calling thread is available from cgb_last_error().  Handles are
+ * independent: calls on different handles may run concurrently from different host
+ * threads.  A handle owns the device copy of the dictionary (re-laid-out once at
+ * creation) and its work buffers; callers own the vectors they pass in and out.
+ *
+ * Reference interfaces replaced (file:line within the reference project):
+ *   LinearOperator.__init__     commit/operator/operator.pyx:40-94     -> cgb_op_create
+ *   LinearOperator.dot (A, A')  commit/operator/operator.pyx:114-184   -> cgb_op_apply_host / cgb_op_apply
+ *   COMMIT_A / COMMIT_At        setup_operator.py:245-365, 591-710     -> cgb_op_apply(adjoint = 0 / 1)
+ *   COMMIT_A_nolut / _At_nolut  setup_operator.py:776-811, 877-915     -> same, on a handle created with nolut = 1
+ *   Evaluation.set_threads      commit/core.pyx:586-724                -> (no counterpart: the device re-layout in
+ *                                                                         cgb_op_create replaces the CPU partitions)
+ *   solvers.fista / solve       commit/solvers.py:218-391              -> cgb_fista_run
+ *   proximals.pyx               commit/proximals.pyx:13-186            -> cgb_prox_* / cgb_omega_*
+ */
+#ifndef COMMIT_GB300_H
+#define COMMIT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status codes */
+#define CGB_OK 0
+#define CGB_ERR_INVALID 1     /* bad argument or dictionary content (index out of range, ...)   */
+#define CGB_ERR_CUDA 2        /* a CUDA runtime call failed                                        */
+#define CGB_ERR_NOMEM 3       /* device allocation failed                                          */
+#define CGB_ERR_UNSUPPORTED 4 /* shape outside what the kernels handle (e.g. nS > 1024)            */
+#define CGB_ERR_DIMENSION 5   /* vector length does not match the operator ("dimensions do not match") */
+
+/* arithmetic of the FP64 operator path */
+#define CGB_ARITH_F64 0 /* native FP64 FMA, the reference's own arithmetic                             */
+#define CGB_ARITH_FF 1  /* float-float (two FP32 words, ~48-bit significand) products and sums, FP64    */
+                        /* inputs/outputs; error well below 1e-10 relative at a fraction of FP64 cost  */
+/* reduced-precision operator path (FP32 vectors, FP32 accumulation) */
+#define CGB_ARITH_BF16 2 /* LUT in bfloat16, segment lengths in FP16                                   */
+#define CGB_ARITH_FP16 3 /* LUT in FP16, segment lengths in FP16                                       */
+#define CGB_ARITH_F32 4  /* LUT and lengths in FP32, FP32 accumulation                                  */
+
+/* vector element types for cgb_op_apply */
+#define CGB_DTYPE_F64 0
+#define CGB_DTYPE_F32 1
+
+typedef struct cgb_op cgb_op; /* opaque operator handle */
+
+/* Human-readable message of the last failing call on this thread ("" if none). */
+const char *cgb_last_error(void);
+
+/* Library version string. */
+const char *cgb_version(void);
+
+/*
+ * Create an operator on device `device` from the dictionary and LUT arrays (HOST
+ * pointers, layout of LinearOperator.__init__, operator.pyx:40-94):
+ *   IC: ICf[n] fibre (column) index, ICv[n] voxel, ICo[n] orientation, ICl[n] length,
+ *       ICeval[nF*nIC] per-column 0/1 mask;
+ *   EC: ECv[nE], ECo[nE];  ISO: ISOv[nISOv];
+ *   LUTs: lutIC[nIC*ndirs*nS], lutEC[nEC*ndirs*nS], lutISO[nISO*nS] (float32, C order).
+ * nV is the number of voxels (rows = nV*nS).  Columns: nF*nIC + nE*nEC + nISOv*nISO.
+ * The arrays need not be sorted; they are copied, validated and re-laid-out on the
+ * device (voxel-ordered stream for A, fibre-ordered index for A').  With nolut = 1 the
+ * operator is the LUT-free scalar operator of setup_operator.py:713-915 (nS must be 1,
+ * IC uses one response, ISO at most one).  `arith` selects the default arithmetic
+ * (CGB_ARITH_F64 or CGB_ARITH_FF); reduced-precision copies are made on demand.
+ */
+int cgb_op_create(int device, int nS, int ndirs, int nF, int64_t n, int nE, int nV, int nISOv,
+                  const uint32_t *ICf, const uint32_t *ICeval, const uint32_t *ICv, const uint16_t *ICo,
+                  const float *ICl, const uint32_t *ECv, const uint16_t *ECo, const uint32_t *ISOv,
+                  const float *lutIC, const float *lutEC, const float *lutISO, int nIC, int nEC, int nISO,
+                  int nolut, int arith, cgb_op **out);
+
+/* Release the handle and every device buffer it owns. */
+int cgb_op_destroy(cgb_op *op);
+
+/* nROWS and nCOLS of A (operator.pyx:69-70). */
+int cgb_op_shape(const cgb_op *op, int64_t *nrows, int64_t *ncols);
+
+/* Device bytes held by the handle. */
+int cgb_op_device_bytes(const cgb_op *op, size_t *bytes);
+
+/* Select the arithmetic used by later FP64 applies (CGB_ARITH_F64 / CGB_ARITH_FF). */
+int cgb_op_set_arith(cgb_op *op, int arith);
+
+/*
+ * out = A*in (adjoint = 0) or out = A'*in (adjoint = 1) on DEVICE vectors, enqueued on
+ * `stream` (a cudaStream_t; NULL = legacy default stream).  `out` is fully written (no
+ * pre-zeroing needed).  dtype CGB_DTYPE_F64 uses the handle's FP64 arithmetic;
+ * CGB_DTYPE_F32 uses the reduced-precision path `arith` (CGB_ARITH_BF16/FP16/F32).
+ * in_len/out_len are checked against the operator shape (CGB_ERR_DIMENSION).
+ */
+int cgb_op_apply(cgb_op *op, int adjoint, const void *in, int64_t in_len, void *out, int64_t out_len, int dtype,
+                 int arith, void *stream);
+
+/*
+ * The LinearOperator.dot contract on HOST float64 buffers: copies `in` to the device,
+ * applies A or A', copies the result to `out` and synchronises.  Replaces COMMIT_A /
+ * COMMIT_At called from operator.pyx:136-182.
+ */
+int cgb_op_apply_host(cgb_op *op, int adjoint, const double *in, int64_t in_len, double *out, int64_t out_len);
+
+/* ------------------------------------------------------------------ regularisation */
+#define CGB_REG_NONE 0
+#define CGB_REG_LASSO 1
+#define CGB_REG_GROUP_LASSO 2
+#define CGB_REG_SPARSE_GROUP_LASSO 3
+
+/*
+ * Regulariser of commit/solvers.py:16-206, per compartment.  Ranges are column ranges of
+ * x.  All pointers are DEVICE pointers (may be NULL when unused).
+ */
+typedef struct {
+    int64_t start_ic, size_ic, start_ec, size_ec, start_iso, size_iso;
+    int reg_ic, reg_ec, reg_iso; /* CGB_REG_* (EC/ISO: NONE or LASSO)                      */
+    int nn_ic, nn_ec, nn_iso;    /* non-negativity per compartment                        */
+    double lambda_ic, lambda_ic_group; /* lasso / l1 part and group part (sparse group lasso) */
+    double lambda_ec, lambda_iso;
+    const double *coeff_weights; /* all_coeff_weights[ncols] (solvers.py:38-46) or NULL   */
+    int weighted_ic, weighted_iso; /* use coeff_weights in the IC / ISO l1 terms            */
+    /* groups (IC): concatenated indices, CSR offsets [ngroups+1], weights [ngroups] */
+    const int32_t *group_idx;
+    const int64_t *group_ptr;
+    const double *group_w;
+    int64_t ngroups;
+    /* level schedule: groups [level_ptr[k], level_ptr[k+1]) are pairwise disjoint and are
+       processed together; levels run in order (reproduces the sequential loop of
+       proximals.pyx:103-134 for overlapping, hierarchical groups).  HOST pointer. */
+    const int64_t *level_ptr;
+    int64_t nlevels;
+} cgb_reg;
+
+typedef struct {
+    double tol_fun, tol_x;
+    int max_iter;
+    int verbose;          /* 0: quiet                                                    */
+    int arith;            /* CGB_ARITH_F64 / CGB_ARITH_FF                                 */
+    int momentum_reuse;   /* 1: A*xhat from A*x and A*prev_x (exact in exact arithmetic) */
+} cgb_fista_params;
+
+typedef struct {
+    double residual, regterm, cost_function, abs_cost, rel_cost, abs_x, rel_x;
+    int iterations;
+    int stopping_criterion; /* 0 abs obj, 1 rel obj, 2 abs x, 3 rel x, 4 max iter          */
+    int backtracks;
+    int operator_calls;     /* number of A and A' products                                  */
+} cgb_fista_result;
+
+/*
+ * FISTA with backtracking (solvers.py:244-391) on device vectors: y[nrows], optional
+ * sqrt_w[nrows] (square root of the confidence map, or NULL), x[ncols] holds x0 on
+ * entry and the solution on return.  Enqueued on `stream`; returns after the solve.
+ */
+int cgb_fista_run(cgb_op *op, const double *y, const double *sqrt_w, const cgb_reg *reg,
+                  const cgb_fista_params *params, double *x, cgb_fista_result *result, void *stream);
+
+/* ------------------------------------------------------------------ proximal maps */
+/* In-place proximal maps on a DEVICE float64 vector (proximals.pyx:13-77). */
+int cgb_prox_non_negativity(double *x, int64_t start, int64_t size, void *stream);
+int cgb_prox_soft_thresholding(double *x, double lam, int64_t start, int64_t size, void *stream);
+int cgb_prox_w_soft_thresholding(double *x, const double *w, double lam, int64_t start, int64_t size,
+                                 void *stream);
+int cgb_prox_projection_onto_l2_ball(double *x, double lam, int64_t start, int64_t size, void *stream);
+/* prox_group_lasso (proximals.pyx:103-134): groups as CSR (device), level schedule (host);
+   nx = length of x (group indices outside [0, nx) are ignored). */
+int cgb_prox_group_lasso(double *x, int64_t nx, const int32_t *group_idx, const int64_t *group_ptr, const double *group_w,
+                         int64_t ngroups, const int64_t *level_ptr, int64_t nlevels, double lam, void *stream);
+/* penalties (proximals.pyx:80-99, 138-186); result written to *out (host), synchronous. */
+int cgb_omega_group_lasso(const double *x, int64_t nx, const int32_t *group_idx, const int64_t *group_ptr,
+                          const double *group_w, int64_t ngroups, double lam, double *out, void *stream);
+int cgb_omega_sparse_group_lasso(const double *x, int64_t nx, const double *w, const int32_t *group_idx,
+                                 const int64_t *group_ptr, const double *group_w, int64_t ngroups, double lam1,
+                                 double lam2, double *out, void *stream);
+/* weighted / plain l1 over [start, start+size): lam * sum |w_i x_i| (w may be NULL). */
+int cgb_omega_l1(const double *x, const double *w, int64_t start, int64_t size, double lam, double *out,
+                 void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* COMMIT_GB300_H */

@@ -1,0 +1,117 @@
+"""Parity of the GB300 operator with the reference operator (golden fixtures) and the oracle.
+
+Bar (FP64 path, both arithmetics): relative error <= 1e-10 (2-norm) on A*x and A'*y.
+"""
+import numpy as np
+import pytest
+import torch
+
+import golden_io as G
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+CASES = G.case_names()
+
+
+def _op(c, arith='ff', D=None):
+    from commit_gb300.operator import LinearOperator
+    return LinearOperator(D or c['D'], c['K'], None, nolut=c['nolut'], arith=arith)
+
+
+@pytest.mark.parametrize('arith', ['ff', 'f64'])
+@pytest.mark.parametrize('name', CASES)
+def test_operator_matches_reference_golden(name, arith):
+    c = G.load_case(name)
+    A = _op(c, arith)
+    assert A.shape == (c['Ax'].size, c['x_in'].size)
+    assert A.T.shape == (c['x_in'].size, c['Ax'].size)
+    assert G.rel(A.dot(c['x_in']), c['Ax']) <= TOL
+    assert G.rel(A.T.dot(c['y_in']), c['Aty']) <= TOL
+
+
+@pytest.mark.parametrize('name', CASES)
+def test_operator_device_tensors(name):
+    c = G.load_case(name)
+    A = _op(c)
+    x = torch.from_numpy(c['x_in']).cuda()
+    y = torch.from_numpy(c['y_in']).cuda()
+    ax = A.dot(x)
+    aty = A.T.dot(y)
+    assert ax.is_cuda and aty.is_cuda
+    assert G.rel(ax.cpu().numpy(), c['Ax']) <= TOL
+    assert G.rel(aty.cpu().numpy(), c['Aty']) <= TOL
+
+
+@pytest.mark.parametrize('name', CASES)
+def test_dimension_mismatch_raises(name):
+    c = G.load_case(name)
+    A = _op(c)
+    with pytest.raises(RuntimeError, match='dimensions do not match'):
+        A.dot(np.zeros(A.nCOLS + 1))
+    with pytest.raises(RuntimeError, match='dimensions do not match'):
+        A.T.dot(np.zeros(A.nROWS - 1))
+
+
+@pytest.mark.parametrize('name', ['szb', 'multi_rf', 'eval_gaps'])
+def test_unsorted_dictionary_gives_same_operator(name):
+    """The device re-layout sorts; a shuffled dictionary defines the same A."""
+    c = G.load_case(name)
+    D = c['D']
+    rng = np.random.default_rng(0)
+    p = rng.permutation(D['IC']['n'])
+    IC = dict(D['IC'])
+    for k in ('str', 'vox', 'dir', 'len'):
+        IC[k] = np.ascontiguousarray(IC[k][p])
+    D2 = {'IC': IC, 'EC': D['EC'], 'ISO': D['ISO']}
+    A = _op(c, D=D2)
+    assert G.rel(A.dot(c['x_in']), c['Ax']) <= TOL
+    assert G.rel(A.T.dot(c['y_in']), c['Aty']) <= TOL
+
+
+@pytest.mark.parametrize('name', CASES)
+def test_dot_product_identity(name):
+    c = G.load_case(name)
+    A = _op(c)
+    rng = np.random.default_rng(1)
+    x = rng.normal(size=A.nCOLS)
+    y = rng.normal(size=A.nROWS)
+    lhs = float(np.dot(A.dot(x), y))
+    rhs = float(np.dot(x, A.T.dot(y)))
+    assert abs(lhs - rhs) <= 1e-11 * max(1.0, abs(lhs))
+
+
+def test_invalid_dictionary_is_rejected():
+    from commit_gb300._lib import CgbError
+    c = G.load_case('szb')
+    D = c['D']
+    IC = dict(D['IC'])
+    IC['vox'] = IC['vox'].copy()
+    IC['vox'][3] = D['IC']['nVOX'] + 5
+    with pytest.raises(CgbError, match='IC voxel index'):
+        _op(c, D={'IC': IC, 'EC': D['EC'], 'ISO': D['ISO']})
+
+
+def test_demo_scale_against_oracle():
+    """The 5k-streamline demo workload (nS=66, ~580k segments) against the C port."""
+    from commit_gb300 import synth
+    from commit_gb300.operator import LinearOperator
+    D, K = synth.make_dictionary(synth.SPECS['demo_5k'])
+    P = O.PortOperator(D, K, None, nthreads=8)
+    rng = np.random.default_rng(2)
+    x = rng.uniform(-0.2, 1.0, size=P.nCOLS)
+    y = rng.normal(size=P.nROWS)
+    ax, aty = P.dot(x), P.T.dot(y)
+    for arith in ('ff', 'f64'):
+        A = LinearOperator(D, K, None, arith=arith)
+        assert G.rel(A.dot(x), ax) <= TOL
+        assert G.rel(A.T.dot(y), aty) <= TOL
+
+
+def test_repeatable_bitwise():
+    c = G.load_case('szb')
+    A = _op(c)
+    a1 = A.T.dot(c['y_in'])
+    a2 = A.T.dot(c['y_in'])
+    assert np.array_equal(a1, a2)
