@@ -14,9 +14,9 @@
 // (coalesced), the coefficient c = l*x*eval is formed once by the loading lane and
 // broadcast with shuffles, and every lane streams its slice of the LUT row.  Output rows
 // are written once, so A needs no zero fill and no atomics.  A' runs the same voxel pass:
-// each lane accumulates partial dot products for a batch of LPV segments, a shared-memory
-// transpose hands lane t the LPV partials of segment t, and the per-segment terms l*<L,y>
-// go to a scratch stream in voxel order; a second pass sums them per fibre through the
+// each lane accumulates partial dot products for a batch of 8 segments, a butterfly
+// reduce-scatter across the group leaves each segment's total in one lane, and the
+// per-segment terms l*<L,y> go to a scratch stream in voxel order; a second pass sums them per fibre through the
 // fibre-ordered index (deterministic, no atomics).  EC/ISO outputs are owned by one voxel
 // and are written directly by the first pass.
 //
@@ -39,6 +39,9 @@ struct ArF64 {
     __device__ static __forceinline__ bool nz(const Coef &c) { return c != 0.0; }
     __device__ static __forceinline__ Coef shfl(unsigned m, const Coef &c, int src, int w) {
         return __shfl_sync(m, c, src, w);
+    }
+    __device__ static __forceinline__ Acc shfl_xor(unsigned m, const Acc &a, int lm, int w) {
+        return __shfl_xor_sync(m, a, lm, w);
     }
     __device__ static __forceinline__ void fma_(Acc &a, const Coef &c, float L) { a = fma(c, (double)L, a); }
     __device__ static __forceinline__ void add(Acc &a, const Acc &b) { a += b; }
@@ -64,6 +67,12 @@ struct ArFF {
         Coef r;
         r.h = __shfl_sync(m, c.h, src, w);
         r.l = __shfl_sync(m, c.l, src, w);
+        return r;
+    }
+    __device__ static __forceinline__ Acc shfl_xor(unsigned m, const Acc &a, int lm, int w) {
+        Acc r;
+        r.s = __shfl_xor_sync(m, a.s, lm, w);
+        r.e = __shfl_xor_sync(m, a.e, lm, w);
         return r;
     }
     // a += (c.h + c.l) * L with an exact two-product of the high word and a two-sum
@@ -248,36 +257,43 @@ __global__ void __launch_bounds__(kBlock) k_forward(const OpDev P, const double 
 }
 
 // ------------------------------------------------------------------ adjoint
-// Group-wide dot products <LUT row of item t, z> for up to LPV items; lane `sub` returns
-// the total of item `sub`.  red: this group's LPV x (LPV+1) shared-memory tile.
-template <int LPV, int NCH, class AR>
+// Dot products <LUT row of item q, z> for the B = min(8, LPV) items of a sub-batch
+// (row(q) gives item q's LUT offset; only q < cnt are computed).  Each lane holds partial
+// sums over its samples; a butterfly reduce-scatter across the group leaves the total of
+// item q = sub / (LPV / B) in lane sub -- no shared memory, about two shuffles and one
+// error-free add per item and lane.
+template <int LPV, int NCH, class AR, class RowFn>
 __device__ __forceinline__ typename AR::Acc batch_dots(const Group<LPV> &G, const float *__restrict__ lut,
-                                                       uint32_t row, int cnt, int nS,
-                                                       const typename AR::Coef (&z)[NCH],
-                                                       typename AR::Acc *__restrict__ red) {
-    typename AR::Acc part[LPV];
+                                                       RowFn row, int cnt, int nS,
+                                                       const typename AR::Coef (&z)[NCH]) {
+    constexpr int B = LPV < 8 ? LPV : 8;
+    typename AR::Acc P[B];
 #pragma unroll
-    for (int t = 0; t < LPV; ++t) {
-        AR::zero(part[t]);
-        if (t < cnt) {
-            const uint32_t rt = __shfl_sync(G.mask, row, t, LPV);
-            const float *L = lut + rt;
+    for (int q = 0; q < B; ++q) {
+        AR::zero(P[q]);
+        if (q < cnt) {
+            const float *L = lut + row(q);
 #pragma unroll
             for (int k = 0; k < NCH; ++k) {
                 const int s = G.sub + k * LPV;
-                if (s < nS) AR::fma_(part[t], z[k], __ldg(L + s));
+                if (s < nS) AR::fma_(P[q], z[k], __ldg(L + s));
             }
         }
     }
-    if (LPV == 1) return part[0];
 #pragma unroll
-    for (int t = 0; t < LPV; ++t) red[t * (LPV + 1) + G.sub] = part[t];
-    __syncwarp(G.mask);
-    typename AR::Acc tot = red[G.sub * (LPV + 1)];
+    for (int h = B / 2, m = LPV / 2; h >= 1; h /= 2, m /= 2) {
+        const bool hi = (G.sub & m) != 0;
 #pragma unroll
-    for (int q = 1; q < LPV; ++q) AR::add(tot, red[G.sub * (LPV + 1) + q]);
-    __syncwarp(G.mask);
-    return tot;
+        for (int j = 0; j < h; ++j) {
+            const typename AR::Acc send = hi ? P[j] : P[j + h];
+            typename AR::Acc keep = hi ? P[j + h] : P[j];
+            AR::add(keep, AR::shfl_xor(G.mask, send, m, LPV));
+            P[j] = keep;
+        }
+    }
+#pragma unroll
+    for (int m = LPV / B / 2; m >= 1; m /= 2) AR::add(P[0], AR::shfl_xor(G.mask, P[0], m, LPV));
+    return P[0];
 }
 
 // in_mode 0: z = yin[v,:]
@@ -290,13 +306,14 @@ __global__ void __launch_bounds__(kBlock) k_adjoint(const OpDev P, const double 
                                                     const double *__restrict__ ax_b, double ca, double cb,
                                                     double *__restrict__ scratch, double *__restrict__ xout,
                                                     double *__restrict__ partials) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    typename AR::Acc *red =
-        reinterpret_cast<typename AR::Acc *>(smem_raw) + ((int)threadIdx.x / LPV) * LPV * (LPV + 1);
+    constexpr int B = LPV < 8 ? LPV : 8;
+    constexpr int SPAN = LPV / B;  // lanes holding the same item after the reduce-scatter
     const Group<LPV> G;
     const int gpb = kBlock / LPV;
     const int ngroups = gridDim.x * gpb;
     const int nS = P.nS;
+    const int q_me = G.sub / SPAN;
+    const bool writer = (G.sub % SPAN) == 0;
     double nrm = 0.0;
     for (int v = blockIdx.x * gpb + (int)threadIdx.x / LPV; v < P.nV; v += ngroups) {
         typename AR::Coef z[NCH];
@@ -335,7 +352,7 @@ __global__ void __launch_bounds__(kBlock) k_adjoint(const OpDev P, const double 
                 z[k] = AR::coef(zz);
             }
         }
-        // IC segments -> per-segment terms in voxel order
+        // IC segments -> per-segment terms l * <LUT, z> in voxel order
         if (P.nIC > 0) {
             const uint32_t beg = P.vox_ptr[v], end = P.vox_ptr[v + 1];
             for (uint32_t b = beg; b < end; b += LPV) {
@@ -343,11 +360,16 @@ __global__ void __launch_bounds__(kBlock) k_adjoint(const OpDev P, const double 
                 const bool valid = j < end;
                 const uint32_t o = valid ? P.seg_o[j] : 0;
                 const float l = valid ? P.seg_l[j] : 0.f;
-                const int cnt = min((int)(end - b), LPV);
+                const int cntL = min((int)(end - b), LPV);
                 for (int i = 0; i < P.nIC; ++i) {
                     const uint32_t row = ((uint32_t)i * P.ndirs + o) * (uint32_t)nS;
-                    const typename AR::Acc tot = batch_dots<LPV, NCH, AR>(G, P.lutIC, row, cnt, nS, z, red);
-                    if (valid) scratch[(size_t)i * P.n + j] = (double)l * AR::val(tot);
+                    for (int t0 = 0; t0 < cntL; t0 += B) {
+                        const int cnt = min(B, cntL - t0);
+                        auto rowf = [&](int q) { return __shfl_sync(G.mask, row, t0 + q, LPV); };
+                        const typename AR::Acc tot = batch_dots<LPV, NCH, AR>(G, P.lutIC, rowf, cnt, nS, z);
+                        const float lq = __shfl_sync(G.mask, l, t0 + q_me, LPV);
+                        if (writer && q_me < cnt) scratch[(size_t)i * P.n + b + t0 + q_me] = (double)lq * AR::val(tot);
+                    }
                 }
             }
         }
@@ -358,25 +380,32 @@ __global__ void __launch_bounds__(kBlock) k_adjoint(const OpDev P, const double 
                 const bool valid = j < end;
                 const uint32_t o = valid ? P.ec_o[j] : 0;
                 const uint32_t col = valid ? P.ec_col[j] : 0;
-                const int cnt = min((int)(end - b), LPV);
+                const int cntL = min((int)(end - b), LPV);
                 for (int i = 0; i < P.nEC; ++i) {
                     const uint32_t row = ((uint32_t)i * P.ndirs + o) * (uint32_t)nS;
-                    const typename AR::Acc tot = batch_dots<LPV, NCH, AR>(G, P.lutEC, row, cnt, nS, z, red);
-                    if (valid) xout[P.ec_base + (size_t)i * P.nE + col] = AR::val(tot);
+                    for (int t0 = 0; t0 < cntL; t0 += B) {
+                        const int cnt = min(B, cntL - t0);
+                        auto rowf = [&](int q) { return __shfl_sync(G.mask, row, t0 + q, LPV); };
+                        const typename AR::Acc tot = batch_dots<LPV, NCH, AR>(G, P.lutEC, rowf, cnt, nS, z);
+                        const uint32_t cq = __shfl_sync(G.mask, col, t0 + q_me, LPV);
+                        if (writer && q_me < cnt) xout[P.ec_base + (size_t)i * P.nE + cq] = AR::val(tot);
+                    }
                 }
             }
         }
         if (P.nISO > 0) {
+            // one dot product per ISO response, shared by the voxel's ISO elements
             const uint32_t beg = P.iso_ptr[v], end = P.iso_ptr[v + 1];
-            for (uint32_t b = beg; b < end; b += LPV) {
-                const uint32_t j = b + G.sub;
-                const bool valid = j < end;
-                const uint32_t col = valid ? P.iso_col[j] : 0;
-                const int cnt = min((int)(end - b), LPV);
-                for (int i = 0; i < P.nISO; ++i) {
-                    const typename AR::Acc tot =
-                        batch_dots<LPV, NCH, AR>(G, P.lutISO, (uint32_t)(i * nS), cnt, nS, z, red);
-                    if (valid) xout[P.iso_base + (size_t)i * P.nISOv + col] = AR::val(tot);
+            if (beg < end) {
+                for (int t0 = 0; t0 < P.nISO; t0 += B) {
+                    const int cnt = min(B, P.nISO - t0);
+                    auto rowf = [&](int q) { return (uint32_t)((t0 + q) * nS); };
+                    const typename AR::Acc tot = batch_dots<LPV, NCH, AR>(G, P.lutISO, rowf, cnt, nS, z);
+                    if (writer && q_me < cnt) {
+                        const double d = AR::val(tot);
+                        for (uint32_t e = beg; e < end; ++e)
+                            xout[P.iso_base + (size_t)(t0 + q_me) * P.nISOv + P.iso_col[e]] = d;
+                    }
                 }
             }
         }

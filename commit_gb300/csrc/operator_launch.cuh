@@ -91,8 +91,7 @@ struct AdjLaunch {
     int run() {
         const OpDev P = op->dev();
         auto kern = k_adjoint<L, N, AR>;
-        const size_t smem = L > 1 ? (size_t)kBlock * (L + 1) * sizeof(typename AR::Acc) : 0;
-        CGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        const size_t smem = 0;
         int g = 0;
         CGB_TRY(grid_for_kernel(kern, smem, op->nsm, op->nV, kBlock / L, &g));
         if (g > reduction_blocks(op)) g = reduction_blocks(op);

@@ -257,7 +257,9 @@ def _voxelise(spec: ProblemSpec, nctrl: np.ndarray, pts: np.ndarray, dirs: np.nd
         inm = mask_t[lin]
         lin, d, ln, fib = lin[inm], d[inm], ln[inm], fib[inm]
         u = d / ln[:, None]
-        o = torch.argmax((u @ dirs_t.T).abs(), dim=1)
+        o = torch.empty(u.shape[0], dtype=torch.int64, device=dev)
+        for r0 in range(0, u.shape[0], 1 << 20):
+            o[r0:r0 + (1 << 20)] = torch.argmax((u[r0:r0 + (1 << 20)] @ dirs_t.T).abs(), dim=1)
         # merge all steps of one fibre that share (voxel, orientation), summing their
         # lengths, as the per-fibre std::map of trk2dictionary_c.cpp:484-552 does
         if lin.numel():
