@@ -73,6 +73,8 @@ def lib() -> ctypes.CDLL:
     L.cgb_op_set_arith.argtypes = [P, c_i32]
     L.cgb_op_apply.argtypes = [P, c_i32, P, c_i64, P, c_i64, c_i32, c_i32, P]
     L.cgb_op_apply_host.argtypes = [P, c_i32, P, c_i64, P, c_i64]
+    L.cgb_op_adjoint_noalloc.argtypes = [c_i32, c_i32, c_i32, c_i64, c_i32, c_i32, c_i32, P, P,
+                                         P, P, P, P, P, P, P, P, P, P, P, c_i32, c_i32, c_i32, P, P, P]
     L.cgb_fista_run.argtypes = [P, P, P, ctypes.POINTER(CgbReg), ctypes.POINTER(CgbFistaParams), P,
                                 ctypes.POINTER(CgbFistaResult), P]
     L.cgb_prox_non_negativity.argtypes = [P, c_i64, c_i64, P]

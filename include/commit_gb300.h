@@ -106,6 +106,36 @@ int cgb_op_apply(cgb_op *op, int adjoint, const void *in, int64_t in_len, void *
  */
 int cgb_op_apply_host(cgb_op *op, int adjoint, const double *in, int64_t in_len, double *out, int64_t out_len);
 
+/*
+ * A'*y that allocates no device memory.  No counterpart in the reference.
+ *
+ * For callers that cannot let a library call cudaMalloc: an application that reserves
+ * the GPU's memory up front in its own pool (a plug-in's cudaMalloc would fail or
+ * fragment that pool), or one that issues work on a latency-critical stream and cannot
+ * accept cudaMalloc's implicit device-wide synchronisation.  Every input and output is a
+ * DEVICE buffer owned by the caller, in the reference's layout: IC segments, EC and ISO
+ * elements sorted by voxel (as load_dictionary leaves them, commit/core.pyx:508-562),
+ * the eval mask and the f32 LUTs, plus a fibre index computed once by the caller:
+ * fib_perm[n] lists segment indices grouped by fibre and fib_ptr[nF+1] gives each
+ * fibre's range (a stable argsort of ICf and its counts).  x (nF*nIC + nE*nEC +
+ * nISOv*nISO doubles) is fully written.  Float-float arithmetic, as cgb_op_apply.
+ *
+ * Working memory is a static device array of CGB_NOALLOC_MAX_TERMS doubles (8 MiB),
+ * held by every GPU that loads the library until the process exits; calls with
+ * n*nIC > CGB_NOALLOC_MAX_TERMS return CGB_ERR_UNSUPPORTED.  The first call on a device
+ * looks up that array's device address (cudaGetSymbolAddress) with the device current;
+ * make this first call before any stream capture.  All calls share the array: calls
+ * whose work overlaps on the GPU (different streams, or different host threads) race and
+ * must be serialised by the caller.  Enqueued on `stream`; returns without synchronising.
+ */
+#define CGB_NOALLOC_MAX_TERMS (1 << 20)
+int cgb_op_adjoint_noalloc(int nS, int ndirs, int nF, int64_t n, int nE, int nV, int nISOv, const double *y,
+                           double *x, const uint32_t *ICf, const uint32_t *ICeval, const uint32_t *ICv,
+                           const uint16_t *ICo, const float *ICl, const uint32_t *ECv, const uint16_t *ECo,
+                           const uint32_t *ISOv, const float *lutIC, const float *lutEC, const float *lutISO,
+                           int nIC, int nEC, int nISO, const uint32_t *fib_ptr, const uint32_t *fib_perm,
+                           void *stream);
+
 /* ------------------------------------------------------------------ regularisation */
 #define CGB_REG_NONE 0
 #define CGB_REG_LASSO 1
