@@ -42,6 +42,18 @@ int cgb_op_apply(cgb_op *op, int adjoint, const void *in, int64_t in_len, void *
         if (adjoint) return launch_adjoint(op, (const double *)in, (double *)out, st, ar);
         return launch_forward(op, (const double *)in, (double *)out, st, ar);
     }
+    if (dtype == CGB_DTYPE_F32) {
+        if (arith != CGB_ARITH_BF16 && arith != CGB_ARITH_FP16 && arith != CGB_ARITH_F32)
+            return fail(CGB_ERR_INVALID, "FP32 vectors need arith BF16, FP16 or F32");
+        if (!op->d_x64) CGB_CUDA(cudaMalloc((void **)&op->d_x64, (op->ncols > 0 ? op->ncols : 1) * sizeof(double)));
+        if (!adjoint) {
+            CGB_TRY(convert_f32_to_f64((const float *)in, op->d_x64, op->ncols, st));
+            return launch_resnorm_mix(op, op->d_x64, nullptr, nullptr, nullptr, nullptr, (float *)out, st, arith,
+                                      nullptr);
+        }
+        CGB_TRY(launch_adjoint_mix(op, (const float *)in, op->d_x64, st, arith));
+        return convert_f64_to_f32(op->d_x64, (float *)out, op->ncols, st);
+    }
     return fail(CGB_ERR_UNSUPPORTED, "unsupported dtype / arithmetic combination");
 }
 

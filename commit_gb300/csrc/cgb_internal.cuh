@@ -65,12 +65,17 @@ struct cgb_op {
     int nS, ndirs, nF, nE, nV, nISOv, nIC, nEC, nISO, nolut;
     int64_t n, nrows, ncols;
     int arith;
+    int ff_variant;                 // float-float kernels: 0 scalar samples, 1 packed pairs
     int lpv;                        // lanes per voxel (1..32)
     // device buffers (owned)
     float *lutIC, *lutEC, *lutISO;
+    float *lutIC_p, *lutEC_p, *lutISO_p;  // zero-padded rows of stride nSp (paired kernels)
+    int nSp;
     void *lutIC_r, *lutEC_r;        // reduced-precision LUT copies
     int lut_r_kind;                 // CGB_ARITH_BF16 / CGB_ARITH_FP16 / 0
-    __half *seg_l16;
+    __half *seg_l16;                // FP16 lengths scaled by 2^k (reduced path)
+    float len16_inv_scale;          // 2^-k
+    double *d_x64;                  // [ncols] staging for FP32 applies
     uint32_t *vox_ptr, *seg_f, *eval, *fib_ptr, *fib_perm, *ec_ptr, *ec_col, *iso_ptr, *iso_col;
     uint16_t *seg_o, *ec_o;
     float *seg_l;
@@ -84,6 +89,9 @@ struct cgb_op {
     size_t bytes;
     int nsm;
     cgb::OpDev dev() const;
+    // reduced-precision LUT rows (padded pair layout) for CGB_ARITH_BF16 / FP16 / F32
+    const void *lut_r_ic(int kind) const { return kind == CGB_ARITH_F32 ? (const void *)lutIC_p : lutIC_r; }
+    const void *lut_r_ec(int kind) const { return kind == CGB_ARITH_F32 ? (const void *)lutEC_p : lutEC_r; }
 };
 
 namespace cgb {
@@ -99,4 +107,14 @@ int launch_gradient_grid(cgb_op *op, const double *x, const double *y, const dou
                          double *partials, const double *ax_a, const double *ax_b, double ca, double cb,
                          cudaStream_t st, int arith, int *grid);
 int reduction_blocks(const cgb_op *op);
+// reduced-precision path (mixed.cu): FP32 rows, FP64 columns
+int ensure_reduced(cgb_op *op, int arith);
+int launch_resnorm_mix(cgb_op *op, const double *x, const float *y, const float *sqw, double *partials,
+                       float *ax_out, float *yout, cudaStream_t st, int arith, int *grid);
+int launch_gradient_mix(cgb_op *op, const double *x, const float *y, const float *sqw, double *grad,
+                        double *partials, const float *ax_a, const float *ax_b, float ca, float cb,
+                        cudaStream_t st, int arith, int *grid);
+int launch_adjoint_mix(cgb_op *op, const float *yin, double *xout, cudaStream_t st, int arith);
+int convert_f64_to_f32(const double *in, float *out, int64_t n, cudaStream_t st);
+int convert_f32_to_f64(const float *in, double *out, int64_t n, cudaStream_t st);
 }  // namespace cgb

@@ -239,9 +239,11 @@ struct FistaWS {
     int64_t ncols = 0, nrows = 0;
     double *xhat = nullptr, *prev = nullptr, *grad = nullptr, *ax[2] = {nullptr, nullptr};
     double *pstats = nullptr, *pgrp = nullptr, *pres = nullptr;
+    // reduced-precision path: FP32 copies of y and sqrt(W), FP32 A*x buffers
+    float *y32 = nullptr, *sqw32 = nullptr, *ax32[2] = {nullptr, nullptr};
     ~FistaWS() {
-        double *ps[] = {xhat, prev, grad, ax[0], ax[1], pstats, pgrp, pres};
-        for (double *p : ps)
+        void *ps[] = {xhat, prev, grad, ax[0], ax[1], pstats, pgrp, pres, y32, sqw32, ax32[0], ax32[1]};
+        for (void *p : ps)
             if (p) cudaFree(p);
     }
 };
@@ -266,13 +268,28 @@ struct Solver {
     double group_omega_coef = 0.0;
     int calls = 0;
 
+    bool mixed = false;
+
     int init() {
         const int64_t nc = op->ncols, nr = op->nrows;
         const int rb = reduction_blocks(op);
+        mixed = prm->arith == CGB_ARITH_BF16 || prm->arith == CGB_ARITH_FP16 || prm->arith == CGB_ARITH_F32;
         CGB_TRY(ws_alloc(&ws.xhat, nc));
         CGB_TRY(ws_alloc(&ws.prev, nc));
         CGB_TRY(ws_alloc(&ws.grad, nc));
-        if (prm->momentum_reuse) {
+        if (mixed) {
+            CGB_TRY(ensure_reduced(op, prm->arith));
+            CGB_CUDA(cudaMalloc((void **)&ws.y32, (nr > 0 ? nr : 1) * sizeof(float)));
+            CGB_TRY(convert_f64_to_f32(y, ws.y32, nr, st));
+            if (sqw) {
+                CGB_CUDA(cudaMalloc((void **)&ws.sqw32, (nr > 0 ? nr : 1) * sizeof(float)));
+                CGB_TRY(convert_f64_to_f32(sqw, ws.sqw32, nr, st));
+            }
+            if (prm->momentum_reuse) {
+                CGB_CUDA(cudaMalloc((void **)&ws.ax32[0], (nr > 0 ? nr : 1) * sizeof(float)));
+                CGB_CUDA(cudaMalloc((void **)&ws.ax32[1], (nr > 0 ? nr : 1) * sizeof(float)));
+            }
+        } else if (prm->momentum_reuse) {
             CGB_TRY(ws_alloc(&ws.ax[0], nr));
             CGB_TRY(ws_alloc(&ws.ax[1], nr));
         }
@@ -393,10 +410,16 @@ struct Solver {
         return om;
     }
 
-    // |sqw*(A x - y)|^2 -> dscal[0]; optionally A x -> ax
-    int objective(const double *x, double *ax) {
+    // |sqw*(A x - y)|^2 -> dscal[0]; with slot >= 0, A x -> A*x buffer `slot`
+    int objective(const double *x, int slot) {
         int g = 0;
-        CGB_TRY(launch_resnorm_grid(op, x, y, sqw, op->partials, ax, st, prm->arith, &g));
+        if (mixed) {
+            CGB_TRY(launch_resnorm_mix(op, x, ws.y32, ws.sqw32, op->partials, slot >= 0 ? ws.ax32[slot] : nullptr,
+                                       nullptr, st, prm->arith, &g));
+        } else {
+            CGB_TRY(launch_resnorm_grid(op, x, y, sqw, op->partials, slot >= 0 ? ws.ax[slot] : nullptr, st,
+                                        prm->arith, &g));
+        }
         calls++;
         if (g > 0) {
             CGB_TRY(finalize(op->partials, g, 1, op->dscal + 0, st));
@@ -406,11 +429,17 @@ struct Solver {
         return CGB_OK;
     }
 
-    // grad = A'(W (A x - y)) (or from the A x combination), |r|^2 -> dscal[10]
-    int gradient(const double *x, double *grad, const double *ax_a, const double *ax_b, double ca, double cb) {
+    // grad = A'(W (A x - y)) (or, with sa >= 0, A x = ca*ax[sa] + cb*ax[sb]), |r|^2 -> dscal[10]
+    int gradient(const double *x, double *grad, int sa, int sb, double ca, double cb) {
         int g = 0;
-        CGB_TRY(launch_gradient_grid(op, x, y, sqw, grad, ws.pres, ax_a, ax_b, ca, cb, st, prm->arith, &g));
-        calls += ax_a ? 1 : 2;
+        if (mixed) {
+            CGB_TRY(launch_gradient_mix(op, x, ws.y32, ws.sqw32, grad, ws.pres, sa >= 0 ? ws.ax32[sa] : nullptr,
+                                        sb >= 0 ? ws.ax32[sb] : nullptr, (float)ca, (float)cb, st, prm->arith, &g));
+        } else {
+            CGB_TRY(launch_gradient_grid(op, x, y, sqw, grad, ws.pres, sa >= 0 ? ws.ax[sa] : nullptr,
+                                         sb >= 0 ? ws.ax[sb] : nullptr, ca, cb, st, prm->arith, &g));
+        }
+        calls += sa >= 0 ? 1 : 2;
         if (g > 0) {
             CGB_TRY(finalize(ws.pres, g, 1, op->dscal + 10, st));
         } else {
@@ -433,7 +462,7 @@ struct Solver {
         int backtracks = 0;
         // initialisation (solvers.py:260-286)
         CGB_CUDA(cudaMemcpyAsync(ws.xhat, x, nc * sizeof(double), cudaMemcpyDeviceToDevice, st));
-        CGB_TRY(gradient(ws.xhat, ws.grad, nullptr, nullptr, 0.0, 0.0));
+        CGB_TRY(gradient(ws.xhat, ws.grad, -1, -1, 0.0, 0.0));
         CGB_TRY(prox(ws.xhat, ws.xhat, nullptr, 0.0, 1.0));
         CGB_TRY(stats(ws.xhat, nullptr, nullptr, nullptr));
         CGB_TRY(fetch(h));
@@ -449,7 +478,12 @@ struct Solver {
             k_dot<<<elem_grid(op, nc), kBlock, 0, st>>>(ws.grad, ws.grad, nc, ws.pstats);
             CGB_CUDA(cudaGetLastError());
             CGB_TRY(finalize(ws.pstats, elem_grid(op, nc), 1, op->dscal + 11, st));
-            CGB_TRY(launch_resnorm_grid(op, ws.grad, nullptr, sqw, op->partials, nullptr, st, prm->arith, &g));
+            if (mixed) {
+                CGB_TRY(launch_resnorm_mix(op, ws.grad, nullptr, ws.sqw32, op->partials, nullptr, nullptr, st,
+                                           prm->arith, &g));
+            } else {
+                CGB_TRY(launch_resnorm_grid(op, ws.grad, nullptr, sqw, op->partials, nullptr, st, prm->arith, &g));
+            }
             calls++;
             if (g > 0) {
                 CGB_TRY(finalize(op->partials, g, 1, op->dscal + 12, st));
@@ -476,7 +510,7 @@ struct Solver {
             auto eval_x = [&](double s) -> int {
                 CGB_TRY(prox(x, ws.xhat, ws.grad, s, s));
                 CGB_TRY(stats(x, ws.xhat, ws.grad, ws.prev));
-                CGB_TRY(objective(x, prm->momentum_reuse ? ws.ax[cur] : nullptr));
+                CGB_TRY(objective(x, prm->momentum_reuse ? cur : -1));
                 return fetch(h);
             };
             CGB_TRY(eval_x(step));
@@ -514,10 +548,9 @@ struct Solver {
             CGB_CUDA(cudaGetLastError());
             if (prm->momentum_reuse && (c == 0.0 || have_prev_ax)) {
                 // A*xhat = (1+c) A*x - c A*prev_x
-                CGB_TRY(gradient(ws.xhat, ws.grad, ws.ax[cur], have_prev_ax ? ws.ax[1 - cur] : ws.ax[cur], 1.0 + c,
-                                 -c));
+                CGB_TRY(gradient(ws.xhat, ws.grad, cur, have_prev_ax ? 1 - cur : cur, 1.0 + c, -c));
             } else {
-                CGB_TRY(gradient(ws.xhat, ws.grad, nullptr, nullptr, 0.0, 0.0));
+                CGB_TRY(gradient(ws.xhat, ws.grad, -1, -1, 0.0, 0.0));
             }
             if (prm->momentum_reuse) {
                 cur = 1 - cur;
@@ -570,8 +603,8 @@ extern "C" {
 int cgb_fista_run(cgb_op *op, const double *y, const double *sqrt_w, const cgb_reg *reg,
                   const cgb_fista_params *params, double *x, cgb_fista_result *result, void *stream) {
     if (!op || !y || !reg || !params || !x || !result) return fail(CGB_ERR_INVALID, "null argument");
-    if (params->arith != CGB_ARITH_F64 && params->arith != CGB_ARITH_FF)
-        return fail(CGB_ERR_INVALID, "FISTA arith must be F64 or FF");
+    if (params->arith < CGB_ARITH_F64 || params->arith > CGB_ARITH_F32)
+        return fail(CGB_ERR_INVALID, "unknown FISTA arith");
     if (reg->reg_ec > CGB_REG_LASSO || reg->reg_iso > CGB_REG_LASSO)
         return fail(CGB_ERR_INVALID, "EC/ISO regularisers must be none or lasso");
     if ((reg->reg_ic == CGB_REG_GROUP_LASSO || reg->reg_ic == CGB_REG_SPARSE_GROUP_LASSO) && reg->ngroups > 0 &&

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "cgb_internal.cuh"
+#include "operator_pair.cuh"
 
 namespace cgb {
 
@@ -184,10 +185,10 @@ using namespace cgb;
 
 static void free_op(cgb_op *op) {
     if (!op) return;
-    void *ptrs[] = {op->lutIC, op->lutEC, op->lutISO, op->lutIC_r, op->lutEC_r, op->seg_l16, op->vox_ptr,
+    void *ptrs[] = {op->lutIC, op->lutEC, op->lutISO, op->lutIC_p, op->lutEC_p, op->lutISO_p, op->lutIC_r, op->lutEC_r, op->seg_l16, op->vox_ptr,
                     op->seg_f, op->eval, op->fib_ptr, op->fib_perm, op->ec_ptr, op->ec_col, op->iso_ptr,
                     op->iso_col, op->seg_o, op->ec_o, op->seg_l, op->scratch, op->scratch32, op->partials,
-                    op->dscal, op->d_in, op->d_out};
+                    op->dscal, op->d_in, op->d_out, op->d_x64};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (op->h_scal) cudaFreeHost(op->h_scal);
@@ -234,6 +235,11 @@ static int create_impl(int device, int nS, int ndirs, int nF, int64_t n, int nE,
     op->nrows = (int64_t)nV * nS;
     op->ncols = (int64_t)nF * nIC + (int64_t)nE * nEC + (int64_t)nISOv * nISO;
     op->arith = arith;
+    {
+        // float-float kernel family: packed pairs (default) or scalar samples
+        const char *v = getenv("CGB_FF_KERNEL");
+        op->ff_variant = (v && strcmp(v, "scalar") == 0) ? 0 : 1;
+    }
     CGB_CUDA(cudaDeviceGetAttribute(&op->nsm, cudaDevAttrMultiProcessorCount, device));
     // lanes per voxel: whole warps for long sample vectors, sub-warps for short ones
     if (nS >= 96) op->lpv = 32;
@@ -284,6 +290,27 @@ static int create_impl(int device, int nS, int ndirs, int nF, int64_t n, int nE,
     CGB_TRY(dalloc(op, &op->lutIC, lutIC_n)); CGB_TRY(upload(op->lutIC, lutIC, nolut ? 0 : lutIC_n));
     CGB_TRY(dalloc(op, &op->lutEC, lutEC_n)); CGB_TRY(upload(op->lutEC, lutEC, nolut ? 0 : lutEC_n));
     CGB_TRY(dalloc(op, &op->lutISO, lutISO_n)); CGB_TRY(upload(op->lutISO, lutISO, nolut ? 0 : lutISO_n));
+    // zero-padded copies with row stride nSp for the paired float-float kernels
+    {
+        const detail::PairShape ps = detail::pick_pair_shape(nS);
+        op->nSp = 2 * ps.lpv * ps.np;
+        const size_t sp = (size_t)op->nSp;
+        CGB_TRY(dalloc(op, &op->lutIC_p, (size_t)nIC * op->ndirs * sp));
+        CGB_TRY(dalloc(op, &op->lutEC_p, (size_t)nEC * op->ndirs * sp));
+        CGB_TRY(dalloc(op, &op->lutISO_p, (size_t)nISO * sp));
+        auto padded = [&](size_t rows) { return (rows * sp > 0 ? rows * sp : 1) * sizeof(float); };
+        CGB_CUDA(cudaMemset(op->lutIC_p, 0, padded((size_t)nIC * op->ndirs)));
+        CGB_CUDA(cudaMemset(op->lutEC_p, 0, padded((size_t)nEC * op->ndirs)));
+        CGB_CUDA(cudaMemset(op->lutISO_p, 0, padded((size_t)nISO)));
+        if (!nolut) {
+            if (lutIC_n) CGB_CUDA(cudaMemcpy2D(op->lutIC_p, sp * sizeof(float), lutIC, nS * sizeof(float),
+                                               nS * sizeof(float), (size_t)nIC * op->ndirs, cudaMemcpyHostToDevice));
+            if (lutEC_n) CGB_CUDA(cudaMemcpy2D(op->lutEC_p, sp * sizeof(float), lutEC, nS * sizeof(float),
+                                               nS * sizeof(float), (size_t)nEC * op->ndirs, cudaMemcpyHostToDevice));
+            if (lutISO_n) CGB_CUDA(cudaMemcpy2D(op->lutISO_p, sp * sizeof(float), lutISO, nS * sizeof(float),
+                                                nS * sizeof(float), (size_t)nISO, cudaMemcpyHostToDevice));
+        }
+    }
     CGB_TRY(dalloc(op, &op->eval, (size_t)nF * (nIC > 0 ? nIC : 1)));
     if (ICeval) {
         CGB_TRY(upload(op->eval, ICeval, (size_t)nF * nIC));

@@ -1,0 +1,206 @@
+// Reduced-precision operator path: on-demand BF16/FP16 LUT copies and FP16 lengths, launch
+// of the mixed kernels (operator_mixed_*.cu) and the per-fibre FP64 sum of FP32 terms.
+#include <math.h>
+
+#include "cgb_internal.cuh"
+
+namespace cgb {
+
+int forward_mix_bf16(cgb_op *, const double *, float *, float *, const float *, const float *, double *,
+                     cudaStream_t, int *);
+int forward_mix_fp16(cgb_op *, const double *, float *, float *, const float *, const float *, double *,
+                     cudaStream_t, int *);
+int forward_mix_f32(cgb_op *, const double *, float *, float *, const float *, const float *, double *,
+                    cudaStream_t, int *);
+int adjoint_mix_bf16(cgb_op *, const float *, int, const double *, const float *, const float *, const float *,
+                     const float *, float, float, double *, double *, cudaStream_t, int *);
+int adjoint_mix_fp16(cgb_op *, const float *, int, const double *, const float *, const float *, const float *,
+                     const float *, float, float, double *, double *, cudaStream_t, int *);
+int adjoint_mix_f32(cgb_op *, const float *, int, const double *, const float *, const float *, const float *,
+                    const float *, float, float, double *, double *, cudaStream_t, int *);
+
+namespace {
+
+__global__ void k_to_bf16(const float *in, __nv_bfloat16 *out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = __float2bfloat16_rn(in[i]);
+}
+
+__global__ void k_to_fp16(const float *in, __half *out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = __float2half_rn(in[i]);
+}
+
+__global__ void k_len16(const float *in, __half *out, size_t n, float scale) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = __float2half_rn(in[i] * scale);
+}
+
+__global__ void k_maxabs(const float *in, size_t n, unsigned int *out) {
+    float m = 0.f;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        m = fmaxf(m, fabsf(in[i]));
+    // non-negative floats order like their bit patterns
+    atomicMax(out, __float_as_uint(m));
+}
+
+__global__ void k_f64_to_f32(const double *in, float *out, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (float)in[i];
+}
+
+__global__ void k_f32_to_f64(const float *in, double *out, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (double)in[i];
+}
+
+__global__ void k_fibre_sum32(const OpDev P, const float *__restrict__ scr, double *__restrict__ xout) {
+    const int64_t total = (int64_t)P.nF * P.nIC;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(q / P.nF);
+        const uint32_t f = (uint32_t)(q - (int64_t)i * P.nF);
+        const float *S = scr + (size_t)i * P.n;
+        double s = 0.0;
+        for (uint32_t k = P.fib_ptr[f]; k < P.fib_ptr[f + 1]; ++k) s += (double)S[P.fib_perm[k]];
+        xout[q] = s * (double)P.eval[q];
+    }
+}
+
+int grid_n(size_t n) {
+    size_t g = (n + 255) / 256;
+    if (g > 4096) g = 4096;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+int fibre_sum32(cgb_op *op, double *xout, cudaStream_t st) {
+    if (op->nIC > 0 && op->nF > 0) {
+        const int64_t total = (int64_t)op->nF * op->nIC;
+        int gb = (int)((total + 255) / 256);
+        if (gb > op->nsm * 16) gb = op->nsm * 16;
+        k_fibre_sum32<<<gb, 256, 0, st>>>(op->dev(), op->scratch32, xout);
+        CGB_CUDA(cudaGetLastError());
+    }
+    return CGB_OK;
+}
+
+}  // namespace
+
+int convert_f64_to_f32(const double *in, float *out, int64_t n, cudaStream_t st) {
+    if (n <= 0) return CGB_OK;
+    k_f64_to_f32<<<grid_n(n), 256, 0, st>>>(in, out, n);
+    CGB_CUDA(cudaGetLastError());
+    return CGB_OK;
+}
+
+int convert_f32_to_f64(const float *in, double *out, int64_t n, cudaStream_t st) {
+    if (n <= 0) return CGB_OK;
+    k_f32_to_f64<<<grid_n(n), 256, 0, st>>>(in, out, n);
+    CGB_CUDA(cudaGetLastError());
+    return CGB_OK;
+}
+
+int ensure_reduced(cgb_op *op, int arith) {
+    if (arith != CGB_ARITH_BF16 && arith != CGB_ARITH_FP16 && arith != CGB_ARITH_F32)
+        return fail(CGB_ERR_INVALID, "reduced-precision arith must be BF16, FP16 or F32");
+    if (op->nolut) return fail(CGB_ERR_UNSUPPORTED, "the reduced-precision path needs a LUT operator");
+    if (!op->scratch32) {
+        CGB_CUDA(cudaMalloc((void **)&op->scratch32, (size_t)(op->n > 0 ? op->n : 1) * (op->nIC > 0 ? op->nIC : 1) *
+                                                         sizeof(float)));
+        op->bytes += (size_t)op->n * op->nIC * sizeof(float);
+    }
+    if (arith == CGB_ARITH_F32) return CGB_OK;
+    if (op->lut_r_kind != arith) {
+        if (op->lutIC_r) cudaFree(op->lutIC_r);
+        if (op->lutEC_r) cudaFree(op->lutEC_r);
+        op->lutIC_r = op->lutEC_r = nullptr;
+        const size_t nic = (size_t)op->nIC * op->ndirs * op->nSp, nec = (size_t)op->nEC * op->ndirs * op->nSp;
+        CGB_CUDA(cudaMalloc(&op->lutIC_r, (nic ? nic : 1) * 2));
+        CGB_CUDA(cudaMalloc(&op->lutEC_r, (nec ? nec : 1) * 2));
+        if (arith == CGB_ARITH_BF16) {
+            if (nic) k_to_bf16<<<grid_n(nic), 256>>>(op->lutIC_p, (__nv_bfloat16 *)op->lutIC_r, nic);
+            if (nec) k_to_bf16<<<grid_n(nec), 256>>>(op->lutEC_p, (__nv_bfloat16 *)op->lutEC_r, nec);
+        } else {
+            if (nic) k_to_fp16<<<grid_n(nic), 256>>>(op->lutIC_p, (__half *)op->lutIC_r, nic);
+            if (nec) k_to_fp16<<<grid_n(nec), 256>>>(op->lutEC_p, (__half *)op->lutEC_r, nec);
+        }
+        CGB_CUDA(cudaGetLastError());
+        op->lut_r_kind = arith;
+    }
+    if (!op->seg_l16 && op->n > 0) {
+        // lengths as FP16 of l * 2^k, with the largest length just below 2^15
+        unsigned int *dmax;
+        CGB_CUDA(cudaMalloc((void **)&dmax, sizeof(unsigned int)));
+        CGB_CUDA(cudaMemset(dmax, 0, sizeof(unsigned int)));
+        k_maxabs<<<grid_n(op->n), 256>>>(op->seg_l, op->n, dmax);
+        unsigned int hb = 0;
+        cudaError_t e = cudaMemcpy(&hb, dmax, sizeof(hb), cudaMemcpyDeviceToHost);
+        cudaFree(dmax);
+        CGB_CUDA(e);
+        float mx;
+        memcpy(&mx, &hb, 4);
+        int k = 0;
+        if (mx > 0.f && isfinite(mx)) k = (int)floor(log2(32768.0 / mx));
+        if (k > 60) k = 60;
+        if (k < -60) k = -60;
+        CGB_CUDA(cudaMalloc((void **)&op->seg_l16, (size_t)op->n * sizeof(__half)));
+        op->bytes += (size_t)op->n * sizeof(__half);
+        k_len16<<<grid_n(op->n), 256>>>(op->seg_l, op->seg_l16, op->n, ldexpf(1.f, k));
+        CGB_CUDA(cudaGetLastError());
+        op->len16_inv_scale = ldexpf(1.f, -k);
+    }
+    CGB_CUDA(cudaDeviceSynchronize());
+    return CGB_OK;
+}
+
+static int fwd_mix(cgb_op *op, int arith, const double *x, float *y, float *ax, const float *yobs, const float *sqw,
+                   double *partials, cudaStream_t st, int *grid) {
+    if (arith == CGB_ARITH_BF16) return forward_mix_bf16(op, x, y, ax, yobs, sqw, partials, st, grid);
+    if (arith == CGB_ARITH_FP16) return forward_mix_fp16(op, x, y, ax, yobs, sqw, partials, st, grid);
+    return forward_mix_f32(op, x, y, ax, yobs, sqw, partials, st, grid);
+}
+
+static int adj_mix(cgb_op *op, int arith, const float *yin, int mode, const double *x, const float *yobs,
+                   const float *sqw, const float *ax_a, const float *ax_b, float ca, float cb, double *xout,
+                   double *partials, cudaStream_t st, int *grid) {
+    if (arith == CGB_ARITH_BF16)
+        return adjoint_mix_bf16(op, yin, mode, x, yobs, sqw, ax_a, ax_b, ca, cb, xout, partials, st, grid);
+    if (arith == CGB_ARITH_FP16)
+        return adjoint_mix_fp16(op, yin, mode, x, yobs, sqw, ax_a, ax_b, ca, cb, xout, partials, st, grid);
+    return adjoint_mix_f32(op, yin, mode, x, yobs, sqw, ax_a, ax_b, ca, cb, xout, partials, st, grid);
+}
+
+int launch_resnorm_mix(cgb_op *op, const double *x, const float *y, const float *sqw, double *partials,
+                       float *ax_out, float *yout, cudaStream_t st, int arith, int *grid) {
+    if (grid) *grid = 0;
+    CGB_TRY(ensure_reduced(op, arith));
+    if (op->nV == 0) return CGB_OK;
+    return fwd_mix(op, arith, x, yout, ax_out, y, sqw, partials, st, grid);
+}
+
+int launch_gradient_mix(cgb_op *op, const double *x, const float *y, const float *sqw, double *grad,
+                        double *partials, const float *ax_a, const float *ax_b, float ca, float cb,
+                        cudaStream_t st, int arith, int *grid) {
+    if (grid) *grid = 0;
+    CGB_TRY(ensure_reduced(op, arith));
+    if (op->nV == 0) {
+        if (op->ncols > 0) CGB_CUDA(cudaMemsetAsync(grad, 0, op->ncols * sizeof(double), st));
+        return CGB_OK;
+    }
+    CGB_TRY(adj_mix(op, arith, nullptr, ax_a ? 2 : 1, x, y, sqw, ax_a, ax_b, ca, cb, grad, partials, st, grid));
+    return fibre_sum32(op, grad, st);
+}
+
+int launch_adjoint_mix(cgb_op *op, const float *yin, double *xout, cudaStream_t st, int arith) {
+    CGB_TRY(ensure_reduced(op, arith));
+    if (op->nV == 0) {
+        if (op->ncols > 0) CGB_CUDA(cudaMemsetAsync(xout, 0, op->ncols * sizeof(double), st));
+        return CGB_OK;
+    }
+    CGB_TRY(adj_mix(op, arith, yin, 0, nullptr, nullptr, nullptr, nullptr, nullptr, 0.f, 0.f, xout, nullptr, st,
+                    nullptr));
+    return fibre_sum32(op, xout, st);
+}
+
+}  // namespace cgb

@@ -9,6 +9,11 @@ int forward_f64(cgb_op *op, const double *x, double *y, double *ax, const double
 int adjoint_f64(cgb_op *op, const double *yin, int in_mode, const double *x, const double *yobs,
                 const double *sqw, const double *ax_a, const double *ax_b, double ca, double cb, double *xout,
                 double *partials, cudaStream_t st, int *grid);
+int forward_ffs(cgb_op *op, const double *x, double *y, double *ax, const double *yobs, const double *sqw,
+                double *partials, cudaStream_t st, int *grid);
+int adjoint_ffs(cgb_op *op, const double *yin, int in_mode, const double *x, const double *yobs,
+                const double *sqw, const double *ax_a, const double *ax_b, double ca, double cb, double *xout,
+                double *partials, cudaStream_t st, int *grid);
 int forward_ff(cgb_op *op, const double *x, double *y, double *ax, const double *yobs, const double *sqw,
                double *partials, cudaStream_t st, int *grid);
 int adjoint_ff(cgb_op *op, const double *yin, int in_mode, const double *x, const double *yobs,
@@ -130,6 +135,7 @@ static int run_forward(cgb_op *op, const double *x, double *y, double *ax, const
         return CGB_OK;
     }
     if (arith == CGB_ARITH_F64) return forward_f64(op, x, y, ax, yobs, sqw, partials, st, grid_out);
+    if (op->ff_variant == 0) return forward_ffs(op, x, y, ax, yobs, sqw, partials, st, grid_out);
     return forward_ff(op, x, y, ax, yobs, sqw, partials, st, grid_out);
 }
 
@@ -151,6 +157,8 @@ static int run_adjoint(cgb_op *op, const double *yin, int in_mode, const double 
         if (grid_out) *grid_out = g;
     } else if (arith == CGB_ARITH_F64) {
         CGB_TRY(adjoint_f64(op, yin, in_mode, x, yobs, sqw, ax_a, ax_b, ca, cb, xout, partials, st, grid_out));
+    } else if (op->ff_variant == 0) {
+        CGB_TRY(adjoint_ffs(op, yin, in_mode, x, yobs, sqw, ax_a, ax_b, ca, cb, xout, partials, st, grid_out));
     } else {
         CGB_TRY(adjoint_ff(op, yin, in_mode, x, yobs, sqw, ax_a, ax_b, ca, cb, xout, partials, st, grid_out));
     }

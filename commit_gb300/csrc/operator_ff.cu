@@ -1,17 +1,73 @@
-// Instantiation of the voxel kernels for the float-float arithmetic policy.
-#include "operator_kernels.cuh"
+// Float-float operator launches: the packed-pair kernels of operator_pair.cuh.
 #include "operator_launch.cuh"
+#include "operator_pair.cuh"
 
 namespace cgb {
+namespace {
+
+using namespace detail;
+
+struct FwdPair {
+    cgb_op *op;
+    const double *x;
+    double *y, *ax;
+    const double *yobs, *sqw;
+    double *partials;
+    cudaStream_t st;
+    int *grid_out;
+    template <int L, int N>
+    int run() {
+        const OpDev P = op->dev();
+        const PadLut T{op->lutIC_p, op->lutEC_p, op->lutISO_p, op->nSp};
+        auto kern = k_forward_p<L, N>;
+        int g = 0;
+        CGB_TRY(grid_for_kernel(kern, 0, op->nsm, op->nV, kBlock / L, &g));
+        if (g > reduction_blocks(op)) g = reduction_blocks(op);
+        const int vec_ok = ((uintptr_t)y % 16 == 0) && ((uintptr_t)ax % 16 == 0);
+        kern<<<g, kBlock, 0, st>>>(P, T, x, y, ax, yobs, sqw, partials, vec_ok);
+        CGB_CUDA(cudaGetLastError());
+        if (grid_out) *grid_out = g;
+        return CGB_OK;
+    }
+};
+
+struct AdjPair {
+    cgb_op *op;
+    const double *yin;
+    int in_mode;
+    const double *x, *yobs, *sqw, *ax_a, *ax_b;
+    double ca, cb;
+    double *xout, *partials;
+    cudaStream_t st;
+    int *grid_out;
+    template <int L, int N>
+    int run() {
+        const OpDev P = op->dev();
+        const PadLut T{op->lutIC_p, op->lutEC_p, op->lutISO_p, op->nSp};
+        auto kern = k_adjoint_p<L, N>;
+        int g = 0;
+        CGB_TRY(grid_for_kernel(kern, 0, op->nsm, op->nV, kBlock / L, &g));
+        if (g > reduction_blocks(op)) g = reduction_blocks(op);
+        kern<<<g, kBlock, 0, st>>>(P, T, yin, in_mode, x, yobs, sqw, ax_a, ax_b, ca, cb, op->scratch, xout, partials);
+        CGB_CUDA(cudaGetLastError());
+        if (grid_out) *grid_out = g;
+        return CGB_OK;
+    }
+};
+
+}  // namespace
+
 int forward_ff(cgb_op *op, const double *x, double *y, double *ax, const double *yobs, const double *sqw,
-                double *partials, cudaStream_t st, int *grid) {
-    detail::FwdLaunch<detail::ArFF> L{op, x, y, ax, yobs, sqw, partials, st, grid};
-    return detail::dispatch_shape(detail::pick_shape(op->nS), L);
+               double *partials, cudaStream_t st, int *grid) {
+    FwdPair L{op, x, y, ax, yobs, sqw, partials, st, grid};
+    return dispatch_pair_shape(pick_pair_shape(op->nS), L);
 }
-int adjoint_ff(cgb_op *op, const double *yin, int in_mode, const double *x, const double *yobs,
-                const double *sqw, const double *ax_a, const double *ax_b, double ca, double cb, double *xout,
-                double *partials, cudaStream_t st, int *grid) {
-    detail::AdjLaunch<detail::ArFF> L{op, yin, in_mode, x, yobs, sqw, ax_a, ax_b, ca, cb, xout, partials, st, grid};
-    return detail::dispatch_shape(detail::pick_shape(op->nS), L);
+
+int adjoint_ff(cgb_op *op, const double *yin, int in_mode, const double *x, const double *yobs, const double *sqw,
+               const double *ax_a, const double *ax_b, double ca, double cb, double *xout, double *partials,
+               cudaStream_t st, int *grid) {
+    AdjPair L{op, yin, in_mode, x, yobs, sqw, ax_a, ax_b, ca, cb, xout, partials, st, grid};
+    return dispatch_pair_shape(pick_pair_shape(op->nS), L);
 }
+
 }  // namespace cgb

@@ -1,0 +1,477 @@
+// Float-float A*x and A'*y kernels on packed FP32 pairs (Blackwell f32x2 instructions).
+//
+// Same voxel ownership as operator_kernels.cuh, but each lane owns PAIRS of samples
+// (2p, 2p+1) for p = sub + k*LPV, k < NP, and every float-float operation is issued as one
+// f32x2 instruction acting on both samples.  The LUT rows used here are a zero-padded copy
+// with row stride nSp = 2*LPV*NP >= nS, so loads are aligned 8-byte loads with no bounds
+// guards and padded samples contribute zeros.  Per term the arithmetic is the exact
+// two-product (FMA) and two-sum of the scalar float-float policy -- 11 FP32 operations --
+// but issued as 5.5 instructions, which is what the FP32 pipes need to approach their
+// throughput instead of being limited by instruction issue.
+#pragma once
+#include "operator_kernels.cuh"
+
+namespace cgb {
+namespace detail {
+
+typedef unsigned long long f2;  // two packed FP32 words: low = even sample, high = odd
+
+__device__ __forceinline__ f2 f2_pack(float a, float b) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(f2 v, float &a, float &b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f2 f2_add(f2 a, f2 b) {
+    f2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 f2_sub(f2 a, f2 b) {
+    f2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 f2_mul(f2 a, f2 b) {
+    f2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c) {
+    f2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ f2 f2_ldg(const float *p) {
+    return __ldg(reinterpret_cast<const unsigned long long *>(p));
+}
+
+// float-float accumulator of two samples
+struct DD2 {
+    f2 s, e;
+};
+
+// coefficient c = h + l split in FP32, broadcast to both halves, with -h precomputed
+struct Coef2 {
+    f2 nh, h, l;
+};
+
+__device__ __forceinline__ Coef2 coef2(float h, float l) {
+    Coef2 c;
+    c.h = f2_pack(h, h);
+    c.l = f2_pack(l, l);
+    c.nh = f2_pack(-h, -h);
+    return c;
+}
+
+// a += (c.h + c.l) * L on both halves: exact two-product of the high word (the product
+// is formed negated so the FMA yields its rounding error directly) and a two-sum.
+__device__ __forceinline__ void dd2_fma(DD2 &a, const Coef2 &c, f2 L) {
+    const f2 pn = f2_mul(c.nh, L);
+    f2 e = f2_fma(c.h, L, pn);
+    e = f2_fma(c.l, L, e);
+    const f2 s = f2_sub(a.s, pn);
+    const f2 bb = f2_sub(s, a.s);
+    const f2 t2 = f2_sub(a.s, f2_sub(s, bb));
+    const f2 t3 = f2_add(pn, bb);
+    const f2 err = f2_sub(t2, t3);
+    a.e = f2_add(a.e, f2_add(err, e));
+    a.s = s;
+}
+
+__device__ __forceinline__ void dd2_add(DD2 &a, const DD2 &b) {
+    const f2 s = f2_add(a.s, b.s);
+    const f2 bb = f2_sub(s, a.s);
+    const f2 t2 = f2_sub(a.s, f2_sub(s, bb));
+    const f2 t3 = f2_sub(b.s, bb);
+    a.e = f2_add(f2_add(a.e, b.e), f2_add(t2, t3));
+    a.s = s;
+}
+
+__device__ __forceinline__ void dd2_zero(DD2 &a) {
+    a.s = 0ull;
+    a.e = 0ull;
+}
+
+// the two halves as doubles
+__device__ __forceinline__ void dd2_val(const DD2 &a, double &v0, double &v1) {
+    float s0, s1, e0, e1;
+    f2_unpack(a.s, s0, s1);
+    f2_unpack(a.e, e0, e1);
+    v0 = (double)s0 + (double)e0;
+    v1 = (double)s1 + (double)e1;
+}
+
+// sum of the two halves (scalar float-float) as a double
+__device__ __forceinline__ double dd2_hsum(const DD2 &a) {
+    float s0, s1, e0, e1;
+    f2_unpack(a.s, s0, s1);
+    f2_unpack(a.e, e0, e1);
+    ArFF::Acc x{s0, e0}, y{s1, e1};
+    ArFF::add(x, y);
+    return ArFF::val(x);
+}
+
+__device__ __forceinline__ DD2 dd2_shfl_xor(unsigned m, const DD2 &a, int lm, int w) {
+    DD2 r;
+    r.s = __shfl_xor_sync(m, a.s, lm, w);
+    r.e = __shfl_xor_sync(m, a.e, lm, w);
+    return r;
+}
+
+__device__ __forceinline__ void split2(double a, double b, f2 &h, f2 &l, f2 &nh) {
+    const float ha = __double2float_rn(a), hb = __double2float_rn(b);
+    const float la = __double2float_rn(a - (double)ha), lb = __double2float_rn(b - (double)hb);
+    h = f2_pack(ha, hb);
+    l = f2_pack(la, lb);
+    nh = f2_pack(-ha, -hb);
+}
+
+// Padded-row view of the LUTs
+struct PadLut {
+    const float *ic, *ec, *iso;
+    int nSp;
+};
+
+template <int LPV, int NP>
+__device__ __forceinline__ void forward_row_p(const OpDev &P, const PadLut &T, const Group<LPV> &G, int v,
+                                              const double *__restrict__ x, DD2 (&acc)[NP]) {
+#pragma unroll
+    for (int k = 0; k < NP; ++k) dd2_zero(acc[k]);
+    const int base = 2 * G.sub;
+    if (P.nIC > 0) {
+        const uint32_t beg = P.vox_ptr[v], end = P.vox_ptr[v + 1];
+        for (uint32_t b = beg; b < end; b += LPV) {
+            const uint32_t j = b + G.sub;
+            const bool valid = j < end;
+            uint32_t f = 0, o = 0;
+            float l = 0.f;
+            if (valid) {
+                f = P.seg_f[j];
+                o = P.seg_o[j];
+                l = P.seg_l[j];
+            }
+            const int cnt = min((int)(end - b), LPV);
+            for (int i = 0; i < P.nIC; ++i) {
+                float ch = 0.f, cl = 0.f;
+                if (valid) {
+                    const size_t col = (size_t)i * P.nF + f;
+                    const double c = (double)l * (x[col] * (double)P.eval[col]);
+                    ch = __double2float_rn(c);
+                    cl = __double2float_rn(c - (double)ch);
+                }
+                const uint32_t row = ((uint32_t)i * P.ndirs + o) * (uint32_t)T.nSp;
+                for (int t = 0; t < cnt; ++t) {
+                    const float th = __shfl_sync(G.mask, ch, t, LPV);
+                    const float tl = __shfl_sync(G.mask, cl, t, LPV);
+                    const uint32_t rt = __shfl_sync(G.mask, row, t, LPV);
+                    if (th != 0.f || tl != 0.f) {
+                        const Coef2 cf = coef2(th, tl);
+                        const float *L = T.ic + rt + base;
+#pragma unroll
+                        for (int k = 0; k < NP; ++k) dd2_fma(acc[k], cf, f2_ldg(L + 2 * LPV * k));
+                    }
+                }
+            }
+        }
+    }
+    if (P.nEC > 0) {
+        const uint32_t beg = P.ec_ptr[v], end = P.ec_ptr[v + 1];
+        for (uint32_t b = beg; b < end; b += LPV) {
+            const uint32_t j = b + G.sub;
+            const bool valid = j < end;
+            uint32_t col = 0, o = 0;
+            if (valid) {
+                col = P.ec_col[j];
+                o = P.ec_o[j];
+            }
+            const int cnt = min((int)(end - b), LPV);
+            for (int i = 0; i < P.nEC; ++i) {
+                float ch = 0.f, cl = 0.f;
+                if (valid) {
+                    const double c = x[P.ec_base + (size_t)i * P.nE + col];
+                    ch = __double2float_rn(c);
+                    cl = __double2float_rn(c - (double)ch);
+                }
+                const uint32_t row = ((uint32_t)i * P.ndirs + o) * (uint32_t)T.nSp;
+                for (int t = 0; t < cnt; ++t) {
+                    const float th = __shfl_sync(G.mask, ch, t, LPV);
+                    const float tl = __shfl_sync(G.mask, cl, t, LPV);
+                    const uint32_t rt = __shfl_sync(G.mask, row, t, LPV);
+                    if (th != 0.f || tl != 0.f) {
+                        const Coef2 cf = coef2(th, tl);
+                        const float *L = T.ec + rt + base;
+#pragma unroll
+                        for (int k = 0; k < NP; ++k) dd2_fma(acc[k], cf, f2_ldg(L + 2 * LPV * k));
+                    }
+                }
+            }
+        }
+    }
+    if (P.nISO > 0) {
+        const uint32_t beg = P.iso_ptr[v], end = P.iso_ptr[v + 1];
+        for (uint32_t b = beg; b < end; b += LPV) {
+            const uint32_t j = b + G.sub;
+            const bool valid = j < end;
+            const uint32_t col = valid ? P.iso_col[j] : 0;
+            const int cnt = min((int)(end - b), LPV);
+            for (int i = 0; i < P.nISO; ++i) {
+                float ch = 0.f, cl = 0.f;
+                if (valid) {
+                    const double c = x[P.iso_base + (size_t)i * P.nISOv + col];
+                    ch = __double2float_rn(c);
+                    cl = __double2float_rn(c - (double)ch);
+                }
+                for (int t = 0; t < cnt; ++t) {
+                    const float th = __shfl_sync(G.mask, ch, t, LPV);
+                    const float tl = __shfl_sync(G.mask, cl, t, LPV);
+                    if (th != 0.f || tl != 0.f) {
+                        const Coef2 cf = coef2(th, tl);
+                        const float *L = T.iso + (size_t)i * T.nSp + base;
+#pragma unroll
+                        for (int k = 0; k < NP; ++k) dd2_fma(acc[k], cf, f2_ldg(L + 2 * LPV * k));
+                    }
+                }
+            }
+        }
+    }
+}
+
+template <int LPV, int NP>
+__global__ void __launch_bounds__(kBlock) k_forward_p(const OpDev P, const PadLut T, const double *__restrict__ x,
+                                                      double *__restrict__ yout, double *__restrict__ axout,
+                                                      const double *__restrict__ yobs, const double *__restrict__ sqw,
+                                                      double *__restrict__ partials, int vec_ok) {
+    const Group<LPV> G;
+    const int gpb = kBlock / LPV;
+    const int ngroups = gridDim.x * gpb;
+    const int nS = P.nS;
+    // 16-byte row stores need an even row length and 16-byte aligned outputs
+    const bool even = (nS & 1) == 0 && vec_ok;
+    double nrm = 0.0;
+    for (int v = blockIdx.x * gpb + (int)threadIdx.x / LPV; v < P.nV; v += ngroups) {
+        DD2 acc[NP];
+        forward_row_p<LPV, NP>(P, T, G, v, x, acc);
+#pragma unroll
+        for (int k = 0; k < NP; ++k) {
+            const int s = 2 * (G.sub + k * LPV);
+            if (s < nS) {
+                double a0, a1;
+                dd2_val(acc[k], a0, a1);
+                const size_t idx = (size_t)v * nS + s;
+                const bool two = s + 1 < nS;
+                if (yout) {
+                    if (two && even) *reinterpret_cast<double2 *>(yout + idx) = make_double2(a0, a1);
+                    else { yout[idx] = a0; if (two) yout[idx + 1] = a1; }
+                }
+                if (axout) {
+                    if (two && even) *reinterpret_cast<double2 *>(axout + idx) = make_double2(a0, a1);
+                    else { axout[idx] = a0; if (two) axout[idx + 1] = a1; }
+                }
+                if (partials) {
+                    double r0 = yobs ? a0 - yobs[idx] : a0;
+                    if (sqw) r0 *= sqw[idx];
+                    nrm = fma(r0, r0, nrm);
+                    if (two) {
+                        double r1 = yobs ? a1 - yobs[idx + 1] : a1;
+                        if (sqw) r1 *= sqw[idx + 1];
+                        nrm = fma(r1, r1, nrm);
+                    }
+                }
+            }
+        }
+    }
+    if (partials) block_sum_store(nrm, partials + (size_t)blockIdx.x * kRedSlots);
+}
+
+// <LUT row of item q, z> for the B items of a sub-batch (PairBatch); the total of item
+// q = sub / (LPV/B) ends in lane sub (butterfly reduce-scatter on packed accumulators,
+// halves combined at the end).
+// items per reduce-scatter batch: 8, or 4 when the pair registers are many
+template <int LPV, int NP>
+struct PairBatch {
+    static constexpr int B = LPV < (NP >= 5 ? 4 : 8) ? LPV : (NP >= 5 ? 4 : 8);
+};
+
+template <int LPV, int NP, class RowFn>
+__device__ __forceinline__ double batch_dots_p(const Group<LPV> &G, const float *__restrict__ lut, RowFn row,
+                                               int cnt, const f2 (&zh)[NP], const f2 (&zl)[NP],
+                                               const f2 (&znh)[NP]) {
+    constexpr int B = PairBatch<LPV, NP>::B;
+    DD2 Pq[B];
+    const int base = 2 * G.sub;
+#pragma unroll
+    for (int q = 0; q < B; ++q) {
+        dd2_zero(Pq[q]);
+        if (q < cnt) {
+            const float *L = lut + row(q) + base;
+#pragma unroll
+            for (int k = 0; k < NP; ++k) {
+                Coef2 zc;
+                zc.h = zh[k];
+                zc.l = zl[k];
+                zc.nh = znh[k];
+                dd2_fma(Pq[q], zc, f2_ldg(L + 2 * LPV * k));
+            }
+        }
+    }
+#pragma unroll
+    for (int h = B / 2, m = LPV / 2; h >= 1; h /= 2, m /= 2) {
+        const bool hi = (G.sub & m) != 0;
+#pragma unroll
+        for (int j = 0; j < h; ++j) {
+            DD2 send, keep;
+            send.s = hi ? Pq[j].s : Pq[j + h].s;
+            send.e = hi ? Pq[j].e : Pq[j + h].e;
+            keep.s = hi ? Pq[j + h].s : Pq[j].s;
+            keep.e = hi ? Pq[j + h].e : Pq[j].e;
+            dd2_add(keep, dd2_shfl_xor(G.mask, send, m, LPV));
+            Pq[j] = keep;
+        }
+    }
+#pragma unroll
+    for (int m = LPV / B / 2; m >= 1; m /= 2) dd2_add(Pq[0], dd2_shfl_xor(G.mask, Pq[0], m, LPV));
+    return dd2_hsum(Pq[0]);
+}
+
+template <int LPV, int NP>
+__global__ void __launch_bounds__(kBlock) k_adjoint_p(const OpDev P, const PadLut T, const double *__restrict__ yin,
+                                                      int in_mode, const double *__restrict__ x,
+                                                      const double *__restrict__ yobs, const double *__restrict__ sqw,
+                                                      const double *__restrict__ ax_a, const double *__restrict__ ax_b,
+                                                      double ca, double cb, double *__restrict__ scratch,
+                                                      double *__restrict__ xout, double *__restrict__ partials) {
+    constexpr int B = PairBatch<LPV, NP>::B;
+    constexpr int SPAN = LPV / B;
+    const Group<LPV> G;
+    const int gpb = kBlock / LPV;
+    const int ngroups = gridDim.x * gpb;
+    const int nS = P.nS;
+    const int q_me = G.sub / SPAN;
+    const bool writer = (G.sub % SPAN) == 0;
+    double nrm = 0.0;
+    for (int v = blockIdx.x * gpb + (int)threadIdx.x / LPV; v < P.nV; v += ngroups) {
+        double a[2 * NP];
+        if (in_mode == 1) {
+            DD2 acc[NP];
+            forward_row_p<LPV, NP>(P, T, G, v, x, acc);
+#pragma unroll
+            for (int k = 0; k < NP; ++k) dd2_val(acc[k], a[2 * k], a[2 * k + 1]);
+        }
+        f2 zh[NP], zl[NP], znh[NP];
+#pragma unroll
+        for (int k = 0; k < NP; ++k) {
+            double zz[2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int s = 2 * (G.sub + k * LPV) + u;
+                zz[u] = 0.0;
+                if (s < nS) {
+                    const size_t idx = (size_t)v * nS + s;
+                    if (in_mode == 0) {
+                        zz[u] = yin[idx];
+                    } else {
+                        const double av = in_mode == 1 ? a[2 * k + u] : ca * ax_a[idx] + cb * ax_b[idx];
+                        double r = av - yobs[idx];
+                        if (sqw) r *= sqw[idx];
+                        nrm = fma(r, r, nrm);
+                        zz[u] = sqw ? sqw[idx] * r : r;
+                    }
+                }
+            }
+            split2(zz[0], zz[1], zh[k], zl[k], znh[k]);
+        }
+        if (P.nIC > 0) {
+            const uint32_t beg = P.vox_ptr[v], end = P.vox_ptr[v + 1];
+            for (uint32_t b = beg; b < end; b += LPV) {
+                const uint32_t j = b + G.sub;
+                const bool valid = j < end;
+                const uint32_t o = valid ? P.seg_o[j] : 0;
+                const float l = valid ? P.seg_l[j] : 0.f;
+                const int cntL = min((int)(end - b), LPV);
+                for (int i = 0; i < P.nIC; ++i) {
+                    const uint32_t row = ((uint32_t)i * P.ndirs + o) * (uint32_t)T.nSp;
+                    for (int t0 = 0; t0 < cntL; t0 += B) {
+                        const int cnt = min(B, cntL - t0);
+                        auto rowf = [&](int q) { return __shfl_sync(G.mask, row, t0 + q, LPV); };
+                        const double tot = batch_dots_p<LPV, NP>(G, T.ic, rowf, cnt, zh, zl, znh);
+                        const float lq = __shfl_sync(G.mask, l, t0 + q_me, LPV);
+                        if (writer && q_me < cnt) scratch[(size_t)i * P.n + b + t0 + q_me] = (double)lq * tot;
+                    }
+                }
+            }
+        }
+        if (P.nEC > 0) {
+            const uint32_t beg = P.ec_ptr[v], end = P.ec_ptr[v + 1];
+            for (uint32_t b = beg; b < end; b += LPV) {
+                const uint32_t j = b + G.sub;
+                const bool valid = j < end;
+                const uint32_t o = valid ? P.ec_o[j] : 0;
+                const uint32_t col = valid ? P.ec_col[j] : 0;
+                const int cntL = min((int)(end - b), LPV);
+                for (int i = 0; i < P.nEC; ++i) {
+                    const uint32_t row = ((uint32_t)i * P.ndirs + o) * (uint32_t)T.nSp;
+                    for (int t0 = 0; t0 < cntL; t0 += B) {
+                        const int cnt = min(B, cntL - t0);
+                        auto rowf = [&](int q) { return __shfl_sync(G.mask, row, t0 + q, LPV); };
+                        const double tot = batch_dots_p<LPV, NP>(G, T.ec, rowf, cnt, zh, zl, znh);
+                        const uint32_t cq = __shfl_sync(G.mask, col, t0 + q_me, LPV);
+                        if (writer && q_me < cnt) xout[P.ec_base + (size_t)i * P.nE + cq] = tot;
+                    }
+                }
+            }
+        }
+        if (P.nISO > 0) {
+            const uint32_t beg = P.iso_ptr[v], end = P.iso_ptr[v + 1];
+            if (beg < end) {
+                for (int t0 = 0; t0 < P.nISO; t0 += B) {
+                    const int cnt = min(B, P.nISO - t0);
+                    auto rowf = [&](int q) { return (uint32_t)((t0 + q) * T.nSp); };
+                    const double tot = batch_dots_p<LPV, NP>(G, T.iso, rowf, cnt, zh, zl, znh);
+                    if (writer && q_me < cnt)
+                        for (uint32_t e = beg; e < end; ++e)
+                            xout[P.iso_base + (size_t)(t0 + q_me) * P.nISOv + P.iso_col[e]] = tot;
+                }
+            }
+        }
+    }
+    if (partials) block_sum_store(nrm, partials + (size_t)blockIdx.x * kRedSlots);
+}
+
+// (LPV, NP) pairs with kernels; 2*LPV*NP samples per voxel row
+struct PairShape {
+    int lpv, np;
+};
+constexpr PairShape kPairShapes[] = {{1, 1},  {2, 1},  {4, 1},  {4, 2},  {8, 1},  {8, 2},  {8, 3},  {8, 5},
+                                     {16, 1}, {16, 2}, {16, 3}, {16, 5}, {16, 9}, {32, 1}, {32, 2}, {32, 3},
+                                     {32, 5}, {32, 8}};
+
+inline PairShape pick_pair_shape(int nS) {
+    PairShape best = {32, 8};
+    int best_slots = 1 << 30;
+    for (const PairShape &s : kPairShapes) {
+        const int slots = 2 * s.lpv * s.np;
+        if (slots < nS) continue;
+        if (slots < best_slots || (slots == best_slots && s.lpv > best.lpv)) {
+            best = s;
+            best_slots = slots;
+        }
+    }
+    return best;
+}
+
+template <class Fn>
+int dispatch_pair_shape(PairShape s, Fn &fn) {
+#define CGB_PSHAPE(L, N) \
+    if (s.lpv == L && s.np == N) return fn.template run<L, N>();
+    CGB_PSHAPE(1, 1) CGB_PSHAPE(2, 1) CGB_PSHAPE(4, 1) CGB_PSHAPE(4, 2) CGB_PSHAPE(8, 1) CGB_PSHAPE(8, 2)
+    CGB_PSHAPE(8, 3) CGB_PSHAPE(8, 5) CGB_PSHAPE(16, 1) CGB_PSHAPE(16, 2) CGB_PSHAPE(16, 3) CGB_PSHAPE(16, 5)
+    CGB_PSHAPE(16, 9) CGB_PSHAPE(32, 1) CGB_PSHAPE(32, 2) CGB_PSHAPE(32, 3) CGB_PSHAPE(32, 5) CGB_PSHAPE(32, 8)
+#undef CGB_PSHAPE
+    return fail(CGB_ERR_UNSUPPORTED, "no paired kernel shape for this number of samples");
+}
+
+}  // namespace detail
+}  // namespace cgb

@@ -130,12 +130,29 @@ class LinearOperator:
         """A @ v_in (or A' @ v_in for the adjoint).
 
         numpy float64 in -> numpy float64 out (host copies inside the call);
-        torch CUDA float64 in -> torch CUDA float64 out (no host round-trip).
+        torch CUDA float64 in -> torch CUDA float64 out (no host round-trip);
+        torch CUDA float32 in -> float32 out through the reduced-precision kernels
+        (``arith`` 'bf16' (default), 'fp16' or 'f32': LUT in that format, FP16 lengths,
+        FP32 accumulation).
         """
+        if isinstance(v_in, torch.Tensor) and v_in.is_cuda and v_in.dtype == torch.float32:
+            ar32 = _lib.ARITH[arith or 'bf16']
+            if ar32 < _lib.ARITH['bf16']:
+                raise ValueError("float32 vectors need arith 'bf16', 'fp16' or 'f32'")
+            v_in = v_in.contiguous()
+            if v_in.numel() != self.shape[1]:
+                raise RuntimeError("A.dot(): dimensions do not match")
+            if out is None:
+                out = torch.empty(self.shape[0], dtype=torch.float32, device=v_in.device)
+            st = torch.cuda.current_stream(v_in.device).cuda_stream
+            check(lib().cgb_op_apply(self._h.ptr, self.adjoint, ctypes.c_void_p(v_in.data_ptr()), v_in.numel(),
+                                     ctypes.c_void_p(out.data_ptr()), out.numel(), _lib.DTYPE_F32, ar32,
+                                     ctypes.c_void_p(st)))
+            return out
         ar = _lib.ARITH[arith or self.arith]
         if isinstance(v_in, torch.Tensor) and v_in.is_cuda:
             if v_in.dtype != torch.float64:
-                raise TypeError('LinearOperator.dot expects float64 tensors')
+                raise TypeError('LinearOperator.dot expects float64 or float32 CUDA tensors')
             v_in = v_in.contiguous()
             if v_in.numel() != self.shape[1]:
                 raise RuntimeError("A.dot(): dimensions do not match")

@@ -279,3 +279,28 @@ def _fista(y, A, spec: RegSpec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, a
     details['operator_calls'] = int(res.operator_calls)
     x = xd.cpu().numpy() if host else xd
     return x, details
+
+
+def solve_mixed(y, A, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, verbose=0, x0=None, regularisation=None,
+                confidence_array=None, arith='bf16', refine_arith=None, refine_max_iter=None,
+                refine_tol_fun=None, refine_tol_x=None):
+    """Reduced-precision FISTA followed by an FP64 refinement solve.
+
+    Phase 1 runs FISTA with the operator in ``arith`` ('bf16', 'fp16' or 'f32': LUT in
+    that format, FP16 lengths, FP32 accumulation; FISTA vectors, the Lipschitz estimate
+    and every objective / stopping reduction in FP64).  Phase 2 restarts the plain FP64
+    solver (float-float by default) from the phase-1 solution, which removes the bias of
+    the reduced-precision operator.  Returns (x, details) with details['mixed'] and
+    details['refine'] holding each phase's opt_details.
+    """
+    x1, d1 = solve(y, A, A.T, tol_fun=tol_fun, tol_x=tol_x, max_iter=max_iter, verbose=verbose, x0=x0,
+                   regularisation=regularisation, confidence_array=confidence_array, arith=arith)
+    x2, d2 = solve(y, A, A.T, tol_fun=refine_tol_fun if refine_tol_fun is not None else tol_fun,
+                   tol_x=refine_tol_x if refine_tol_x is not None else tol_x,
+                   max_iter=refine_max_iter if refine_max_iter is not None else max_iter, verbose=verbose, x0=x1,
+                   regularisation=regularisation, confidence_array=confidence_array, arith=refine_arith)
+    det = dict(d2)
+    det['mixed'] = d1
+    det['refine'] = d2
+    det['iterations'] = d1['iterations'] + d2['iterations']
+    return x2, det

@@ -150,9 +150,9 @@ SPECS = {
     # the demo case scaled to 50k streamlines (gradient checks)
     'demo_50k': ProblemSpec(n_fibers=50000),
     # 145x174x145 grid, 600k-voxel mask, 1M streamlines of lognormal length giving ~120
-    # segments per streamline (arc length mean 99 voxels), 18 b0 + 3 shells x 90 dirs (nS=288)
+    # segments per streamline (arc length mean 86 voxels), 18 b0 + 3 shells x 90 dirs (nS=288)
     'hcp_1m': ProblemSpec(dim=(145, 174, 145), n_mask=600000, n_fibers=1000000, ctrl='walk',
-                          mean_len=99.0, n_b0=18, shells=[(1000.0, 90), (2000.0, 90), (3000.0, 90)]),
+                          mean_len=86.0, n_b0=18, shells=[(1000.0, 90), (2000.0, 90), (3000.0, 90)]),
 }
 
 
@@ -195,14 +195,17 @@ def _control_points(spec: ProblemSpec, rng: np.random.Generator, mask: np.ndarra
         nd /= np.linalg.norm(nd, axis=1, keepdims=True)
         d = nd
         nxt = cur + d * seglen[:, None]
-        # keep the walk inside the mask ellipsoid: steps that would leave it turn back
-        # towards the centre, and points are pulled onto the 0.95 iso-surface if needed
+        # keep the walk inside the mask ellipsoid: a step that would leave it is reflected
+        # off the surface (specular reflection about the ellipsoid normal), and points are
+        # pulled back onto the 0.9 level set if still outside
         out = _ell_r2(nxt, spec.dim, ell) > 0.9
         if out.any():
-            back = centre - cur[out]
-            back /= np.linalg.norm(back, axis=1, keepdims=True) + 1e-12
-            d[out] = back
-            nxt[out] = cur[out] + back * seglen[out, None]
+            nrm = (cur[out] - centre) / (centre ** 2)
+            nrm /= np.linalg.norm(nrm, axis=1, keepdims=True) + 1e-12
+            dd = d[out]
+            dd = dd - 2.0 * np.sum(dd * nrm, axis=1, keepdims=True) * nrm
+            d[out] = dd
+            nxt[out] = cur[out] + dd * seglen[out, None]
         r2 = _ell_r2(nxt, spec.dim, ell)
         shrink = np.where(r2 > 0.9, np.sqrt(0.9 / np.maximum(r2, 1e-12)), 1.0)
         nxt = centre + (nxt - centre) * shrink[:, None]

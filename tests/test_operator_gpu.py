@@ -115,3 +115,46 @@ def test_repeatable_bitwise():
     a1 = A.T.dot(c['y_in'])
     a2 = A.T.dot(c['y_in'])
     assert np.array_equal(a1, a2)
+
+
+@pytest.mark.parametrize('n_b0,shells', [(1, [(1000.0, 6)]), (3, [(1000.0, 30)]), (1, [(1000.0, 45), (2000.0, 45)]),
+                                         (18, [(1000.0, 90), (2000.0, 90), (3000.0, 90)])])
+def test_sample_counts_against_oracle(n_b0, shells):
+    """nS = 7, 33, 91 (odd: scalar row stores) and 288 (the full-brain acquisition)."""
+    from commit_gb300 import synth
+    from commit_gb300.operator import LinearOperator
+    spec = synth.ProblemSpec(dim=(24, 24, 16), n_mask=5000, n_fibers=800, ndirs=200, n_b0=n_b0, shells=shells,
+                             seed=5)
+    D, K = synth.make_dictionary(spec)
+    P = O.PortOperator(D, K, None, nthreads=8)
+    rng = np.random.default_rng(3)
+    x = rng.uniform(-0.3, 1.0, size=P.nCOLS)
+    y = rng.normal(size=P.nROWS)
+    ax, aty = P.dot(x), P.T.dot(y)
+    for arith in ('ff', 'f64'):
+        A = LinearOperator(D, K, None, arith=arith)
+        assert G.rel(A.dot(x), ax) <= TOL, arith
+        assert G.rel(A.T.dot(y), aty) <= TOL, arith
+
+
+@pytest.mark.parametrize('arith,tol', [('bf16', 1.5e-2), ('fp16', 4e-3), ('f32', 2e-5)])
+def test_reduced_precision_operator(arith, tol):
+    """LUT in BF16/FP16 (or FP32), FP16 lengths, FP32 accumulation vs the FP64 oracle."""
+    from commit_gb300 import synth
+    from commit_gb300.operator import LinearOperator
+    D, K = synth.make_dictionary(synth.SPECS['demo_5k'])
+    P = O.PortOperator(D, K, None, nthreads=8)
+    rng = np.random.default_rng(4)
+    x = rng.uniform(0.0, 1.0, size=P.nCOLS)
+    y = rng.uniform(0.0, 1.0, size=P.nROWS)
+    A = LinearOperator(D, K, None)
+    ax = A.dot(torch.from_numpy(x).float().cuda(), arith=arith).double().cpu().numpy()
+    aty = A.T.dot(torch.from_numpy(y).float().cuda(), arith=arith).double().cpu().numpy()
+    assert G.rel(ax, P.dot(x)) <= tol
+    assert G.rel(aty, P.T.dot(y)) <= tol
+    # the reduced operator is itself an exact adjoint pair up to FP32 rounding
+    xs = rng.normal(size=P.nCOLS)
+    ys = rng.normal(size=P.nROWS)
+    lhs = float(np.dot(A.dot(torch.from_numpy(xs).float().cuda(), arith=arith).double().cpu().numpy(), ys))
+    rhs = float(np.dot(xs, A.T.dot(torch.from_numpy(ys).float().cuda(), arith=arith).double().cpu().numpy()))
+    assert abs(lhs - rhs) <= 1e-4 * (abs(lhs) + abs(rhs))

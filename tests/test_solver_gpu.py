@@ -71,3 +71,22 @@ def test_fista_demo_scale_against_oracle():
     assert dg['iterations'] == do['iterations'] == 200
     assert G.rel(xg, xo) <= 1e-8
     assert abs(dg['cost_function'] - do['cost_function']) <= 1e-8 * do['cost_function']
+
+
+@pytest.mark.parametrize('arith', ['bf16', 'fp16'])
+def test_mixed_fista_with_refinement_reaches_fp64_solution(arith):
+    """Reduced-precision FISTA + FP64 refinement reaches the FP64 solution within 1e-4."""
+    import oracle as O
+    from commit_gb300 import solvers, synth
+    from commit_gb300.operator import LinearOperator
+    D, K = synth.make_dictionary(synth.SPECS['demo_5k'])
+    A = LinearOperator(D, K, None)
+    P = O.PortOperator(D, K, None, nthreads=8)
+    y = synth.make_signal(P.dot(synth.make_x(P.nCOLS, 1)), 2)
+    rp = O.reg_params(D, K)
+    x_ref, _ = solvers.solve(y, A, A.T, tol_fun=1e-12, tol_x=1e-12, max_iter=3000, verbose=0,
+                             regularisation=solvers.init_regularisation(dict(rp)))
+    xm, dm = solvers.solve_mixed(y, A, tol_fun=1e-9, tol_x=1e-9, max_iter=1500, verbose=0,
+                                 regularisation=solvers.init_regularisation(dict(rp)), arith=arith,
+                                 refine_tol_fun=1e-12, refine_tol_x=1e-12, refine_max_iter=3000)
+    assert G.rel(xm, x_ref) <= 1e-4
