@@ -71,6 +71,8 @@ def lib() -> ctypes.CDLL:
     L.cgb_op_shape.argtypes = [P, ctypes.POINTER(c_i64), ctypes.POINTER(c_i64)]
     L.cgb_op_device_bytes.argtypes = [P, ctypes.POINTER(ctypes.c_size_t)]
     L.cgb_op_set_arith.argtypes = [P, c_i32]
+    L.cgb_op_set_lut.argtypes = [P, P, P, P]
+    L.cgb_op_lut_grad.argtypes = [P, P, P, P, P, P, P]
     L.cgb_op_apply.argtypes = [P, c_i32, P, c_i64, P, c_i64, c_i32, c_i32, P]
     L.cgb_op_apply_host.argtypes = [P, c_i32, P, c_i64, P, c_i64]
     L.cgb_op_adjoint_noalloc.argtypes = [c_i32, c_i32, c_i32, c_i64, c_i32, c_i32, c_i32, P, P,

@@ -76,6 +76,7 @@ struct cgb_op {
     __half *seg_l16;                // FP16 lengths scaled by 2^k (reduced path)
     float len16_inv_scale;          // 2^-k
     double *d_x64;                  // [ncols] staging for FP32 applies
+    void *gstate;                   // LUT-gradient streams (lutgrad.cu), built on first use
     uint32_t *vox_ptr, *seg_f, *eval, *fib_ptr, *fib_perm, *ec_ptr, *ec_col, *iso_ptr, *iso_col;
     uint16_t *seg_o, *ec_o;
     float *seg_l;
@@ -107,6 +108,7 @@ int launch_gradient_grid(cgb_op *op, const double *x, const double *y, const dou
                          double *partials, const double *ax_a, const double *ax_b, double ca, double cb,
                          cudaStream_t st, int arith, int *grid);
 int reduction_blocks(const cgb_op *op);
+void free_grad_state(cgb_op *op);
 // reduced-precision path (mixed.cu): FP32 rows, FP64 columns
 int ensure_reduced(cgb_op *op, int arith);
 int launch_resnorm_mix(cgb_op *op, const double *x, const float *y, const float *sqw, double *partials,

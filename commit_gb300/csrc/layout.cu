@@ -185,6 +185,7 @@ using namespace cgb;
 
 static void free_op(cgb_op *op) {
     if (!op) return;
+    free_grad_state(op);
     void *ptrs[] = {op->lutIC, op->lutEC, op->lutISO, op->lutIC_p, op->lutEC_p, op->lutISO_p, op->lutIC_r, op->lutEC_r, op->seg_l16, op->vox_ptr,
                     op->seg_f, op->eval, op->fib_ptr, op->fib_perm, op->ec_ptr, op->ec_col, op->iso_ptr,
                     op->iso_col, op->seg_o, op->ec_o, op->seg_l, op->scratch, op->scratch32, op->partials,
@@ -426,6 +427,28 @@ int cgb_op_shape(const cgb_op *op, int64_t *nrows, int64_t *ncols) {
 int cgb_op_device_bytes(const cgb_op *op, size_t *bytes) {
     if (!op || !bytes) return fail(CGB_ERR_INVALID, "null argument");
     *bytes = op->bytes;
+    return CGB_OK;
+}
+
+int cgb_op_set_lut(cgb_op *op, const float *lutIC, const float *lutEC, const float *lutISO) {
+    if (!op) return fail(CGB_ERR_INVALID, "null handle");
+    if (op->nolut) return fail(CGB_ERR_UNSUPPORTED, "the LUT-free operator has no LUT");
+    DeviceGuard g(op->device);
+    const size_t nS = op->nS, sp = op->nSp;
+    struct Part {
+        const float *src;
+        float *dst, *dstp;
+        size_t rows;
+    } parts[3] = {{lutIC, op->lutIC, op->lutIC_p, (size_t)op->nIC * op->ndirs},
+                  {lutEC, op->lutEC, op->lutEC_p, (size_t)op->nEC * op->ndirs},
+                  {lutISO, op->lutISO, op->lutISO_p, (size_t)op->nISO}};
+    for (const Part &p : parts) {
+        if (!p.src || p.rows == 0) continue;
+        CGB_CUDA(cudaMemcpy(p.dst, p.src, p.rows * nS * sizeof(float), cudaMemcpyDefault));
+        CGB_CUDA(cudaMemcpy2D(p.dstp, sp * sizeof(float), p.src, nS * sizeof(float), nS * sizeof(float), p.rows,
+                              cudaMemcpyDefault));
+    }
+    op->lut_r_kind = 0;  // reduced-precision copies are rebuilt on their next use
     return CGB_OK;
 }
 

@@ -18,13 +18,13 @@ struct FwdPair {
     template <int L, int N>
     int run() {
         const OpDev P = op->dev();
-        const PadLut T{op->lutIC_p, op->lutEC_p, op->lutISO_p, op->nSp};
+        const Comps C = make_comps(op);
         auto kern = k_forward_p<L, N>;
         int g = 0;
         CGB_TRY(grid_for_kernel(kern, 0, op->nsm, op->nV, kBlock / L, &g));
         if (g > reduction_blocks(op)) g = reduction_blocks(op);
         const int vec_ok = ((uintptr_t)y % 16 == 0) && ((uintptr_t)ax % 16 == 0);
-        kern<<<g, kBlock, 0, st>>>(P, T, x, y, ax, yobs, sqw, partials, vec_ok);
+        kern<<<g, kBlock, 0, st>>>(P, C, x, y, ax, yobs, sqw, partials, vec_ok);
         CGB_CUDA(cudaGetLastError());
         if (grid_out) *grid_out = g;
         return CGB_OK;
@@ -43,12 +43,12 @@ struct AdjPair {
     template <int L, int N>
     int run() {
         const OpDev P = op->dev();
-        const PadLut T{op->lutIC_p, op->lutEC_p, op->lutISO_p, op->nSp};
+        const Comps C = make_comps(op);
         auto kern = k_adjoint_p<L, N>;
         int g = 0;
         CGB_TRY(grid_for_kernel(kern, 0, op->nsm, op->nV, kBlock / L, &g));
         if (g > reduction_blocks(op)) g = reduction_blocks(op);
-        kern<<<g, kBlock, 0, st>>>(P, T, yin, in_mode, x, yobs, sqw, ax_a, ax_b, ca, cb, op->scratch, xout, partials);
+        kern<<<g, kBlock, 0, st>>>(P, C, yin, in_mode, x, yobs, sqw, ax_a, ax_b, ca, cb, op->scratch, xout, partials);
         CGB_CUDA(cudaGetLastError());
         if (grid_out) *grid_out = g;
         return CGB_OK;

@@ -135,101 +135,111 @@ struct PadLut {
     int nSp;
 };
 
+// One compartment's items as the voxel kernels see them.  Item j of voxel v is in
+// [ptr[v], ptr[v+1]); its column for response i is xbase + i*xstride + col[j], its LUT row
+// is lut + i*rf_stride + o[j]*nSp.  Null o / l / eval mean orientation 0, length 1, eval 1.
+struct Comp {
+    const uint32_t *ptr, *col;
+    const uint16_t *o;
+    const float *l;
+    const uint32_t *eval;
+    const float *lut;
+    int64_t xbase, xstride;
+    uint32_t rf_stride;
+    int nrf;
+    int to_scratch;  // A': per-segment terms l*<L,y> go to the scratch stream (IC)
+};
+
+struct Comps {
+    Comp c[3];
+    int n;
+    int nSp;
+};
+
+__device__ __forceinline__ void ff_add(float &h, float &l, float bh, float bl) {
+    const float s = __fadd_rn(h, bh);
+    const float bb = __fsub_rn(s, h);
+    const float err = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(bh, bb));
+    l = __fadd_rn(l, __fadd_rn(bl, err));
+    h = s;
+}
+
+template <int LPV>
+__device__ __forceinline__ unsigned group_bits(unsigned ballot) {
+    const unsigned shift = (threadIdx.x & 31) & ~(LPV - 1);
+    return LPV == 32 ? ballot : (ballot >> shift) & ((1u << LPV) - 1u);
+}
+
+// Items of a batch are sorted by orientation within the voxel, so equal rows are adjacent:
+// head = first item of a run of equal orientation, tail = last one.
+template <int LPV>
+__device__ __forceinline__ void run_flags(const Group<LPV> &G, bool valid, uint32_t o, int cntL, bool &head,
+                                          bool &tail) {
+    const uint32_t o_prev = __shfl_up_sync(G.mask, o, 1, LPV);
+    const uint32_t o_next = __shfl_down_sync(G.mask, o, 1, LPV);
+    head = valid && (G.sub == 0 || o_prev != o);
+    tail = valid && (G.sub == cntL - 1 || o_next != o);
+}
+
 template <int LPV, int NP>
-__device__ __forceinline__ void forward_row_p(const OpDev &P, const PadLut &T, const Group<LPV> &G, int v,
+__device__ __forceinline__ void forward_row_p(const Comps &C, const Group<LPV> &G, int v,
                                               const double *__restrict__ x, DD2 (&acc)[NP]) {
 #pragma unroll
     for (int k = 0; k < NP; ++k) dd2_zero(acc[k]);
     const int base = 2 * G.sub;
-    if (P.nIC > 0) {
-        const uint32_t beg = P.vox_ptr[v], end = P.vox_ptr[v + 1];
-        for (uint32_t b = beg; b < end; b += LPV) {
-            const uint32_t j = b + G.sub;
-            const bool valid = j < end;
-            uint32_t f = 0, o = 0;
-            float l = 0.f;
-            if (valid) {
-                f = P.seg_f[j];
-                o = P.seg_o[j];
-                l = P.seg_l[j];
-            }
-            const int cnt = min((int)(end - b), LPV);
-            for (int i = 0; i < P.nIC; ++i) {
-                float ch = 0.f, cl = 0.f;
-                if (valid) {
-                    const size_t col = (size_t)i * P.nF + f;
-                    const double c = (double)l * (x[col] * (double)P.eval[col]);
-                    ch = __double2float_rn(c);
-                    cl = __double2float_rn(c - (double)ch);
-                }
-                const uint32_t row = ((uint32_t)i * P.ndirs + o) * (uint32_t)T.nSp;
-                for (int t = 0; t < cnt; ++t) {
-                    const float th = __shfl_sync(G.mask, ch, t, LPV);
-                    const float tl = __shfl_sync(G.mask, cl, t, LPV);
-                    const uint32_t rt = __shfl_sync(G.mask, row, t, LPV);
-                    if (th != 0.f || tl != 0.f) {
-                        const Coef2 cf = coef2(th, tl);
-                        const float *L = T.ic + rt + base;
-#pragma unroll
-                        for (int k = 0; k < NP; ++k) dd2_fma(acc[k], cf, f2_ldg(L + 2 * LPV * k));
-                    }
-                }
-            }
-        }
-    }
-    if (P.nEC > 0) {
-        const uint32_t beg = P.ec_ptr[v], end = P.ec_ptr[v + 1];
+#pragma unroll 1
+    for (int ci = 0; ci < C.n; ++ci) {
+        const Comp &cm = C.c[ci];
+        const uint32_t beg = cm.ptr[v], end = cm.ptr[v + 1];
+#pragma unroll 1
         for (uint32_t b = beg; b < end; b += LPV) {
             const uint32_t j = b + G.sub;
             const bool valid = j < end;
             uint32_t col = 0, o = 0;
+            float l = 1.f;
             if (valid) {
-                col = P.ec_col[j];
-                o = P.ec_o[j];
+                col = cm.col[j];
+                if (cm.o) o = cm.o[j];
+                if (cm.l) l = cm.l[j];
             }
-            const int cnt = min((int)(end - b), LPV);
-            for (int i = 0; i < P.nEC; ++i) {
+            const int cntL = min((int)(end - b), LPV);
+            bool head, tail;
+            run_flags<LPV>(G, valid, o, cntL, head, tail);
+            const unsigned tails = group_bits<LPV>(__ballot_sync(G.mask, tail));
+#pragma unroll 1
+            for (int i = 0; i < cm.nrf; ++i) {
                 float ch = 0.f, cl = 0.f;
                 if (valid) {
-                    const double c = x[P.ec_base + (size_t)i * P.nE + col];
+                    const int64_t q = (int64_t)i * cm.xstride + col;
+                    double c = (double)l * x[cm.xbase + q];
+                    if (cm.eval) c *= (double)cm.eval[q];
                     ch = __double2float_rn(c);
                     cl = __double2float_rn(c - (double)ch);
                 }
-                const uint32_t row = ((uint32_t)i * P.ndirs + o) * (uint32_t)T.nSp;
-                for (int t = 0; t < cnt; ++t) {
+                // merged coefficient of each run (segmented inclusive scan, float-float)
+                int start = head;
+#pragma unroll
+                for (int d = 1; d < LPV; d <<= 1) {
+                    const float uh = __shfl_up_sync(G.mask, ch, d, LPV);
+                    const float ul = __shfl_up_sync(G.mask, cl, d, LPV);
+                    const int us = __shfl_up_sync(G.mask, start, d, LPV);
+                    if (G.sub >= d) {
+                        if (!start) ff_add(ch, cl, uh, ul);
+                        start |= us;
+                    }
+                }
+                const uint32_t row = (uint32_t)i * cm.rf_stride + o * (uint32_t)C.nSp;
+                unsigned m = tails;
+#pragma unroll 1
+                while (m) {
+                    const int t = __ffs(m) - 1;
+                    m &= m - 1;
                     const float th = __shfl_sync(G.mask, ch, t, LPV);
                     const float tl = __shfl_sync(G.mask, cl, t, LPV);
                     const uint32_t rt = __shfl_sync(G.mask, row, t, LPV);
                     if (th != 0.f || tl != 0.f) {
                         const Coef2 cf = coef2(th, tl);
-                        const float *L = T.ec + rt + base;
-#pragma unroll
-                        for (int k = 0; k < NP; ++k) dd2_fma(acc[k], cf, f2_ldg(L + 2 * LPV * k));
-                    }
-                }
-            }
-        }
-    }
-    if (P.nISO > 0) {
-        const uint32_t beg = P.iso_ptr[v], end = P.iso_ptr[v + 1];
-        for (uint32_t b = beg; b < end; b += LPV) {
-            const uint32_t j = b + G.sub;
-            const bool valid = j < end;
-            const uint32_t col = valid ? P.iso_col[j] : 0;
-            const int cnt = min((int)(end - b), LPV);
-            for (int i = 0; i < P.nISO; ++i) {
-                float ch = 0.f, cl = 0.f;
-                if (valid) {
-                    const double c = x[P.iso_base + (size_t)i * P.nISOv + col];
-                    ch = __double2float_rn(c);
-                    cl = __double2float_rn(c - (double)ch);
-                }
-                for (int t = 0; t < cnt; ++t) {
-                    const float th = __shfl_sync(G.mask, ch, t, LPV);
-                    const float tl = __shfl_sync(G.mask, cl, t, LPV);
-                    if (th != 0.f || tl != 0.f) {
-                        const Coef2 cf = coef2(th, tl);
-                        const float *L = T.iso + (size_t)i * T.nSp + base;
+                        const float *L = cm.lut + rt + base;
 #pragma unroll
                         for (int k = 0; k < NP; ++k) dd2_fma(acc[k], cf, f2_ldg(L + 2 * LPV * k));
                     }
@@ -240,7 +250,8 @@ __device__ __forceinline__ void forward_row_p(const OpDev &P, const PadLut &T, c
 }
 
 template <int LPV, int NP>
-__global__ void __launch_bounds__(kBlock) k_forward_p(const OpDev P, const PadLut T, const double *__restrict__ x,
+__global__ void __launch_bounds__(kBlock) k_forward_p(const OpDev P, const __grid_constant__ Comps C,
+                                                      const double *__restrict__ x,
                                                       double *__restrict__ yout, double *__restrict__ axout,
                                                       const double *__restrict__ yobs, const double *__restrict__ sqw,
                                                       double *__restrict__ partials, int vec_ok) {
@@ -253,7 +264,7 @@ __global__ void __launch_bounds__(kBlock) k_forward_p(const OpDev P, const PadLu
     double nrm = 0.0;
     for (int v = blockIdx.x * gpb + (int)threadIdx.x / LPV; v < P.nV; v += ngroups) {
         DD2 acc[NP];
-        forward_row_p<LPV, NP>(P, T, G, v, x, acc);
+        forward_row_p<LPV, NP>(C, G, v, x, acc);
 #pragma unroll
         for (int k = 0; k < NP; ++k) {
             const int s = 2 * (G.sub + k * LPV);
@@ -286,19 +297,18 @@ __global__ void __launch_bounds__(kBlock) k_forward_p(const OpDev P, const PadLu
     if (partials) block_sum_store(nrm, partials + (size_t)blockIdx.x * kRedSlots);
 }
 
-// <LUT row of item q, z> for the B items of a sub-batch (PairBatch); the total of item
-// q = sub / (LPV/B) ends in lane sub (butterfly reduce-scatter on packed accumulators,
-// halves combined at the end).
 // items per reduce-scatter batch: 8, or 4 when the pair registers are many
 template <int LPV, int NP>
 struct PairBatch {
     static constexpr int B = LPV < (NP >= 5 ? 4 : 8) ? LPV : (NP >= 5 ? 4 : 8);
 };
 
+// <LUT row of item q, z> for the B items of a sub-batch (PairBatch); the total of item
+// q = sub / (LPV/B) ends in lane sub (butterfly reduce-scatter on packed accumulators,
+// halves combined at the end).
 template <int LPV, int NP, class RowFn>
 __device__ __forceinline__ double batch_dots_p(const Group<LPV> &G, const float *__restrict__ lut, RowFn row,
-                                               int cnt, const f2 (&zh)[NP], const f2 (&zl)[NP],
-                                               const f2 (&znh)[NP]) {
+                                               int cnt, const f2 (&zh)[NP], const f2 (&zl)[NP]) {
     constexpr int B = PairBatch<LPV, NP>::B;
     DD2 Pq[B];
     const int base = 2 * G.sub;
@@ -312,7 +322,7 @@ __device__ __forceinline__ double batch_dots_p(const Group<LPV> &G, const float 
                 Coef2 zc;
                 zc.h = zh[k];
                 zc.l = zl[k];
-                zc.nh = znh[k];
+                zc.nh = zh[k] ^ 0x8000000080000000ull;  // both halves negated
                 dd2_fma(Pq[q], zc, f2_ldg(L + 2 * LPV * k));
             }
         }
@@ -332,12 +342,16 @@ __device__ __forceinline__ double batch_dots_p(const Group<LPV> &G, const float 
         }
     }
 #pragma unroll
-    for (int m = LPV / B / 2; m >= 1; m /= 2) dd2_add(Pq[0], dd2_shfl_xor(G.mask, Pq[0], m, LPV));
+    for (int m = LPV / PairBatch<LPV, NP>::B / 2; m >= 1; m /= 2) dd2_add(Pq[0], dd2_shfl_xor(G.mask, Pq[0], m, LPV));
     return dd2_hsum(Pq[0]);
 }
 
+// A' pass 1 over all compartments.  Per batch, one dot product per run of equal
+// orientation; every item of the run takes that total: IC items write l*<L,z> to the
+// per-segment scratch stream, EC / ISO items write their column of xout.
 template <int LPV, int NP>
-__global__ void __launch_bounds__(kBlock) k_adjoint_p(const OpDev P, const PadLut T, const double *__restrict__ yin,
+__global__ void __launch_bounds__(kBlock) k_adjoint_p(const OpDev P, const __grid_constant__ Comps C,
+                                                      const double *__restrict__ yin,
                                                       int in_mode, const double *__restrict__ x,
                                                       const double *__restrict__ yobs, const double *__restrict__ sqw,
                                                       const double *__restrict__ ax_a, const double *__restrict__ ax_b,
@@ -349,18 +363,16 @@ __global__ void __launch_bounds__(kBlock) k_adjoint_p(const OpDev P, const PadLu
     const int gpb = kBlock / LPV;
     const int ngroups = gridDim.x * gpb;
     const int nS = P.nS;
-    const int q_me = G.sub / SPAN;
-    const bool writer = (G.sub % SPAN) == 0;
     double nrm = 0.0;
     for (int v = blockIdx.x * gpb + (int)threadIdx.x / LPV; v < P.nV; v += ngroups) {
         double a[2 * NP];
         if (in_mode == 1) {
             DD2 acc[NP];
-            forward_row_p<LPV, NP>(P, T, G, v, x, acc);
+            forward_row_p<LPV, NP>(C, G, v, x, acc);
 #pragma unroll
             for (int k = 0; k < NP; ++k) dd2_val(acc[k], a[2 * k], a[2 * k + 1]);
         }
-        f2 zh[NP], zl[NP], znh[NP];
+        f2 zh[NP], zl[NP];
 #pragma unroll
         for (int k = 0; k < NP; ++k) {
             double zz[2];
@@ -381,63 +393,74 @@ __global__ void __launch_bounds__(kBlock) k_adjoint_p(const OpDev P, const PadLu
                     }
                 }
             }
-            split2(zz[0], zz[1], zh[k], zl[k], znh[k]);
+            f2 unused;
+            split2(zz[0], zz[1], zh[k], zl[k], unused);
         }
-        if (P.nIC > 0) {
-            const uint32_t beg = P.vox_ptr[v], end = P.vox_ptr[v + 1];
+#pragma unroll 1
+        for (int ci = 0; ci < C.n; ++ci) {
+            const Comp &cm = C.c[ci];
+            const uint32_t beg = cm.ptr[v], end = cm.ptr[v + 1];
+#pragma unroll 1
             for (uint32_t b = beg; b < end; b += LPV) {
                 const uint32_t j = b + G.sub;
                 const bool valid = j < end;
-                const uint32_t o = valid ? P.seg_o[j] : 0;
-                const float l = valid ? P.seg_l[j] : 0.f;
-                const int cntL = min((int)(end - b), LPV);
-                for (int i = 0; i < P.nIC; ++i) {
-                    const uint32_t row = ((uint32_t)i * P.ndirs + o) * (uint32_t)T.nSp;
-                    for (int t0 = 0; t0 < cntL; t0 += B) {
-                        const int cnt = min(B, cntL - t0);
-                        auto rowf = [&](int q) { return __shfl_sync(G.mask, row, t0 + q, LPV); };
-                        const double tot = batch_dots_p<LPV, NP>(G, T.ic, rowf, cnt, zh, zl, znh);
-                        const float lq = __shfl_sync(G.mask, l, t0 + q_me, LPV);
-                        if (writer && q_me < cnt) scratch[(size_t)i * P.n + b + t0 + q_me] = (double)lq * tot;
-                    }
+                uint32_t col = 0, o = 0;
+                float l = 1.f;
+                if (valid) {
+                    col = cm.col[j];
+                    if (cm.o) o = cm.o[j];
+                    if (cm.l) l = cm.l[j];
                 }
-            }
-        }
-        if (P.nEC > 0) {
-            const uint32_t beg = P.ec_ptr[v], end = P.ec_ptr[v + 1];
-            for (uint32_t b = beg; b < end; b += LPV) {
-                const uint32_t j = b + G.sub;
-                const bool valid = j < end;
-                const uint32_t o = valid ? P.ec_o[j] : 0;
-                const uint32_t col = valid ? P.ec_col[j] : 0;
                 const int cntL = min((int)(end - b), LPV);
-                for (int i = 0; i < P.nEC; ++i) {
-                    const uint32_t row = ((uint32_t)i * P.ndirs + o) * (uint32_t)T.nSp;
-                    for (int t0 = 0; t0 < cntL; t0 += B) {
-                        const int cnt = min(B, cntL - t0);
-                        auto rowf = [&](int q) { return __shfl_sync(G.mask, row, t0 + q, LPV); };
-                        const double tot = batch_dots_p<LPV, NP>(G, T.ec, rowf, cnt, zh, zl, znh);
-                        const uint32_t cq = __shfl_sync(G.mask, col, t0 + q_me, LPV);
-                        if (writer && q_me < cnt) xout[P.ec_base + (size_t)i * P.nE + cq] = tot;
+                bool head, tail;
+                run_flags<LPV>(G, valid, o, cntL, head, tail);
+                const unsigned tails = group_bits<LPV>(__ballot_sync(G.mask, tail));
+                const int K = __popc(tails);
+                // run (item) index of this lane's segment
+                const unsigned at_or_after = G.sub < 32 ? tails & (0xffffffffu << G.sub) : 0u;
+                const int my_tail = __ffs(at_or_after) - 1;
+                const int my_item = my_tail >= 0 ? __popc(tails & ((1u << my_tail) - 1u)) : -1;
+#pragma unroll 1
+                for (int i = 0; i < cm.nrf; ++i) {
+                    const uint32_t row = (uint32_t)i * cm.rf_stride + o * (uint32_t)C.nSp;
+#pragma unroll 1
+                    for (int u0 = 0; u0 < K; u0 += B) {
+                        const int cnt = min(B, K - u0);
+                        auto rowf = [&](int q) {
+                            return __shfl_sync(G.mask, row, (int)__fns(tails, 0, u0 + q + 1), LPV);
+                        };
+                        const double tot = batch_dots_p<LPV, NP>(G, cm.lut, rowf, cnt, zh, zl);
+                        const int q = my_item - u0;
+                        const bool mine = valid && q >= 0 && q < cnt;
+                        const double t = __shfl_sync(G.mask, tot, mine ? q * SPAN : 0, LPV);
+                        if (mine) {
+                            if (cm.to_scratch) scratch[(size_t)i * P.n + j] = (double)l * t;
+                            else xout[cm.xbase + (size_t)i * cm.xstride + col] = t;
+                        }
                     }
-                }
-            }
-        }
-        if (P.nISO > 0) {
-            const uint32_t beg = P.iso_ptr[v], end = P.iso_ptr[v + 1];
-            if (beg < end) {
-                for (int t0 = 0; t0 < P.nISO; t0 += B) {
-                    const int cnt = min(B, P.nISO - t0);
-                    auto rowf = [&](int q) { return (uint32_t)((t0 + q) * T.nSp); };
-                    const double tot = batch_dots_p<LPV, NP>(G, T.iso, rowf, cnt, zh, zl, znh);
-                    if (writer && q_me < cnt)
-                        for (uint32_t e = beg; e < end; ++e)
-                            xout[P.iso_base + (size_t)(t0 + q_me) * P.nISOv + P.iso_col[e]] = tot;
                 }
             }
         }
     }
     if (partials) block_sum_store(nrm, partials + (size_t)blockIdx.x * kRedSlots);
+}
+
+// compartment table of a handle for the padded FP32 LUT rows
+inline Comps make_comps(const cgb_op *op) {
+    Comps C;
+    C.n = 0;
+    C.nSp = op->nSp;
+    const uint32_t ndirs = (uint32_t)op->ndirs, nSp = (uint32_t)op->nSp;
+    if (op->nIC > 0)
+        C.c[C.n++] = Comp{op->vox_ptr, op->seg_f, op->seg_o, op->seg_l, op->eval, op->lutIC_p, 0, op->nF,
+                          ndirs * nSp, op->nIC, 1};
+    if (op->nEC > 0 && op->nE > 0)
+        C.c[C.n++] = Comp{op->ec_ptr, op->ec_col, op->ec_o, nullptr, nullptr, op->lutEC_p,
+                          (int64_t)op->nF * op->nIC, op->nE, ndirs * nSp, op->nEC, 0};
+    if (op->nISO > 0 && op->nISOv > 0)
+        C.c[C.n++] = Comp{op->iso_ptr, op->iso_col, nullptr, nullptr, nullptr, op->lutISO_p,
+                          (int64_t)op->nF * op->nIC + (int64_t)op->nE * op->nEC, op->nISOv, nSp, op->nISO, 0};
+    return C;
 }
 
 // (LPV, NP) pairs with kernels; 2*LPV*NP samples per voxel row

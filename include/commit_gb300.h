@@ -86,6 +86,22 @@ int cgb_op_shape(const cgb_op *op, int64_t *nrows, int64_t *ncols);
 /* Device bytes held by the handle. */
 int cgb_op_device_bytes(const cgb_op *op, size_t *bytes);
 
+/*
+ * Replace the LUT values (same shapes as at creation; host or device pointers, NULL leaves
+ * that compartment unchanged).  Used when the LUT itself is being fitted.  No counterpart
+ * in the reference, whose LUTs are fixed after load_kernels (commit/core.pyx:364-433).
+ */
+int cgb_op_set_lut(cgb_op *op, const float *lutIC, const float *lutEC, const float *lutISO);
+
+/*
+ * Gradient of a loss with respect to the LUTs given dLoss/dy = g (DEVICE, nrows doubles)
+ * at the point x (DEVICE, ncols doubles): g_ic[nIC*ndirs*nS], g_ec[nEC*ndirs*nS],
+ * g_iso[nISO*nS] (DEVICE doubles; NULL skips that compartment).  Deterministic: items are
+ * reduced per orientation in a fixed order.  No counterpart in the reference.
+ */
+int cgb_op_lut_grad(cgb_op *op, const double *x, const double *g, double *g_ic, double *g_ec, double *g_iso,
+                    void *stream);
+
 /* Select the arithmetic used by later FP64 applies (CGB_ARITH_F64 / CGB_ARITH_FF). */
 int cgb_op_set_arith(cgb_op *op, int arith);
 
