@@ -39,7 +39,9 @@ def parse():
     p.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     p.add_argument('--workload', default='hcp_1m')
     p.add_argument('--fibers', type=int, default=0, help='override the number of streamlines (smaller runs)')
-    p.add_argument('--arith', default='ff', choices=['ff', 'f64'])
+    p.add_argument('--arith', default='ff', choices=['ff', 'f64', 'bf16', 'fp16', 'f32'])
+    p.add_argument('--fista', action='store_true', help='FISTA time-to-tolerance, plain vs mixed + refinement')
+    p.add_argument('--fista-iters', type=int, default=1500)
     p.add_argument('--sample-frac', type=float, default=1.0 / 16.0, help='CPU sample: fraction of the segments')
     p.add_argument('--no-e2e', action='store_true')
     p.add_argument('--no-cpu', action='store_true')
@@ -114,14 +116,16 @@ def measured_peaks() -> dict:
     return {'hbm_gbs': 6800.0, 'src': 'fallback'}
 
 
-def algorithmic(D, K) -> tuple:
-    """Compulsory bytes and FMAs of one product (A or A'), LUT bytes excluded (on-chip)."""
+def algorithmic(D, K, reduced=False) -> tuple:
+    """Compulsory bytes and FMAs of one product (A or A'), LUT bytes excluded (on-chip).
+    Reduced precision: FP16 lengths and FP32 rows (columns stay FP64)."""
     n, nE, nI = D['IC']['n'], D['EC']['n'], D['ISO']['n']
     nIC, nEC, nISO = K['wmr'].shape[0], K['wmh'].shape[0], K['iso'].shape[0]
     nS = K['wmr'].shape[2]
     nrows = D['IC']['nVOX'] * nS
     ncols = D['IC']['nSTR'] * nIC + nE * nEC + nI * nISO
-    b = n * (4 + 4 + 2 + 4) + (nE * (4 + 2) if nEC else 0) + (nI * 4 if nISO else 0) + ncols * 8 + nrows * 8
+    sl, sy = (2, 4) if reduced else (4, 8)
+    b = n * (4 + 4 + 2 + sl) + (nE * (4 + 2) if nEC else 0) + (nI * 4 if nISO else 0) + ncols * 8 + nrows * sy
     f = n * nS * nIC + nE * nS * nEC + nI * nS * nISO
     return b, f, nrows, ncols
 
@@ -243,16 +247,21 @@ def run_ours(args):
     from commit_gb300 import synth
     from commit_gb300.operator import LinearOperator
     spec, D, K, tgen = build_workload(args, 'cuda')
-    A = LinearOperator(D, K, None, arith=args.arith, device=dev.index)
+    if args.fista:
+        return run_fista(args, spec, D, K, dev)
+    reduced = args.arith in ('bf16', 'fp16', 'f32')
+    A = LinearOperator(D, K, None, arith='ff' if reduced else args.arith, device=dev.index)
     At = A.T
-    nbytes, nfma, nrows, ncols = algorithmic(D, K)
-    x = torch.from_numpy(synth.make_x(ncols, spec.seed + 1)).to(dev)
-    y = torch.empty(nrows, dtype=torch.float64, device=dev)
-    g = torch.empty(ncols, dtype=torch.float64, device=dev)
+    nbytes, nfma, nrows, ncols = algorithmic(D, K, reduced)
+    vdt = torch.float32 if reduced else torch.float64
+    x = torch.from_numpy(synth.make_x(ncols, spec.seed + 1)).to(dev).to(vdt)
+    y = torch.empty(nrows, dtype=vdt, device=dev)
+    g = torch.empty(ncols, dtype=vdt, device=dev)
     st = torch.cuda.current_stream(dev)
+    kw = {'arith': args.arith} if reduced else {}
     for _ in range(args.warmup):
-        A.dot(x, out=y)
-        At.dot(y, out=g)
+        A.dot(x, out=y, **kw)
+        At.dot(y, out=g, **kw)
     torch.cuda.synchronize()
     if ws > 1:
         torch.distributed.barrier()
@@ -265,9 +274,9 @@ def run_ours(args):
     e_start.record(st)
     for k in range(args.steps):
         ev[k][0].record(st)
-        A.dot(x, out=y)
+        A.dot(x, out=y, **kw)
         ev[k][1].record(st)
-        At.dot(y, out=g)
+        At.dot(y, out=g, **kw)
         ev[k][2].record(st)
     e_end.record(st)
     torch.cuda.synchronize()
@@ -286,7 +295,8 @@ def run_ours(args):
     achieved = nbytes / (dom_ms / 1000.0) / 1e9
     out = {'metric': METRIC, 'value': value, 'unit': 'pairs/s', 'n_gpus': ws, 'steps': args.steps,
            'warmup': args.warmup, 'ms_per_step': ms / args.steps, 'higher_is_better': True, 'scaling': 'weak',
-           'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'config': workload_config(spec, D, K, args),
+           'vs_baseline': None, 'dtype': 'f32 rows / ' + args.arith + ' LUT' if reduced else 'f64',
+           'data': 'synthetic', 'config': workload_config(spec, D, K, args),
            'roofline': {'bound': 'hbm', 'kernel': dom, 'achieved': achieved, 'peak': peaks['hbm_gbs'],
                         'unit': 'GB/s', 'frac': achieved / peaks['hbm_gbs'], 'peak_src': peaks['src'],
                         'traffic': None, 'algorithmic_bytes_per_launch': nbytes,
@@ -294,7 +304,7 @@ def run_ours(args):
                         'fma_per_product': nfma, 'achieved_gfma_s': nfma / (dom_ms / 1000.0) / 1e9},
            'clocks': clk, 'gpu_launches': args.steps * (1 + 2), 'setup_s': {'generate': tgen}}
     # end to end through the public API on pinned host buffers
-    if not args.no_e2e:
+    if not args.no_e2e and not reduced:
         xh = torch.empty(ncols, dtype=torch.float64, pin_memory=True).numpy()
         xh[:] = x.cpu().numpy()
         yh = torch.empty(nrows, dtype=torch.float64, pin_memory=True).numpy()
@@ -321,6 +331,60 @@ def run_ours(args):
         print(json.dumps(out))
     if ws > 1:
         torch.distributed.destroy_process_group()
+    return 0
+
+
+def run_fista(args, spec, D, K, dev):
+    """FISTA time-to-tolerance (nnls on all compartments): plain FP64-accurate solver vs
+    reduced precision (BF16 LUT) followed by FP64 refinement, both measured against a
+    reference solution from a 4x longer plain solve.  Prints one JSON line."""
+    import torch
+    from commit_gb300 import solvers, synth
+    from commit_gb300.operator import LinearOperator
+    A = LinearOperator(D, K, None, arith='ff', device=dev.index)
+    x_true = synth.make_x(A.nCOLS, spec.seed + 1)
+    y = A.dot(torch.from_numpy(x_true).to(dev))
+    y = torch.from_numpy(synth.make_signal(y.cpu().numpy(), spec.seed + 2)).to(dev)
+    rp = {'startIC': 0, 'sizeIC': A.ICnSTR * A.ICnRF, 'startEC': A.ICnSTR * A.ICnRF, 'sizeEC': A.ECn * A.ECnRF,
+          'startISO': A.ICnSTR * A.ICnRF + A.ECn * A.ECnRF, 'sizeISO': A.ISOn * A.ISOnRF,
+          'regIC': None, 'regEC': None, 'regISO': None, 'nnIC': True, 'nnEC': True, 'nnISO': True,
+          'dictIC_params': None, 'dictEC_params': None, 'dictISO_params': None}
+    reg = lambda: solvers.init_regularisation(dict(rp))  # noqa: E731
+    n = args.fista_iters
+    t0 = time.perf_counter()
+    x_ref, d_ref = solvers.solve(y, A, A.T, tol_fun=0.0, tol_x=0.0, max_iter=4 * n, verbose=0, regularisation=reg())
+    t_ref = time.perf_counter() - t0
+    _, d_plain = solvers.solve(y, A, A.T, tol_fun=0.0, tol_x=0.0, max_iter=n, verbose=0, regularisation=reg(),
+                               x_ref=x_ref)
+    # warm the reduced-precision LUT copies (one-time) before timing the mixed solve
+    A.dot(torch.zeros(A.nCOLS, dtype=torch.float32, device=dev), arith='bf16')
+    n_mix = (3 * n) // 4
+    _, d_mix = solvers.solve_mixed(y, A, tol_fun=0.0, tol_x=0.0, max_iter=n_mix, verbose=0, regularisation=reg(),
+                                   arith='bf16', refine_max_iter=n - n_mix, x_ref=x_ref)
+
+    def first_below(tr, tol):
+        idx = np.flatnonzero(tr[:, 1] <= tol)
+        return (float(tr[idx[0], 0]), int(idx[0]) + 1) if idx.size else (None, None)
+
+    res = {}
+    for tol in (1e-2, 1e-3, 1e-4):
+        tp, ip = first_below(d_plain['trace'], tol)
+        tm, im = first_below(d_mix['trace'], tol)
+        res[f'{tol:g}'] = {'plain_s': tp, 'plain_iter': ip, 'mixed_s': tm, 'mixed_iter': im,
+                           'speedup': (tp / tm) if (tp and tm) else None}
+    tr_p, tr_m = d_plain['trace'], d_mix['trace']
+    out = {'metric': 'FISTA time-to-tolerance, plain (float-float FP64) vs BF16-LUT + FP64 refinement',
+           'unit': 's', 'higher_is_better': False, 'data': 'synthetic',
+           'config': workload_config(spec, D, K, args) | {'regulariser': 'nnls (all compartments)',
+                                                           'reference': f'plain FISTA, {4 * n} iterations'},
+           'plain': {'iterations': int(d_plain['iterations']), 'seconds': float(tr_p[-1, 0]),
+                     'ms_per_iteration': 1000.0 * float(tr_p[-1, 0]) / len(tr_p), 'final_rel': float(tr_p[-1, 1])},
+           'mixed': {'iterations': int(d_mix['iterations']), 'mixed_iterations': n_mix,
+                     'seconds': float(tr_m[-1, 0]),
+                     'ms_per_mixed_iteration': 1000.0 * float(d_mix['mixed']['trace'][-1, 0]) / n_mix,
+                     'final_rel': float(tr_m[-1, 1])},
+           'reference_solve_s': t_ref, 'time_to_tol': res}
+    print(json.dumps(out))
     return 0
 
 

@@ -71,7 +71,7 @@ struct cgb_op {
     float *lutIC, *lutEC, *lutISO;
     float *lutIC_p, *lutEC_p, *lutISO_p;  // zero-padded rows of stride nSp (paired kernels)
     int nSp;
-    void *lutIC_r, *lutEC_r;        // reduced-precision LUT copies
+    void *lutIC_r, *lutEC_r, *lutISO_r;  // reduced-precision LUT copies (padded pair layout)
     int lut_r_kind;                 // CGB_ARITH_BF16 / CGB_ARITH_FP16 / 0
     __half *seg_l16;                // FP16 lengths scaled by 2^k (reduced path)
     float len16_inv_scale;          // 2^-k
@@ -93,6 +93,7 @@ struct cgb_op {
     // reduced-precision LUT rows (padded pair layout) for CGB_ARITH_BF16 / FP16 / F32
     const void *lut_r_ic(int kind) const { return kind == CGB_ARITH_F32 ? (const void *)lutIC_p : lutIC_r; }
     const void *lut_r_ec(int kind) const { return kind == CGB_ARITH_F32 ? (const void *)lutEC_p : lutEC_r; }
+    const void *lut_r_iso(int kind) const { return kind == CGB_ARITH_F32 ? (const void *)lutISO_p : lutISO_r; }
 };
 
 namespace cgb {

@@ -14,6 +14,7 @@
 // decisions exactly as the reference does.
 #include <math.h>
 
+#include <chrono>
 #include <vector>
 
 #include "cgb_internal.cuh"
@@ -21,7 +22,7 @@
 namespace cgb {
 namespace {
 
-constexpr int kStatSlots = 8;
+constexpr int kStatSlots = 10;
 
 struct RegDev {
     int64_t sIC, nIC, sEC, nEC, sISO, nISO;
@@ -165,8 +166,9 @@ __global__ void k_group_norms(const double *__restrict__ x, int64_t nx, const in
 
 // FISTA statistics: slots 0 <x-xh,g>, 1 |x-xh|^2, 2 |x-p|^2, 3 |x|^2, 4.. l1 terms
 __global__ void k_stats(const double *__restrict__ x, const double *__restrict__ xh, const double *__restrict__ g,
-                        const double *__restrict__ p, int64_t n, L1Terms T, double *__restrict__ partials) {
-    double v[kStatSlots] = {0, 0, 0, 0, 0, 0, 0, 0};
+                        const double *__restrict__ p, int64_t n, L1Terms T, const double *__restrict__ xref,
+                        double *__restrict__ partials) {
+    double v[kStatSlots] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const double xi = x[i];
         if (xh) {
@@ -182,6 +184,12 @@ __global__ void k_stats(const double *__restrict__ x, const double *__restrict__
 #pragma unroll
         for (int k = 0; k < 4; ++k)
             if (k < T.n && i >= T.t[k].a && i < T.t[k].b) v[4 + k] += fabs(T.t[k].w ? T.t[k].w[i] * xi : xi);
+        if (xref) {
+            const double r = xref[i];
+            const double d = xi - r;
+            v[8] = fma(d, d, v[8]);
+            v[9] = fma(r, r, v[9]);
+        }
     }
     block_sum_store_n<kStatSlots>(v, partials + (size_t)blockIdx.x * kRedSlots);
 }
@@ -386,7 +394,7 @@ struct Solver {
     int stats(const double *x, const double *xh, const double *g, const double *p) {
         const int64_t nc = op->ncols;
         const int gb = elem_grid(op, nc);
-        k_stats<<<gb, kBlock, 0, st>>>(x, xh, g, p, nc, terms, ws.pstats);
+        k_stats<<<gb, kBlock, 0, st>>>(x, xh, g, p, nc, terms, xh ? prm->x_ref : nullptr, ws.pstats);
         CGB_CUDA(cudaGetLastError());
         CGB_TRY(finalize(ws.pstats, gb, kStatSlots, op->dscal + 1, st));
         if (group_in_omega) {
@@ -396,9 +404,9 @@ struct Solver {
             k_group_norms<<<(int)blocks, kBlock, 0, st>>>(x, op->ncols, reg->group_idx, reg->group_ptr, reg->group_w,
                                                          reg->ngroups, ws.pgrp);
             CGB_CUDA(cudaGetLastError());
-            CGB_TRY(finalize(ws.pgrp, (int)blocks, 1, op->dscal + 9, st));
+            CGB_TRY(finalize(ws.pgrp, (int)blocks, 1, op->dscal + 11, st));
         } else {
-            CGB_CUDA(cudaMemsetAsync(op->dscal + 9, 0, sizeof(double), st));
+            CGB_CUDA(cudaMemsetAsync(op->dscal + 11, 0, sizeof(double), st));
         }
         return CGB_OK;
     }
@@ -406,7 +414,7 @@ struct Solver {
     double omega_from(const double *h) const {
         double om = 0.0;
         for (int k = 0; k < terms.n; ++k) om += l1coef[k] * h[5 + k];
-        if (group_in_omega) om += group_omega_coef * h[9];
+        if (group_in_omega) om += group_omega_coef * h[11];
         return om;
     }
 
@@ -441,9 +449,9 @@ struct Solver {
         }
         calls += sa >= 0 ? 1 : 2;
         if (g > 0) {
-            CGB_TRY(finalize(ws.pres, g, 1, op->dscal + 10, st));
+            CGB_TRY(finalize(ws.pres, g, 1, op->dscal + 12, st));
         } else {
-            CGB_CUDA(cudaMemsetAsync(op->dscal + 10, 0, sizeof(double), st));
+            CGB_CUDA(cudaMemsetAsync(op->dscal + 12, 0, sizeof(double), st));
         }
         return CGB_OK;
     }
@@ -460,13 +468,14 @@ struct Solver {
         double *h = op->h_scal;
         const double beta = 0.9;
         int backtracks = 0;
+        const auto t_start = std::chrono::steady_clock::now();
         // initialisation (solvers.py:260-286)
         CGB_CUDA(cudaMemcpyAsync(ws.xhat, x, nc * sizeof(double), cudaMemcpyDeviceToDevice, st));
         CGB_TRY(gradient(ws.xhat, ws.grad, -1, -1, 0.0, 0.0));
         CGB_TRY(prox(ws.xhat, ws.xhat, nullptr, 0.0, 1.0));
         CGB_TRY(stats(ws.xhat, nullptr, nullptr, nullptr));
         CGB_TRY(fetch(h));
-        double res_norm = sqrt(h[10]);
+        double res_norm = sqrt(h[12]);
         double reg_term = omega_from(h);
         double prev_obj = 0.5 * res_norm * res_norm + reg_term;
         double told = 1.0;
@@ -477,7 +486,7 @@ struct Solver {
             int g = 0;
             k_dot<<<elem_grid(op, nc), kBlock, 0, st>>>(ws.grad, ws.grad, nc, ws.pstats);
             CGB_CUDA(cudaGetLastError());
-            CGB_TRY(finalize(ws.pstats, elem_grid(op, nc), 1, op->dscal + 11, st));
+            CGB_TRY(finalize(ws.pstats, elem_grid(op, nc), 1, op->dscal + 13, st));
             if (mixed) {
                 CGB_TRY(launch_resnorm_mix(op, ws.grad, nullptr, ws.sqw32, op->partials, nullptr, nullptr, st,
                                            prm->arith, &g));
@@ -486,13 +495,13 @@ struct Solver {
             }
             calls++;
             if (g > 0) {
-                CGB_TRY(finalize(op->partials, g, 1, op->dscal + 12, st));
+                CGB_TRY(finalize(op->partials, g, 1, op->dscal + 14, st));
             } else {
-                CGB_CUDA(cudaMemsetAsync(op->dscal + 12, 0, sizeof(double), st));
+                CGB_CUDA(cudaMemsetAsync(op->dscal + 14, 0, sizeof(double), st));
             }
             CGB_TRY(fetch(h));
         }
-        const double Ln = sqrt(h[12]) / sqrt(h[11]);
+        const double Ln = sqrt(h[14]) / sqrt(h[13]);
         const double L = Ln * Ln;
         double step = 1.9 / L;
         if (prm->verbose == 4) {
@@ -514,7 +523,7 @@ struct Solver {
                 return fetch(h);
             };
             CGB_TRY(eval_x(step));
-            qfval = 0.5 * sqrt(h[10]) * sqrt(h[10]);
+            qfval = 0.5 * sqrt(h[12]) * sqrt(h[12]);
             if (it == 1) qfval = prev_obj;
             reg_term_x = omega_from(h);
             double q = qfval + h[1] + 0.5 / step * (sqrt(h[2]) * sqrt(h[2])) + reg_term_x;
@@ -528,6 +537,10 @@ struct Solver {
                 q = qfval + h[1] + 0.5 / step * (sqrt(h[2]) * sqrt(h[2])) + reg_term_x;
                 res_norm = sqrt(h[0]);
                 curr_obj = 0.5 * res_norm * res_norm + reg_term_x;
+            }
+            if (prm->trace && prm->x_ref && it <= prm->trace_len) {
+                prm->trace[2 * (it - 1)] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+                prm->trace[2 * (it - 1) + 1] = sqrt(h[9]) / sqrt(h[10]);
             }
             abs_obj = fabs(curr_obj - prev_obj);
             rel_obj = abs_obj / curr_obj;
@@ -737,11 +750,11 @@ static int l1_sum(const double *x, const double *w, int64_t a, int64_t b, double
     const int g = grid_n(b - a) > 1024 ? 1024 : grid_n(b - a);
     double *part = nullptr, *dres = nullptr;
     CGB_CUDA(cudaMallocAsync((void **)&part, (size_t)g * kRedSlots * sizeof(double), st));
-    CGB_CUDA(cudaMallocAsync((void **)&dres, 8 * sizeof(double), st));
+    CGB_CUDA(cudaMallocAsync((void **)&dres, kStatSlots * sizeof(double), st));
     L1Terms T;
     T.n = 1;
     T.t[0] = L1Term{a, b, w};
-    k_stats<<<g, kBlock, 0, st>>>(x, nullptr, nullptr, nullptr, b, T, part);
+    k_stats<<<g, kBlock, 0, st>>>(x, nullptr, nullptr, nullptr, b, T, nullptr, part);
     k_finalize<<<kStatSlots, kBlock, 0, st>>>(part, g, dres);
     double h[8];
     cudaError_t e = cudaMemcpyAsync(h, dres, 8 * sizeof(double), cudaMemcpyDeviceToHost, st);

@@ -186,7 +186,7 @@ using namespace cgb;
 static void free_op(cgb_op *op) {
     if (!op) return;
     free_grad_state(op);
-    void *ptrs[] = {op->lutIC, op->lutEC, op->lutISO, op->lutIC_p, op->lutEC_p, op->lutISO_p, op->lutIC_r, op->lutEC_r, op->seg_l16, op->vox_ptr,
+    void *ptrs[] = {op->lutIC, op->lutEC, op->lutISO, op->lutIC_p, op->lutEC_p, op->lutISO_p, op->lutIC_r, op->lutEC_r, op->lutISO_r, op->seg_l16, op->vox_ptr,
                     op->seg_f, op->eval, op->fib_ptr, op->fib_perm, op->ec_ptr, op->ec_col, op->iso_ptr,
                     op->iso_col, op->seg_o, op->ec_o, op->seg_l, op->scratch, op->scratch32, op->partials,
                     op->dscal, op->d_in, op->d_out, op->d_x64};

@@ -114,16 +114,21 @@ int ensure_reduced(cgb_op *op, int arith) {
     if (op->lut_r_kind != arith) {
         if (op->lutIC_r) cudaFree(op->lutIC_r);
         if (op->lutEC_r) cudaFree(op->lutEC_r);
-        op->lutIC_r = op->lutEC_r = nullptr;
-        const size_t nic = (size_t)op->nIC * op->ndirs * op->nSp, nec = (size_t)op->nEC * op->ndirs * op->nSp;
+        if (op->lutISO_r) cudaFree(op->lutISO_r);
+        op->lutIC_r = op->lutEC_r = op->lutISO_r = nullptr;
+        const size_t nic = (size_t)op->nIC * op->ndirs * op->nSp, nec = (size_t)op->nEC * op->ndirs * op->nSp,
+                     niso = (size_t)op->nISO * op->nSp;
         CGB_CUDA(cudaMalloc(&op->lutIC_r, (nic ? nic : 1) * 2));
         CGB_CUDA(cudaMalloc(&op->lutEC_r, (nec ? nec : 1) * 2));
+        CGB_CUDA(cudaMalloc(&op->lutISO_r, (niso ? niso : 1) * 2));
         if (arith == CGB_ARITH_BF16) {
             if (nic) k_to_bf16<<<grid_n(nic), 256>>>(op->lutIC_p, (__nv_bfloat16 *)op->lutIC_r, nic);
             if (nec) k_to_bf16<<<grid_n(nec), 256>>>(op->lutEC_p, (__nv_bfloat16 *)op->lutEC_r, nec);
+            if (niso) k_to_bf16<<<grid_n(niso), 256>>>(op->lutISO_p, (__nv_bfloat16 *)op->lutISO_r, niso);
         } else {
             if (nic) k_to_fp16<<<grid_n(nic), 256>>>(op->lutIC_p, (__half *)op->lutIC_r, nic);
             if (nec) k_to_fp16<<<grid_n(nec), 256>>>(op->lutEC_p, (__half *)op->lutEC_r, nec);
+            if (niso) k_to_fp16<<<grid_n(niso), 256>>>(op->lutISO_p, (__half *)op->lutISO_r, niso);
         }
         CGB_CUDA(cudaGetLastError());
         op->lut_r_kind = arith;

@@ -43,97 +43,87 @@ struct LutPair<float> {
     __device__ static __forceinline__ f2 ld(const float *p) { return f2_ldg(p); }
 };
 
+// One compartment for the reduced-precision kernels (see Comp in operator_pair.cuh); the
+// LUT rows are of type LT and IC lengths may come as scaled FP16 values.
 template <class LT>
-struct MixLut {
-    const LT *ic, *ec;
-    const float *iso;  // ISO rows stay FP32 (nISO x nSp floats)
+struct CompM {
+    const uint32_t *ptr, *col;
+    const uint16_t *o;
+    const float *l;          // FP32 lengths (or null)
+    const __half *l16;       // FP16 lengths * 2^k (or null)
+    float l16_scale;         // 2^-k
+    const uint32_t *eval;
+    const LT *lut;
+    int64_t xbase, xstride;
+    uint32_t rf_stride;
+    int nrf;
+    int to_scratch;
+};
+
+template <class LT>
+struct CompsM {
+    CompM<LT> c[3];
+    int n;
     int nSp;
-    const __half *len16;  // scaled FP16 lengths (null: use seg_l)
-    float len_inv_scale;
 };
 
 template <class LT, int LPV, int NP>
-__device__ __forceinline__ void forward_row_mix(const OpDev &P, const MixLut<LT> &T, const Group<LPV> &G, int v,
+__device__ __forceinline__ void forward_row_mix(const CompsM<LT> &C, const Group<LPV> &G, int v,
                                                 const double *__restrict__ x, f2 (&acc)[NP]) {
 #pragma unroll
     for (int k = 0; k < NP; ++k) acc[k] = 0ull;
     const int base = 2 * G.sub;
-    if (P.nIC > 0) {
-        const uint32_t beg = P.vox_ptr[v], end = P.vox_ptr[v + 1];
-        for (uint32_t b = beg; b < end; b += LPV) {
-            const uint32_t j = b + G.sub;
-            const bool valid = j < end;
-            uint32_t f = 0, o = 0;
-            float l = 0.f;
-            if (valid) {
-                f = P.seg_f[j];
-                o = P.seg_o[j];
-                l = T.len16 ? __half2float(T.len16[j]) * T.len_inv_scale : P.seg_l[j];
-            }
-            const int cnt = min((int)(end - b), LPV);
-            for (int i = 0; i < P.nIC; ++i) {
-                float c = 0.f;
-                if (valid) {
-                    const size_t col = (size_t)i * P.nF + f;
-                    c = l * (float)x[col] * (float)P.eval[col];
-                }
-                const uint32_t row = ((uint32_t)i * P.ndirs + o) * (uint32_t)T.nSp;
-                for (int t = 0; t < cnt; ++t) {
-                    const float ct = __shfl_sync(G.mask, c, t, LPV);
-                    const uint32_t rt = __shfl_sync(G.mask, row, t, LPV);
-                    if (ct != 0.f) {
-                        const f2 c2 = f2_pack(ct, ct);
-                        const LT *L = T.ic + rt + base;
-#pragma unroll
-                        for (int k = 0; k < NP; ++k) acc[k] = f2_fma(c2, LutPair<LT>::ld(L + 2 * LPV * k), acc[k]);
-                    }
-                }
-            }
-        }
-    }
-    if (P.nEC > 0) {
-        const uint32_t beg = P.ec_ptr[v], end = P.ec_ptr[v + 1];
+#pragma unroll 1
+    for (int ci = 0; ci < C.n; ++ci) {
+        const CompM<LT> &cm = C.c[ci];
+        const uint32_t beg = cm.ptr[v], end = cm.ptr[v + 1];
+#pragma unroll 1
         for (uint32_t b = beg; b < end; b += LPV) {
             const uint32_t j = b + G.sub;
             const bool valid = j < end;
             uint32_t col = 0, o = 0;
+            float l = 1.f;
             if (valid) {
-                col = P.ec_col[j];
-                o = P.ec_o[j];
+                col = cm.col[j];
+                if (cm.o) o = cm.o[j];
+                if (cm.l16) l = __half2float(cm.l16[j]) * cm.l16_scale;
+                else if (cm.l) l = cm.l[j];
             }
-            const int cnt = min((int)(end - b), LPV);
-            for (int i = 0; i < P.nEC; ++i) {
-                const float c = valid ? (float)x[P.ec_base + (size_t)i * P.nE + col] : 0.f;
-                const uint32_t row = ((uint32_t)i * P.ndirs + o) * (uint32_t)T.nSp;
-                for (int t = 0; t < cnt; ++t) {
+            const int cntL = min((int)(end - b), LPV);
+            bool head, tail;
+            run_flags<LPV>(G, valid, o, cntL, head, tail);
+            const unsigned tails = group_bits<LPV>(__ballot_sync(G.mask, tail));
+#pragma unroll 1
+            for (int i = 0; i < cm.nrf; ++i) {
+                float c = 0.f;
+                if (valid) {
+                    const int64_t q = (int64_t)i * cm.xstride + col;
+                    c = l * (float)x[cm.xbase + q];
+                    if (cm.eval) c *= (float)cm.eval[q];
+                }
+                int start = head;
+#pragma unroll
+                for (int d = 1; d < LPV; d <<= 1) {
+                    const float u = __shfl_up_sync(G.mask, c, d, LPV);
+                    const int us = __shfl_up_sync(G.mask, start, d, LPV);
+                    if (G.sub >= d) {
+                        if (!start) c += u;
+                        start |= us;
+                    }
+                }
+                const uint32_t row = (uint32_t)i * cm.rf_stride + o * (uint32_t)C.nSp;
+                unsigned m = tails;
+#pragma unroll 1
+                while (m) {
+                    const int t = __ffs(m) - 1;
+                    m &= m - 1;
                     const float ct = __shfl_sync(G.mask, c, t, LPV);
                     const uint32_t rt = __shfl_sync(G.mask, row, t, LPV);
                     if (ct != 0.f) {
                         const f2 c2 = f2_pack(ct, ct);
-                        const LT *L = T.ec + rt + base;
+                        const LT *L = cm.lut + rt + base;
 #pragma unroll
                         for (int k = 0; k < NP; ++k) acc[k] = f2_fma(c2, LutPair<LT>::ld(L + 2 * LPV * k), acc[k]);
-                    }
-                }
-            }
-        }
-    }
-    if (P.nISO > 0) {
-        const uint32_t beg = P.iso_ptr[v], end = P.iso_ptr[v + 1];
-        for (uint32_t b = beg; b < end; b += LPV) {
-            const uint32_t j = b + G.sub;
-            const bool valid = j < end;
-            const uint32_t col = valid ? P.iso_col[j] : 0;
-            const int cnt = min((int)(end - b), LPV);
-            for (int i = 0; i < P.nISO; ++i) {
-                const float c = valid ? (float)x[P.iso_base + (size_t)i * P.nISOv + col] : 0.f;
-                for (int t = 0; t < cnt; ++t) {
-                    const float ct = __shfl_sync(G.mask, c, t, LPV);
-                    if (ct != 0.f) {
-                        const f2 c2 = f2_pack(ct, ct);
-                        const float *L = T.iso + (size_t)i * T.nSp + base;
-#pragma unroll
-                        for (int k = 0; k < NP; ++k) acc[k] = f2_fma(c2, f2_ldg(L + 2 * LPV * k), acc[k]);
                     }
                 }
             }
@@ -143,18 +133,17 @@ __device__ __forceinline__ void forward_row_mix(const OpDev &P, const MixLut<LT>
 
 // y = A x (float rows); optional ax_out; optional FP64 partials of |sqw*(Ax - yobs)|^2
 template <class LT, int LPV, int NP>
-__global__ void __launch_bounds__(kBlock) k_forward_mix(const OpDev P, const MixLut<LT> T,
+__global__ void __launch_bounds__(kBlock) k_forward_mix(const int nV, const int nS, const __grid_constant__ CompsM<LT> C,
                                                         const double *__restrict__ x, float *__restrict__ yout,
                                                         float *__restrict__ axout, const float *__restrict__ yobs,
                                                         const float *__restrict__ sqw, double *__restrict__ partials) {
     const Group<LPV> G;
     const int gpb = kBlock / LPV;
     const int ngroups = gridDim.x * gpb;
-    const int nS = P.nS;
     double nrm = 0.0;
-    for (int v = blockIdx.x * gpb + (int)threadIdx.x / LPV; v < P.nV; v += ngroups) {
+    for (int v = blockIdx.x * gpb + (int)threadIdx.x / LPV; v < nV; v += ngroups) {
         f2 acc[NP];
-        forward_row_mix<LT, LPV, NP>(P, T, G, v, x, acc);
+        forward_row_mix<LT, LPV, NP>(C, G, v, x, acc);
         float vn = 0.f;
 #pragma unroll
         for (int k = 0; k < NP; ++k) {
@@ -215,7 +204,8 @@ __device__ __forceinline__ float batch_dots_mix(const Group<LPV> &G, const LT *_
 // A' pass 1.  in_mode 0: z = yin; 1: z = sqw*r, r = sqw*(A x - yobs) (FP64 norm partials);
 // 2: as 1 with A x = ca*ax_a + cb*ax_b.  IC terms -> scr (FP32), EC/ISO -> xout (FP64).
 template <class LT, int LPV, int NP>
-__global__ void __launch_bounds__(kBlock) k_adjoint_mix(const OpDev P, const MixLut<LT> T,
+__global__ void __launch_bounds__(kBlock) k_adjoint_mix(const int nV, const int nS, const int64_t n,
+                                                        const __grid_constant__ CompsM<LT> C,
                                                         const float *__restrict__ yin, int in_mode,
                                                         const double *__restrict__ x, const float *__restrict__ yobs,
                                                         const float *__restrict__ sqw,
@@ -227,13 +217,10 @@ __global__ void __launch_bounds__(kBlock) k_adjoint_mix(const OpDev P, const Mix
     const Group<LPV> G;
     const int gpb = kBlock / LPV;
     const int ngroups = gridDim.x * gpb;
-    const int nS = P.nS;
-    const int q_me = G.sub / SPAN;
-    const bool writer = (G.sub % SPAN) == 0;
     double nrm = 0.0;
-    for (int v = blockIdx.x * gpb + (int)threadIdx.x / LPV; v < P.nV; v += ngroups) {
+    for (int v = blockIdx.x * gpb + (int)threadIdx.x / LPV; v < nV; v += ngroups) {
         f2 acc[NP];
-        if (in_mode == 1) forward_row_mix<LT, LPV, NP>(P, T, G, v, x, acc);
+        if (in_mode == 1) forward_row_mix<LT, LPV, NP>(C, G, v, x, acc);
         f2 z[NP];
         float vn = 0.f;
 #pragma unroll
@@ -259,56 +246,56 @@ __global__ void __launch_bounds__(kBlock) k_adjoint_mix(const OpDev P, const Mix
             z[k] = f2_pack(zz[0], zz[1]);
         }
         nrm += (double)vn;
-        if (P.nIC > 0) {
-            const uint32_t beg = P.vox_ptr[v], end = P.vox_ptr[v + 1];
+#pragma unroll 1
+        for (int ci = 0; ci < C.n; ++ci) {
+            const CompM<LT> &cm = C.c[ci];
+            const uint32_t beg = cm.ptr[v], end = cm.ptr[v + 1];
+#pragma unroll 1
             for (uint32_t b = beg; b < end; b += LPV) {
                 const uint32_t j = b + G.sub;
                 const bool valid = j < end;
-                const uint32_t o = valid ? P.seg_o[j] : 0;
-                const float l = valid ? (T.len16 ? __half2float(T.len16[j]) * T.len_inv_scale : P.seg_l[j]) : 0.f;
-                const int cntL = min((int)(end - b), LPV);
-                for (int i = 0; i < P.nIC; ++i) {
-                    const uint32_t row = ((uint32_t)i * P.ndirs + o) * (uint32_t)T.nSp;
-                    for (int t0 = 0; t0 < cntL; t0 += B) {
-                        const int cnt = min(B, cntL - t0);
-                        auto rowf = [&](int q) { return __shfl_sync(G.mask, row, t0 + q, LPV); };
-                        const float tot = batch_dots_mix<LPV, NP, LT>(G, T.ic, rowf, cnt, z);
-                        const float lq = __shfl_sync(G.mask, l, t0 + q_me, LPV);
-                        if (writer && q_me < cnt) scr[(size_t)i * P.n + b + t0 + q_me] = lq * tot;
-                    }
+                uint32_t col = 0, o = 0;
+                float l = 1.f;
+                if (valid) {
+                    col = cm.col[j];
+                    if (cm.o) o = cm.o[j];
+                    if (cm.l16) l = __half2float(cm.l16[j]) * cm.l16_scale;
+                    else if (cm.l) l = cm.l[j];
                 }
-            }
-        }
-        if (P.nEC > 0) {
-            const uint32_t beg = P.ec_ptr[v], end = P.ec_ptr[v + 1];
-            for (uint32_t b = beg; b < end; b += LPV) {
-                const uint32_t j = b + G.sub;
-                const bool valid = j < end;
-                const uint32_t o = valid ? P.ec_o[j] : 0;
-                const uint32_t col = valid ? P.ec_col[j] : 0;
                 const int cntL = min((int)(end - b), LPV);
-                for (int i = 0; i < P.nEC; ++i) {
-                    const uint32_t row = ((uint32_t)i * P.ndirs + o) * (uint32_t)T.nSp;
-                    for (int t0 = 0; t0 < cntL; t0 += B) {
-                        const int cnt = min(B, cntL - t0);
-                        auto rowf = [&](int q) { return __shfl_sync(G.mask, row, t0 + q, LPV); };
-                        const float tot = batch_dots_mix<LPV, NP, LT>(G, T.ec, rowf, cnt, z);
-                        const uint32_t cq = __shfl_sync(G.mask, col, t0 + q_me, LPV);
-                        if (writer && q_me < cnt) xout[P.ec_base + (size_t)i * P.nE + cq] = (double)tot;
+                bool head, tail;
+                run_flags<LPV>(G, valid, o, cntL, head, tail);
+                const unsigned tails = group_bits<LPV>(__ballot_sync(G.mask, tail));
+                const int K = __popc(tails);
+                const unsigned at_or_after = tails & (0xffffffffu << G.sub);
+                const int my_tail = __ffs(at_or_after) - 1;
+                const int my_item = my_tail >= 0 ? __popc(tails & ((1u << my_tail) - 1u)) : -1;
+#pragma unroll 1
+                for (int i = 0; i < cm.nrf; ++i) {
+                    const uint32_t row = (uint32_t)i * cm.rf_stride + o * (uint32_t)C.nSp;
+                    unsigned rest = tails;
+#pragma unroll 1
+                    for (int u0 = 0; u0 < K; u0 += B) {
+                        const int cnt = min(B, K - u0);
+                        // lanes of items u0 .. u0+B-1: the lowest remaining tail bits
+                        int src[B];
+                        unsigned mrem = rest;
+#pragma unroll
+                        for (int q = 0; q < B; ++q) {
+                            src[q] = mrem ? __ffs(mrem) - 1 : 0;
+                            mrem &= mrem - 1;
+                        }
+                        rest = mrem;
+                        auto rowf = [&](int q) { return __shfl_sync(G.mask, row, src[q], LPV); };
+                        const float tot = batch_dots_mix<LPV, NP, LT>(G, cm.lut, rowf, cnt, z);
+                        const int q = my_item - u0;
+                        const bool mine = valid && q >= 0 && q < cnt;
+                        const float t = __shfl_sync(G.mask, tot, mine ? q * SPAN : 0, LPV);
+                        if (mine) {
+                            if (cm.to_scratch) scr[(size_t)i * n + j] = l * t;
+                            else xout[cm.xbase + (size_t)i * cm.xstride + col] = (double)t;
+                        }
                     }
-                }
-            }
-        }
-        if (P.nISO > 0) {
-            const uint32_t beg = P.iso_ptr[v], end = P.iso_ptr[v + 1];
-            if (beg < end) {
-                for (int t0 = 0; t0 < P.nISO; t0 += B) {
-                    const int cnt = min(B, P.nISO - t0);
-                    auto rowf = [&](int q) { return (uint32_t)((t0 + q) * T.nSp); };
-                    const float tot = batch_dots_mix<LPV, NP, float>(G, T.iso, rowf, cnt, z);
-                    if (writer && q_me < cnt)
-                        for (uint32_t e = beg; e < end; ++e)
-                            xout[P.iso_base + (size_t)(t0 + q_me) * P.nISOv + P.iso_col[e]] = (double)tot;
                 }
             }
         }

@@ -7,15 +7,25 @@ namespace {
 using namespace detail;
 using LT = __half;
 
-MixLut<LT> mixlut(const cgb_op *op) {
-    MixLut<LT> T;
-    T.ic = (const LT *)op->lut_r_ic(CGB_ARITH_FP16);
-    T.ec = (const LT *)op->lut_r_ec(CGB_ARITH_FP16);
-    T.iso = op->lutISO_p;
-    T.nSp = op->nSp;
-    T.len16 = op->seg_l16;
-    T.len_inv_scale = op->len16_inv_scale;
-    return T;
+CompsM<LT> comps(const cgb_op *op) {
+    CompsM<LT> C;
+    C.n = 0;
+    C.nSp = op->nSp;
+    const uint32_t ndirs = (uint32_t)op->ndirs, nSp = (uint32_t)op->nSp;
+    const LT *ic = (const LT *)op->lut_r_ic(CGB_ARITH_FP16);
+    const LT *ec = (const LT *)op->lut_r_ec(CGB_ARITH_FP16);
+    const LT *iso = (const LT *)op->lut_r_iso(CGB_ARITH_FP16);
+    const bool l16 = true;
+    if (op->nIC > 0)
+        C.c[C.n++] = CompM<LT>{op->vox_ptr, op->seg_f, op->seg_o, l16 ? nullptr : op->seg_l, l16 ? op->seg_l16 : nullptr,
+                               op->len16_inv_scale, op->eval, ic, 0, op->nF, ndirs * nSp, op->nIC, 1};
+    if (op->nEC > 0 && op->nE > 0)
+        C.c[C.n++] = CompM<LT>{op->ec_ptr, op->ec_col, op->ec_o, nullptr, nullptr, 1.f, nullptr, ec,
+                               (int64_t)op->nF * op->nIC, op->nE, ndirs * nSp, op->nEC, 0};
+    if (op->nISO > 0 && op->nISOv > 0)
+        C.c[C.n++] = CompM<LT>{op->iso_ptr, op->iso_col, nullptr, nullptr, nullptr, 1.f, nullptr, iso,
+                               (int64_t)op->nF * op->nIC + (int64_t)op->nE * op->nEC, op->nISOv, nSp, op->nISO, 0};
+    return C;
 }
 
 struct FwdMix {
@@ -32,7 +42,7 @@ struct FwdMix {
         int g = 0;
         CGB_TRY(grid_for_kernel(kern, 0, op->nsm, op->nV, kBlock / L, &g));
         if (g > reduction_blocks(op)) g = reduction_blocks(op);
-        kern<<<g, kBlock, 0, st>>>(op->dev(), mixlut(op), x, y, ax, yobs, sqw, partials);
+        kern<<<g, kBlock, 0, st>>>(op->nV, op->nS, comps(op), x, y, ax, yobs, sqw, partials);
         CGB_CUDA(cudaGetLastError());
         if (grid_out) *grid_out = g;
         return CGB_OK;
@@ -55,7 +65,7 @@ struct AdjMix {
         int g = 0;
         CGB_TRY(grid_for_kernel(kern, 0, op->nsm, op->nV, kBlock / L, &g));
         if (g > reduction_blocks(op)) g = reduction_blocks(op);
-        kern<<<g, kBlock, 0, st>>>(op->dev(), mixlut(op), yin, in_mode, x, yobs, sqw, ax_a, ax_b, ca, cb,
+        kern<<<g, kBlock, 0, st>>>(op->nV, op->nS, op->n, comps(op), yin, in_mode, x, yobs, sqw, ax_a, ax_b, ca, cb,
                                    op->scratch32, xout, partials);
         CGB_CUDA(cudaGetLastError());
         if (grid_out) *grid_out = g;

@@ -423,12 +423,20 @@ __global__ void __launch_bounds__(kBlock) k_adjoint_p(const OpDev P, const __gri
 #pragma unroll 1
                 for (int i = 0; i < cm.nrf; ++i) {
                     const uint32_t row = (uint32_t)i * cm.rf_stride + o * (uint32_t)C.nSp;
+                    unsigned rest = tails;
 #pragma unroll 1
                     for (int u0 = 0; u0 < K; u0 += B) {
                         const int cnt = min(B, K - u0);
-                        auto rowf = [&](int q) {
-                            return __shfl_sync(G.mask, row, (int)__fns(tails, 0, u0 + q + 1), LPV);
-                        };
+                        // lanes of items u0 .. u0+B-1: the lowest remaining tail bits
+                        int src[B];
+                        unsigned mrem = rest;
+#pragma unroll
+                        for (int q = 0; q < B; ++q) {
+                            src[q] = mrem ? __ffs(mrem) - 1 : 0;
+                            mrem &= mrem - 1;
+                        }
+                        rest = mrem;
+                        auto rowf = [&](int q) { return __shfl_sync(G.mask, row, src[q], LPV); };
                         const double tot = batch_dots_p<LPV, NP>(G, cm.lut, rowf, cnt, zh, zl);
                         const int q = my_item - u0;
                         const bool mine = valid && q >= 0 && q < cnt;

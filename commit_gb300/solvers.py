@@ -204,7 +204,7 @@ def evaluate_model(y, A, x, regularisation=None):
 
 
 def solve(y, A, At, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, verbose=True, x0=None, regularisation=None,
-          confidence_array=None, arith=None, momentum_reuse=True):
+          confidence_array=None, arith=None, momentum_reuse=True, x_ref=None):
     """solvers.py:218-241: regularised least squares by FISTA, on the GPU."""
     if regularisation is None:
         spec = _no_reg_spec(A.shape[1])
@@ -216,7 +216,7 @@ def solve(y, A, At, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, verbose=True, x0=No
     if confidence_array is not None:
         sqrt_W = np.sqrt(np.asarray(confidence_array)) if not isinstance(confidence_array, torch.Tensor) \
             else torch.sqrt(confidence_array)
-    return _fista(y, A, spec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, arith, momentum_reuse)
+    return _fista(y, A, spec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, arith, momentum_reuse, x_ref)
 
 
 def fista(y, A, At, omega, prox, sqrt_W=None, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, verbose=False, x0=None,
@@ -240,7 +240,9 @@ def _is_identity(prox, n) -> bool:
     return out is not None and np.array_equal(np.asarray(out), probe)
 
 
-def _fista(y, A, spec: RegSpec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, arith, momentum_reuse):
+def _fista(y, A, spec: RegSpec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, arith, momentum_reuse, x_ref=None):
+    """With x_ref given, details['trace'] holds, per accepted iteration, the seconds since
+    the solve started and |x_k - x_ref| / |x_ref|."""
     if not isinstance(A, LinearOperator):
         raise TypeError('A must be a commit_gb300.operator.LinearOperator')
     if A.adjoint:
@@ -265,6 +267,14 @@ def _fista(y, A, spec: RegSpec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, a
     reg, keep = spec.cstruct(dev)
     prm = _lib.CgbFistaParams(float(tol_fun), float(tol_x), int(max_iter), int(verbose) if verbose is not True else 1,
                               _lib.ARITH[arith or A.arith], int(bool(momentum_reuse)))
+    trace = None
+    if x_ref is not None:
+        xr = torch.as_tensor(np.asarray(x_ref, dtype=np.float64) if not isinstance(x_ref, torch.Tensor) else x_ref,
+                             dtype=torch.float64).to(dev).contiguous()
+        trace = np.full((int(max_iter), 2), np.nan)
+        prm.x_ref = xr.data_ptr()
+        prm.trace = trace.ctypes.data
+        prm.trace_len = int(max_iter)
     res = _lib.CgbFistaResult()
     st = torch.cuda.current_stream(dev).cuda_stream
     check(lib().cgb_fista_run(A.handle, ctypes.c_void_p(yd.data_ptr()),
@@ -275,6 +285,8 @@ def _fista(y, A, spec: RegSpec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, a
     details = {'residual': res.residual, 'regterm': res.regterm, 'cost_function': res.cost_function,
                'abs_cost': res.abs_cost, 'rel_cost': res.rel_cost, 'abs_x': res.abs_x, 'rel_x': res.rel_x,
                'iterations': int(res.iterations), 'stopping_criterion': _lib.CRITERIA[res.stopping_criterion]}
+    if trace is not None:
+        details['trace'] = trace[:int(res.iterations)]
     details['backtracks'] = int(res.backtracks)
     details['operator_calls'] = int(res.operator_calls)
     x = xd.cpu().numpy() if host else xd
@@ -283,7 +295,7 @@ def _fista(y, A, spec: RegSpec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, a
 
 def solve_mixed(y, A, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, verbose=0, x0=None, regularisation=None,
                 confidence_array=None, arith='bf16', refine_arith=None, refine_max_iter=None,
-                refine_tol_fun=None, refine_tol_x=None):
+                refine_tol_fun=None, refine_tol_x=None, x_ref=None):
     """Reduced-precision FISTA followed by an FP64 refinement solve.
 
     Phase 1 runs FISTA with the operator in ``arith`` ('bf16', 'fp16' or 'f32': LUT in
@@ -293,13 +305,20 @@ def solve_mixed(y, A, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, verbose=0, x0=Non
     the reduced-precision operator.  Returns (x, details) with details['mixed'] and
     details['refine'] holding each phase's opt_details.
     """
+    import time
+    t0 = time.perf_counter()
     x1, d1 = solve(y, A, A.T, tol_fun=tol_fun, tol_x=tol_x, max_iter=max_iter, verbose=verbose, x0=x0,
-                   regularisation=regularisation, confidence_array=confidence_array, arith=arith)
+                   regularisation=regularisation, confidence_array=confidence_array, arith=arith, x_ref=x_ref)
+    t1 = time.perf_counter() - t0
     x2, d2 = solve(y, A, A.T, tol_fun=refine_tol_fun if refine_tol_fun is not None else tol_fun,
                    tol_x=refine_tol_x if refine_tol_x is not None else tol_x,
                    max_iter=refine_max_iter if refine_max_iter is not None else max_iter, verbose=verbose, x0=x1,
-                   regularisation=regularisation, confidence_array=confidence_array, arith=refine_arith)
+                   regularisation=regularisation, confidence_array=confidence_array, arith=refine_arith, x_ref=x_ref)
     det = dict(d2)
+    if x_ref is not None:
+        tr2 = d2['trace'].copy()
+        tr2[:, 0] += t1
+        det['trace'] = np.concatenate([d1['trace'], tr2])
     det['mixed'] = d1
     det['refine'] = d2
     det['iterations'] = d1['iterations'] + d2['iterations']

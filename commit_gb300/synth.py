@@ -326,9 +326,12 @@ def make_dictionary(spec: ProblemSpec, device: str = 'cpu') -> tuple[dict, dict]
     EC = {'vox': ecv, 'dir': eco, 'n': int(ecv.size)}
     ISO = {'vox': np.arange(nV, dtype=np.uint32), 'n': nV}
 
+    tdi = np.zeros(int(np.prod(spec.dim)), dtype=np.uint8)
+    tdi[tdi_lin] = 1
     DICTIONARY = {'IC': IC, 'EC': EC, 'ISO': ISO,
                   'TRK': {'kept': kept, 'norm': norm},
-                  'ndirs': spec.ndirs, 'nV': nV, 'dim': spec.dim}
+                  'ndirs': spec.ndirs, 'nV': nV, 'dim': spec.dim,
+                  'MASK': tdi.reshape(spec.dim, order='F')}
     return DICTIONARY, KERNELS
 
 

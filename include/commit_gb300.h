@@ -188,6 +188,12 @@ typedef struct {
     int verbose;          /* 0: quiet                                                    */
     int arith;            /* CGB_ARITH_F64 / CGB_ARITH_FF                                 */
     int momentum_reuse;   /* 1: A*xhat from A*x and A*prev_x (exact in exact arithmetic) */
+    /* optional convergence trace: with x_ref (DEVICE, ncols) and trace (HOST, 2*trace_len
+       doubles) set, accepted iteration k (k < trace_len) records trace[2k] = seconds since
+       the call started and trace[2k+1] = |x_k - x_ref| / |x_ref| */
+    const double *x_ref;
+    double *trace;
+    int trace_len;
 } cgb_fista_params;
 
 typedef struct {

@@ -52,8 +52,10 @@ def test_gradients_against_central_differences():
         xp, xm = x.copy(), x.copy()
         xp[k] += H
         xm[k] -= H
-        fd = (_loss_fp64(P, xp, y) - _loss_fp64(P, xm, y)) / (2 * H)
-        assert abs(gx[k] - fd) <= 1e-5 * max(1.0, abs(fd)), (k, gx[k], fd)
+        lp, lm = _loss_fp64(P, xp, y), _loss_fp64(P, xm, y)
+        fd = (lp - lm) / (2 * H)
+        fd_err = 8 * np.finfo(float).eps * max(lp, lm) / (2 * H)
+        assert abs(gx[k] - fd) <= 4 * fd_err + 1e-7 * abs(fd), (k, gx[k], fd, fd_err)
     # dLoss/dLUT: y is linear in a LUT entry, so loss(theta +- h) follows from r and the
     # entry's column of coefficients; evaluate it in FP64 and difference centrally
     r = P.dot(x) - y
@@ -84,7 +86,9 @@ def test_gradients_against_central_differences():
             lp = 0.5 * float(np.dot(r + H * d, r + H * d))
             lm = 0.5 * float(np.dot(r - H * d, r - H * d))
             fd = (lp - lm) / (2 * H)
-            assert abs(g_kernel - fd) <= 1e-6 * max(1.0, abs(fd)), (which, g_kernel, fd)
+            # the difference quotient itself is accurate to about eps * loss / h
+            fd_err = 8 * np.finfo(float).eps * max(lp, lm) / (2 * H)
+            assert abs(g_kernel - fd) <= 4 * fd_err + 1e-7 * abs(fd), (which, g_kernel, fd, fd_err)
 
 
 def test_adjoint_dot_test_against_oracle():
