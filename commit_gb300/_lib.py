@@ -79,6 +79,10 @@ def lib() -> ctypes.CDLL:
                                          P, P, P, P, P, P, P, P, P, P, P, c_i32, c_i32, c_i32, P, P, P]
     L.cgb_fista_run.argtypes = [P, P, P, ctypes.POINTER(CgbReg), ctypes.POINTER(CgbFistaParams), P,
                                 ctypes.POINTER(CgbFistaResult), P]
+    L.cgb_fista_batch_run.argtypes = [P, P, P, ctypes.POINTER(CgbReg), c_i32, ctypes.POINTER(CgbFistaParams),
+                                      ctypes.POINTER(c_vp), ctypes.POINTER(CgbFistaResult), P]
+    L.cgb_op_batch_width.argtypes = [P, c_i32, ctypes.POINTER(c_i32)]
+    L.cgb_op_apply_batch.argtypes = [P, c_i32, c_i32, ctypes.POINTER(c_vp), ctypes.POINTER(c_vp), P]
     L.cgb_prox_non_negativity.argtypes = [P, c_i64, c_i64, P]
     L.cgb_prox_soft_thresholding.argtypes = [P, c_f64, c_i64, c_i64, P]
     L.cgb_prox_w_soft_thresholding.argtypes = [P, P, c_f64, c_i64, c_i64, P]

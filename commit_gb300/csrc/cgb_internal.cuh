@@ -58,6 +58,21 @@ struct OpDev {
     const uint32_t *iso_col;        // [nISOv]
 };
 
+// vectors of a multi-right-hand-side pass (batch.cuh)
+constexpr int kMaxRhs = 16;
+struct RhsPtrs {
+    const double *x[kMaxRhs];       // column vectors (forward input / gradient point)
+    float *y[kMaxRhs];              // row outputs (forward), may be null
+    float *ax[kMaxRhs];             // A x outputs (momentum reuse), may be null
+    const float *yin[kMaxRhs];      // adjoint inputs (in_mode 0)
+    const float *axa[kMaxRhs];      // momentum reuse inputs (in_mode 2)
+    const float *axb[kMaxRhs];
+    float ca[kMaxRhs], cb[kMaxRhs];
+    double *xout[kMaxRhs];          // adjoint outputs (EC / ISO columns; IC via scratch)
+    float *scr[kMaxRhs];            // per-segment terms
+    int active[kMaxRhs];            // 0: skip this vector (outputs untouched)
+};
+
 }  // namespace cgb
 
 struct cgb_op {
@@ -77,6 +92,7 @@ struct cgb_op {
     float len16_inv_scale;          // 2^-k
     double *d_x64;                  // [ncols] staging for FP32 applies
     void *gstate;                   // LUT-gradient streams (lutgrad.cu), built on first use
+    int batch_rhs;                  // vectors per multi-right-hand-side pass (0: not tuned)
     uint32_t *vox_ptr, *seg_f, *eval, *fib_ptr, *fib_perm, *ec_ptr, *ec_col, *iso_ptr, *iso_col;
     uint16_t *seg_o, *ec_o;
     float *seg_l;
@@ -119,5 +135,11 @@ int launch_gradient_mix(cgb_op *op, const double *x, const float *y, const float
                         cudaStream_t st, int arith, int *grid);
 int launch_adjoint_mix(cgb_op *op, const float *yin, double *xout, cudaStream_t st, int arith);
 int convert_f64_to_f32(const double *in, float *out, int64_t n, cudaStream_t st);
+// multi-right-hand-side BF16 path (batch_r*.cu, mixed.cu)
+int launch_forward_R(cgb_op *op, int R, const RhsPtrs &V, const float *yobs, const float *sqw, double *partials,
+                     cudaStream_t st, int *grid);
+int launch_adjoint_R(cgb_op *op, int R, const RhsPtrs &V, int in_mode, const float *yobs, const float *sqw,
+                     double *partials, cudaStream_t st, int *grid);
+int fibre_sum32_from(cgb_op *op, const float *scr, double *xout, cudaStream_t st);
 int convert_f32_to_f64(const float *in, double *out, int64_t n, cudaStream_t st);
 }  // namespace cgb

@@ -14,6 +14,8 @@
 // decisions exactly as the reference does.
 #include <math.h>
 
+#include <string.h>
+
 #include <chrono>
 #include <vector>
 
@@ -277,15 +279,19 @@ struct Solver {
     int calls = 0;
 
     bool mixed = false;
+    bool batch_member = false;  // one problem of a batch: row buffers belong to the batch
+    double *dsc = nullptr;      // this problem's 16 device scalars
 
     int init() {
         const int64_t nc = op->ncols, nr = op->nrows;
         const int rb = reduction_blocks(op);
         mixed = prm->arith == CGB_ARITH_BF16 || prm->arith == CGB_ARITH_FP16 || prm->arith == CGB_ARITH_F32;
+        if (!dsc) dsc = op->dscal;
         CGB_TRY(ws_alloc(&ws.xhat, nc));
         CGB_TRY(ws_alloc(&ws.prev, nc));
         CGB_TRY(ws_alloc(&ws.grad, nc));
-        if (mixed) {
+        if (batch_member) {
+        } else if (mixed) {
             CGB_TRY(ensure_reduced(op, prm->arith));
             CGB_CUDA(cudaMalloc((void **)&ws.y32, (nr > 0 ? nr : 1) * sizeof(float)));
             CGB_TRY(convert_f64_to_f32(y, ws.y32, nr, st));
@@ -396,7 +402,7 @@ struct Solver {
         const int gb = elem_grid(op, nc);
         k_stats<<<gb, kBlock, 0, st>>>(x, xh, g, p, nc, terms, xh ? prm->x_ref : nullptr, ws.pstats);
         CGB_CUDA(cudaGetLastError());
-        CGB_TRY(finalize(ws.pstats, gb, kStatSlots, op->dscal + 1, st));
+        CGB_TRY(finalize(ws.pstats, gb, kStatSlots, dsc + 1, st));
         if (group_in_omega) {
             int64_t blocks = (reg->ngroups * 32 + kBlock - 1) / kBlock;
             if (blocks > op->nsm * 4) blocks = op->nsm * 4;
@@ -404,9 +410,9 @@ struct Solver {
             k_group_norms<<<(int)blocks, kBlock, 0, st>>>(x, op->ncols, reg->group_idx, reg->group_ptr, reg->group_w,
                                                          reg->ngroups, ws.pgrp);
             CGB_CUDA(cudaGetLastError());
-            CGB_TRY(finalize(ws.pgrp, (int)blocks, 1, op->dscal + 11, st));
+            CGB_TRY(finalize(ws.pgrp, (int)blocks, 1, dsc + 11, st));
         } else {
-            CGB_CUDA(cudaMemsetAsync(op->dscal + 11, 0, sizeof(double), st));
+            CGB_CUDA(cudaMemsetAsync(dsc + 11, 0, sizeof(double), st));
         }
         return CGB_OK;
     }
@@ -595,6 +601,367 @@ struct Solver {
     }
 };
 
+// out[off[j]] = sum over blocks of partials[b*kRedSlots + j] for the j with off[j] >= 0
+struct SlotMap {
+    int off[kMaxRhs];
+};
+__global__ void k_finalize_scatter(const double *__restrict__ partials, int nblocks, SlotMap M, double *__restrict__ out) {
+    double v[1] = {0.0};
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) v[0] += partials[(size_t)b * kRedSlots + blockIdx.x];
+    double tmp[1];
+    block_sum_store_n<1>(v, tmp);
+    if (threadIdx.x == 0 && M.off[blockIdx.x] >= 0) out[M.off[blockIdx.x]] = tmp[0];
+}
+
+// A regularisation path (or any set of problems sharing A, y and sqrt(W)) solved together:
+// every problem follows commit/solvers.py:244-391 exactly as Solver does (its own step,
+// momentum, backtracking and stopping tests), but the operator passes of all problems that
+// need one at the same point run as multi-right-hand-side passes (BF16 LUT, FP32 rows,
+// R = 2 or 4 vectors per pass), which load each segment's LUT row once for R vectors.
+// A problem that has stopped leaves the passes; x of each problem is its own device array.
+struct BatchSolver {
+    cgb_op *op;
+    const double *y, *sqw;
+    const cgb_reg *regs;
+    int P;
+    const cgb_fista_params *prm;
+    cudaStream_t st;
+    std::vector<Solver> S;
+    float *y32 = nullptr, *sqw32 = nullptr;
+    float *scr[4] = {nullptr, nullptr, nullptr, nullptr};
+    std::vector<float *> ax32;  // 2 per problem with momentum reuse
+    double *bscal = nullptr, *hb = nullptr, *partials = nullptr;
+    int R = 4;
+    int calls = 0;
+
+    ~BatchSolver() {
+        if (y32) cudaFree(y32);
+        if (sqw32) cudaFree(sqw32);
+        for (float *p : scr)
+            if (p) cudaFree(p);
+        for (float *p : ax32)
+            if (p) cudaFree(p);
+        if (bscal) cudaFree(bscal);
+        if (partials) cudaFree(partials);
+        if (hb) cudaFreeHost(hb);
+    }
+
+    int init() {
+        const int64_t nr = op->nrows;
+        CGB_TRY(ensure_reduced(op, CGB_ARITH_BF16));
+        CGB_CUDA(cudaMalloc((void **)&bscal, (size_t)P * 16 * sizeof(double)));
+        CGB_CUDA(cudaMemsetAsync(bscal, 0, (size_t)P * 16 * sizeof(double), st));
+        CGB_CUDA(cudaMallocHost((void **)&hb, (size_t)P * 16 * sizeof(double)));
+        CGB_CUDA(cudaMalloc((void **)&partials, (size_t)reduction_blocks(op) * kRedSlots * sizeof(double)));
+        CGB_CUDA(cudaMalloc((void **)&y32, (nr > 0 ? nr : 1) * sizeof(float)));
+        CGB_TRY(convert_f64_to_f32(y, y32, nr, st));
+        if (sqw) {
+            CGB_CUDA(cudaMalloc((void **)&sqw32, (nr > 0 ? nr : 1) * sizeof(float)));
+            CGB_TRY(convert_f64_to_f32(sqw, sqw32, nr, st));
+        }
+        const size_t nscr = (size_t)(op->n > 0 ? op->n : 1) * (op->nIC > 0 ? op->nIC : 1);
+        for (int r = 0; r < 4; ++r) CGB_CUDA(cudaMalloc((void **)&scr[r], nscr * sizeof(float)));
+        if (prm->momentum_reuse) {
+            ax32.assign((size_t)2 * P, nullptr);
+            for (auto &p : ax32) CGB_CUDA(cudaMalloc((void **)&p, (nr > 0 ? nr : 1) * sizeof(float)));
+        }
+        S.resize(P);
+        for (int p = 0; p < P; ++p) {
+            Solver &s = S[p];
+            s.op = op;
+            s.y = y;
+            s.sqw = sqw;
+            s.reg = regs + p;
+            s.prm = prm;
+            s.st = st;
+            s.batch_member = true;
+            s.dsc = bscal + (size_t)16 * p;
+            CGB_TRY(s.init());
+        }
+        R = op->batch_rhs == 2 ? 2 : 4;
+        return CGB_OK;
+    }
+
+    // chunks of the problem list J: full chunks of R, a remainder of 3 as R = 4 with one idle
+    // slot, of 2 as R = 2, of 1 through the single-vector kernels
+    template <class F>
+    int chunks(const std::vector<int> &J, F &&f) {
+        size_t i = 0;
+        while (i < J.size()) {
+            const size_t left = J.size() - i;
+            int take, rr;
+            if (left >= (size_t)R) take = rr = R;
+            else if (left == 3) take = 3, rr = 4;
+            else if (left == 2) take = rr = 2;
+            else take = rr = 1;
+            CGB_TRY(f(&J[i], take, rr));
+            i += take;
+        }
+        return CGB_OK;
+    }
+
+    // |sqw*(A x_p - yobs)|^2 -> slot of each problem in J (yobs null: |sqw*A x_p|^2);
+    // with ax, A x_p is also kept in ax32[2p + slot_ax[p]]
+    int forward(const std::vector<int> &J, double *const *xs, const float *yobs, int slot, const int *slot_ax) {
+        return chunks(J, [&](const int *pp, int take, int rr) -> int {
+            int g = 0;
+            SlotMap M;
+            for (int r = 0; r < kMaxRhs; ++r) M.off[r] = -1;
+            if (rr == 1) {
+                const int p = pp[0];
+                float *ax = slot_ax ? ax32[2 * p + slot_ax[p]] : nullptr;
+                CGB_TRY(launch_resnorm_mix(op, xs[p], yobs, sqw32, partials, ax, nullptr, st, CGB_ARITH_BF16, &g));
+                M.off[0] = 16 * p + slot;
+            } else {
+                RhsPtrs V;
+                memset(&V, 0, sizeof(V));
+                for (int r = 0; r < rr; ++r) {
+                    const int p = pp[r < take ? r : 0];
+                    V.x[r] = xs[p];
+                    V.active[r] = r < take;
+                    if (r < take) {
+                        if (slot_ax) V.ax[r] = ax32[2 * p + slot_ax[p]];
+                        M.off[r] = 16 * p + slot;
+                    }
+                }
+                CGB_TRY(launch_forward_R(op, rr, V, yobs, sqw32, partials, st, &g));
+            }
+            calls += take;
+            if (g > 0) {
+                k_finalize_scatter<<<rr, kBlock, 0, st>>>(partials, g, M, bscal);
+                CGB_CUDA(cudaGetLastError());
+            } else {
+                for (int r = 0; r < take; ++r) CGB_CUDA(cudaMemsetAsync(bscal + M.off[r], 0, sizeof(double), st));
+            }
+            return CGB_OK;
+        });
+    }
+
+    // grad_p = A'(W(A xhat_p - y)), |r_p|^2 -> slot 12; with reuse, A xhat_p = ca*ax[sa] + cb*ax[sb]
+    int gradient(const std::vector<int> &J, bool reuse, const int *sa, const int *sb, const double *ca,
+                 const double *cb) {
+        return chunks(J, [&](const int *pp, int take, int rr) -> int {
+            int g = 0;
+            SlotMap M;
+            for (int r = 0; r < kMaxRhs; ++r) M.off[r] = -1;
+            if (op->nV == 0) {
+                for (int r = 0; r < take; ++r) {
+                    const int p = pp[r];
+                    if (op->ncols > 0) CGB_CUDA(cudaMemsetAsync(S[p].ws.grad, 0, op->ncols * sizeof(double), st));
+                    CGB_CUDA(cudaMemsetAsync(bscal + 16 * p + 12, 0, sizeof(double), st));
+                }
+                return CGB_OK;
+            }
+            if (rr == 1) {
+                const int p = pp[0];
+                CGB_TRY(launch_gradient_mix(op, S[p].ws.xhat, y32, sqw32, S[p].ws.grad, partials,
+                                            reuse ? ax32[2 * p + sa[p]] : nullptr, reuse ? ax32[2 * p + sb[p]] : nullptr,
+                                            reuse ? (float)ca[p] : 0.f, reuse ? (float)cb[p] : 0.f, st, CGB_ARITH_BF16,
+                                            &g));
+                M.off[0] = 16 * p + 12;
+            } else {
+                RhsPtrs V;
+                memset(&V, 0, sizeof(V));
+                for (int r = 0; r < rr; ++r) {
+                    const int p = pp[r < take ? r : 0];
+                    V.x[r] = S[p].ws.xhat;
+                    V.active[r] = r < take;
+                    V.scr[r] = scr[r];
+                    V.xout[r] = S[p].ws.grad;
+                    if (reuse) {
+                        V.axa[r] = ax32[2 * p + sa[p]];
+                        V.axb[r] = ax32[2 * p + sb[p]];
+                        V.ca[r] = (float)ca[p];
+                        V.cb[r] = (float)cb[p];
+                    }
+                    if (r < take) M.off[r] = 16 * p + 12;
+                }
+                CGB_TRY(launch_adjoint_R(op, rr, V, reuse ? 2 : 1, y32, sqw32, partials, st, &g));
+                for (int r = 0; r < take; ++r) CGB_TRY(fibre_sum32_from(op, scr[r], S[pp[r]].ws.grad, st));
+            }
+            calls += take * (reuse ? 1 : 2);
+            if (g > 0) {
+                k_finalize_scatter<<<rr, kBlock, 0, st>>>(partials, g, M, bscal);
+                CGB_CUDA(cudaGetLastError());
+            }
+            return CGB_OK;
+        });
+    }
+
+    int fetch() {
+        CGB_CUDA(cudaMemcpyAsync(hb, bscal, (size_t)P * 16 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CGB_CUDA(cudaStreamSynchronize(st));
+        return CGB_OK;
+    }
+
+    // multi-right-hand-side width: time one gradient pass of 4 problems as one R = 4 pass
+    // and as two R = 2 passes, keep the faster (stored on the operator)
+    int tune(double *const *xs) {
+        if (op->batch_rhs != 0 || P < 4 || op->nV == 0) return CGB_OK;
+        cudaEvent_t e[3];
+        for (auto &ev : e) CGB_CUDA(cudaEventCreate(&ev));
+        std::vector<int> J = {0, 1, 2, 3};
+        float best[2] = {0.f, 0.f};
+        const int widths[2] = {4, 2};
+        for (int rep = 0; rep < 2; ++rep) {
+            for (int k = 0; k < 2; ++k) {
+                R = widths[k];
+                CGB_CUDA(cudaEventRecord(e[0], st));
+                CGB_TRY(gradient(J, false, nullptr, nullptr, nullptr, nullptr));
+                CGB_CUDA(cudaEventRecord(e[1], st));
+                CGB_CUDA(cudaEventSynchronize(e[1]));
+                float ms = 0.f;
+                CGB_CUDA(cudaEventElapsedTime(&ms, e[0], e[1]));
+                if (rep == 1) best[k] = ms;  // first round warms both up
+            }
+        }
+        for (auto &ev : e) cudaEventDestroy(ev);
+        op->batch_rhs = best[1] < best[0] ? 2 : 4;
+        R = op->batch_rhs;
+        (void)xs;
+        return CGB_OK;
+    }
+
+    int run(double *const *xs, cgb_fista_result *res) {
+        const int64_t nc = op->ncols;
+        const double eps = 2.220446049250313e-16;
+        const double beta = 0.9;
+        std::vector<int> all(P);
+        for (int p = 0; p < P; ++p) all[p] = p;
+        for (int p = 0; p < P; ++p)
+            CGB_CUDA(cudaMemcpyAsync(S[p].ws.xhat, xs[p], nc * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        CGB_TRY(tune(xs));
+        // initialisation (solvers.py:260-286), all problems at once
+        CGB_TRY(gradient(all, false, nullptr, nullptr, nullptr, nullptr));
+        std::vector<double *> gp(P);
+        for (int p = 0; p < P; ++p) {
+            Solver &s = S[p];
+            CGB_TRY(s.prox(s.ws.xhat, s.ws.xhat, nullptr, 0.0, 1.0));
+            CGB_TRY(s.stats(s.ws.xhat, nullptr, nullptr, nullptr));
+            k_dot<<<elem_grid(op, nc), kBlock, 0, st>>>(s.ws.grad, s.ws.grad, nc, s.ws.pstats);
+            CGB_CUDA(cudaGetLastError());
+            CGB_TRY(finalize(s.ws.pstats, elem_grid(op, nc), 1, s.dsc + 13, st));
+            gp[p] = s.ws.grad;
+        }
+        CGB_TRY(forward(all, gp.data(), nullptr, 14, nullptr));
+        CGB_TRY(fetch());
+        std::vector<double> step(P), told(P, 1.0), prev_obj(P), qfval(P), res_norm(P), reg_x(P), curr(P, 0.0),
+            abs_obj(P, 0.0), rel_obj(P, 0.0), abs_x(P, 0.0), rel_x(P, 0.0), cc(P, 0.0), ca(P), cb(P);
+        std::vector<int> crit(P, 4), iters(P, 1), bts(P, 0), cur(P, 0), sa(P), sb(P);
+        for (int p = 0; p < P; ++p) {
+            const double *h = hb + 16 * p;
+            res_norm[p] = sqrt(h[12]);
+            prev_obj[p] = 0.5 * res_norm[p] * res_norm[p] + S[p].omega_from(h);
+            qfval[p] = prev_obj[p];
+            const double Ln = sqrt(h[14]) / sqrt(h[13]);
+            step[p] = 1.9 / (Ln * Ln);
+            CGB_CUDA(cudaMemcpyAsync(S[p].ws.prev, S[p].ws.xhat, nc * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        }
+        const bool reuse_on = prm->momentum_reuse != 0;
+        int have_prev_ax = 0;
+        std::vector<int> J = all;
+        int it = 1;
+        while (!J.empty()) {
+            auto eval = [&](const std::vector<int> &K) -> int {
+                for (int p : K) {
+                    Solver &s = S[p];
+                    CGB_TRY(s.prox(xs[p], s.ws.xhat, s.ws.grad, step[p], step[p]));
+                    CGB_TRY(s.stats(xs[p], s.ws.xhat, s.ws.grad, s.ws.prev));
+                }
+                CGB_TRY(forward(K, xs, y32, 0, reuse_on ? cur.data() : nullptr));
+                return fetch();
+            };
+            auto judge = [&](int p, double &q) {
+                const double *h = hb + 16 * p;
+                reg_x[p] = S[p].omega_from(h);
+                q = qfval[p] + h[1] + 0.5 / step[p] * (sqrt(h[2]) * sqrt(h[2])) + reg_x[p];
+                res_norm[p] = sqrt(h[0]);
+                curr[p] = 0.5 * res_norm[p] * res_norm[p] + reg_x[p];
+            };
+            CGB_TRY(eval(J));
+            std::vector<int> B;
+            for (int p : J) {
+                const double *h = hb + 16 * p;
+                qfval[p] = it == 1 ? prev_obj[p] : 0.5 * sqrt(h[12]) * sqrt(h[12]);
+                double q;
+                judge(p, q);
+                if (curr[p] > q) B.push_back(p);
+            }
+            while (!B.empty()) {
+                for (int p : B) {
+                    step[p] *= beta;
+                    bts[p]++;
+                }
+                CGB_TRY(eval(B));
+                std::vector<int> B2;
+                for (int p : B) {
+                    double q;
+                    judge(p, q);
+                    if (curr[p] > q) B2.push_back(p);
+                }
+                B.swap(B2);
+            }
+            std::vector<int> next;
+            for (int p : J) {
+                const double *h = hb + 16 * p;
+                abs_obj[p] = fabs(curr[p] - prev_obj[p]);
+                rel_obj[p] = abs_obj[p] / curr[p];
+                abs_x[p] = sqrt(h[3]);
+                rel_x[p] = abs_x[p] / (sqrt(h[4]) + eps);
+                iters[p] = it;
+                int c = -1;
+                if (abs_obj[p] < eps) c = 0;
+                else if (rel_obj[p] < prm->tol_fun) c = 1;
+                else if (abs_x[p] < eps) c = 2;
+                else if (rel_x[p] < prm->tol_x) c = 3;
+                else if (it >= prm->max_iter) c = 4;
+                if (c >= 0) crit[p] = c;
+                else next.push_back(p);
+            }
+            if (next.empty()) break;
+            // FISTA update (solvers.py:359-368) for the problems that go on
+            for (int p : next) {
+                const double t = 0.5 * (1.0 + sqrt(1.0 + 4.0 * told[p] * told[p]));
+                cc[p] = (told[p] - 1.0) / t;
+                told[p] = t;
+                Solver &s = S[p];
+                k_momentum<<<elem_grid(op, nc), kBlock, 0, st>>>(s.ws.xhat, xs[p], s.ws.prev, cc[p], nc);
+                CGB_CUDA(cudaGetLastError());
+                sa[p] = cur[p];
+                sb[p] = have_prev_ax ? 1 - cur[p] : cur[p];
+                ca[p] = 1.0 + cc[p];
+                cb[p] = -cc[p];
+                prev_obj[p] = curr[p];
+            }
+            // every problem starts with c = 0, so the reuse condition is the same for all
+            CGB_TRY(gradient(next, reuse_on, sa.data(), sb.data(), ca.data(), cb.data()));
+            if (reuse_on) {
+                for (int p : next) cur[p] = 1 - cur[p];
+                have_prev_ax = 1;
+            }
+            J.swap(next);
+            it += 1;
+        }
+        for (int p = 0; p < P; ++p) {
+            cgb_fista_result &r = res[p];
+            r.residual = 0.5 * res_norm[p] * res_norm[p];
+            r.regterm = reg_x[p];
+            r.cost_function = curr[p];
+            r.abs_cost = abs_obj[p];
+            r.rel_cost = rel_obj[p];
+            r.abs_x = abs_x[p];
+            r.rel_x = rel_x[p];
+            r.iterations = iters[p];
+            r.stopping_criterion = crit[p];
+            r.backtracks = bts[p];
+            r.operator_calls = 0;
+        }
+        if (P > 0) res[0].operator_calls = calls;
+        CGB_CUDA(cudaStreamSynchronize(st));
+        return CGB_OK;
+    }
+};
+
 }  // namespace
 }  // namespace cgb
 
@@ -633,6 +1000,106 @@ int cgb_fista_run(cgb_op *op, const double *y, const double *sqrt_w, const cgb_r
     S.st = (cudaStream_t)stream;
     CGB_TRY(S.init());
     return S.run(x, result);
+}
+
+int cgb_fista_batch_run(cgb_op *op, const double *y, const double *sqrt_w, const cgb_reg *regs, int nprob,
+                        const cgb_fista_params *params, double *const *x, cgb_fista_result *results, void *stream) {
+    if (!op || !y || !regs || !params || !x || !results) return fail(CGB_ERR_INVALID, "null argument");
+    if (nprob < 1) return fail(CGB_ERR_INVALID, "nprob must be >= 1");
+    if (params->arith != CGB_ARITH_BF16) return fail(CGB_ERR_UNSUPPORTED, "batched FISTA runs in BF16-LUT arithmetic");
+    for (int p = 0; p < nprob; ++p) {
+        const cgb_reg *reg = regs + p;
+        if (!x[p]) return fail(CGB_ERR_INVALID, "null x");
+        if (reg->reg_ec > CGB_REG_LASSO || reg->reg_iso > CGB_REG_LASSO)
+            return fail(CGB_ERR_INVALID, "EC/ISO regularisers must be none or lasso");
+        if ((reg->reg_ic == CGB_REG_GROUP_LASSO || reg->reg_ic == CGB_REG_SPARSE_GROUP_LASSO) && reg->ngroups > 0 &&
+            (!reg->level_ptr || reg->nlevels < 1))
+            return fail(CGB_ERR_INVALID, "group regulariser needs a level schedule");
+    }
+    DevGuard g(op->device);
+    BatchSolver B;
+    B.op = op;
+    B.y = y;
+    B.sqw = sqrt_w;
+    B.regs = regs;
+    B.P = nprob;
+    B.prm = params;
+    B.st = (cudaStream_t)stream;
+    CGB_TRY(B.init());
+    return B.run(x, results);
+}
+
+int cgb_op_batch_width(cgb_op *op, int set, int *width) {
+    if (!op) return fail(CGB_ERR_INVALID, "null handle");
+    if (set >= 0) {
+        if (set != 0 && set != 2 && set != 4) return fail(CGB_ERR_INVALID, "width must be 0, 2 or 4");
+        op->batch_rhs = set;
+    }
+    if (width) *width = op->batch_rhs;
+    return CGB_OK;
+}
+
+int cgb_op_apply_batch(cgb_op *op, int adjoint, int nvec, const void *const *in, void *const *out, void *stream) {
+    if (!op || !in || !out) return fail(CGB_ERR_INVALID, "null argument");
+    if (nvec < 1) return fail(CGB_ERR_INVALID, "nvec must be >= 1");
+    for (int r = 0; r < nvec; ++r)
+        if (!in[r] || !out[r]) return fail(CGB_ERR_INVALID, "null vector");
+    DevGuard g(op->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    CGB_TRY(ensure_reduced(op, CGB_ARITH_BF16));
+    if (op->nV == 0) {
+        for (int r = 0; r < nvec; ++r) {
+            if (adjoint && op->ncols > 0) CGB_CUDA(cudaMemsetAsync(out[r], 0, op->ncols * sizeof(double), st));
+            if (!adjoint && op->nrows > 0) CGB_CUDA(cudaMemsetAsync(out[r], 0, op->nrows * sizeof(float), st));
+        }
+        return CGB_OK;
+    }
+    const int W = op->batch_rhs == 2 ? 2 : 4;
+    std::vector<float *> scr;
+    if (adjoint) {
+        const size_t nscr = (size_t)(op->n > 0 ? op->n : 1) * (op->nIC > 0 ? op->nIC : 1);
+        for (int r = 0; r < W; ++r) {
+            float *p = nullptr;
+            const cudaError_t e = cudaMalloc((void **)&p, nscr * sizeof(float));
+            if (e != cudaSuccess) {
+                for (float *q : scr) cudaFree(q);
+                return cuda_fail(e, "cudaMalloc");
+            }
+            scr.push_back(p);
+        }
+    }
+    int rc = CGB_OK;
+    for (int i = 0; i < nvec && rc == CGB_OK;) {
+        const int left = nvec - i;
+        const int take = left >= W ? W : (left == 3 ? 3 : (left >= 2 ? 2 : 1));
+        const int rr = take == 3 ? 4 : (take == 1 ? 2 : take);
+        RhsPtrs V;
+        memset(&V, 0, sizeof(V));
+        for (int r = 0; r < rr; ++r) {
+            const int k = i + (r < take ? r : 0);
+            V.active[r] = r < take;
+            if (adjoint) {
+                V.yin[r] = (const float *)in[k];
+                V.xout[r] = (double *)out[k];
+                V.scr[r] = scr[r];
+            } else {
+                V.x[r] = (const double *)in[k];
+                V.y[r] = (float *)out[k];
+            }
+        }
+        if (adjoint) {
+            rc = launch_adjoint_R(op, rr, V, 0, nullptr, nullptr, nullptr, st, nullptr);
+            for (int r = 0; r < take && rc == CGB_OK; ++r) rc = fibre_sum32_from(op, scr[r], (double *)out[i + r], st);
+        } else {
+            rc = launch_forward_R(op, rr, V, nullptr, nullptr, nullptr, st, nullptr);
+        }
+        i += take;
+    }
+    if (!scr.empty()) {
+        cudaStreamSynchronize(st);
+        for (float *q : scr) cudaFree(q);
+    }
+    return rc;
 }
 
 // ------------------------------------------------------------------ standalone proximal maps

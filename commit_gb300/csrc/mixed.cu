@@ -87,6 +87,42 @@ int fibre_sum32(cgb_op *op, double *xout, cudaStream_t st) {
 
 }  // namespace
 
+int fibre_sum32_from(cgb_op *op, const float *scr, double *xout, cudaStream_t st) {
+    if (op->nIC > 0 && op->nF > 0) {
+        const int64_t total = (int64_t)op->nF * op->nIC;
+        int gb = (int)((total + 255) / 256);
+        if (gb > op->nsm * 16) gb = op->nsm * 16;
+        k_fibre_sum32<<<gb, 256, 0, st>>>(op->dev(), scr, xout);
+        CGB_CUDA(cudaGetLastError());
+    }
+    return CGB_OK;
+}
+
+int forward_R2(cgb_op *, const RhsPtrs &, const float *, const float *, double *, cudaStream_t, int *);
+int forward_R4(cgb_op *, const RhsPtrs &, const float *, const float *, double *, cudaStream_t, int *);
+int adjoint_R2(cgb_op *, const RhsPtrs &, int, const float *, const float *, double *, cudaStream_t, int *);
+int adjoint_R4(cgb_op *, const RhsPtrs &, int, const float *, const float *, double *, cudaStream_t, int *);
+
+int launch_forward_R(cgb_op *op, int R, const RhsPtrs &V, const float *yobs, const float *sqw, double *partials,
+                     cudaStream_t st, int *grid) {
+    CGB_TRY(ensure_reduced(op, CGB_ARITH_BF16));
+    if (grid) *grid = 0;
+    if (op->nV == 0) return CGB_OK;
+    if (R == 2) return forward_R2(op, V, yobs, sqw, partials, st, grid);
+    if (R == 4) return forward_R4(op, V, yobs, sqw, partials, st, grid);
+    return fail(CGB_ERR_UNSUPPORTED, "vectors per pass must be 2 or 4");
+}
+
+int launch_adjoint_R(cgb_op *op, int R, const RhsPtrs &V, int in_mode, const float *yobs, const float *sqw,
+                     double *partials, cudaStream_t st, int *grid) {
+    CGB_TRY(ensure_reduced(op, CGB_ARITH_BF16));
+    if (grid) *grid = 0;
+    if (op->nV == 0) return CGB_OK;
+    if (R == 2) return adjoint_R2(op, V, in_mode, yobs, sqw, partials, st, grid);
+    if (R == 4) return adjoint_R4(op, V, in_mode, yobs, sqw, partials, st, grid);
+    return fail(CGB_ERR_UNSUPPORTED, "vectors per pass must be 2 or 4");
+}
+
 int convert_f64_to_f32(const double *in, float *out, int64_t n, cudaStream_t st) {
     if (n <= 0) return CGB_OK;
     k_f64_to_f32<<<grid_n(n), 256, 0, st>>>(in, out, n);

@@ -176,5 +176,33 @@ class LinearOperator:
                 check(lib().cgb_op_set_arith(self._h.ptr, _lib.ARITH[self.arith]))
         return res
 
+    def batch_width(self, set_to: int | None = None) -> int:
+        """Vectors per multi-right-hand-side pass (0: chosen by timing on the next batched
+        solve); ``set_to`` 0, 2 or 4 stores a value."""
+        w = ctypes.c_int32()
+        check(lib().cgb_op_batch_width(self._h.ptr, -1 if set_to is None else int(set_to), ctypes.byref(w)))
+        return int(w.value)
+
+    def dot_batch(self, vs):
+        """A @ v (or A' @ v) for a list of CUDA vectors in multi-right-hand-side passes
+        (BF16 LUT, FP32 accumulation; 2 or 4 vectors per pass).  Forward: float64 columns
+        in, float32 rows out; adjoint: float32 rows in, float64 columns out."""
+        if not vs:
+            return []
+        din, dout = (torch.float32, torch.float64) if self.adjoint else (torch.float64, torch.float32)
+        ins = []
+        for v in vs:
+            if not (isinstance(v, torch.Tensor) and v.is_cuda and v.dtype == din):
+                raise TypeError(f'dot_batch expects CUDA {din} vectors')
+            if v.numel() != self.shape[1]:
+                raise RuntimeError("A.dot(): dimensions do not match")
+            ins.append(v.contiguous())
+        outs = [torch.empty(self.shape[0], dtype=dout, device=ins[0].device) for _ in ins]
+        pin = (ctypes.c_void_p * len(ins))(*[t.data_ptr() for t in ins])
+        pout = (ctypes.c_void_p * len(ins))(*[t.data_ptr() for t in outs])
+        st = torch.cuda.current_stream(ins[0].device).cuda_stream
+        check(lib().cgb_op_apply_batch(self._h.ptr, self.adjoint, len(ins), pin, pout, ctypes.c_void_p(st)))
+        return outs
+
     def __matmul__(self, v):
         return self.dot(v)

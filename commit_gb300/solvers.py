@@ -323,3 +323,78 @@ def solve_mixed(y, A, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, verbose=0, x0=Non
     det['refine'] = d2
     det['iterations'] = d1['iterations'] + d2['iterations']
     return x2, det
+
+
+def solve_batch(y, A, regularisations, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, x0=None, confidence_array=None,
+                momentum_reuse=True):
+    """Several problems on one operator and one y, e.g. a regularisation path over lambda.
+
+    ``regularisations`` is a list of regularisation dicts (as for ``solve``; None for no
+    regulariser).  Every problem runs the FISTA of commit/solvers.py:244-391 with its own
+    step size, backtracking and stopping test; the operator runs in BF16-LUT arithmetic and
+    the products of all problems at the same stage share multi-right-hand-side passes
+    (``cgb_fista_batch_run``).  Returns a list of (x, opt_details), x on the device of A when
+    y is a CUDA tensor, numpy otherwise.  Polish a solution with ``solve(..., x0=x)`` in FP64
+    where the BF16 operator's bias matters (as ``solve_mixed`` does for one problem)."""
+    if not isinstance(A, LinearOperator):
+        raise TypeError('A must be a commit_gb300.operator.LinearOperator')
+    if A.adjoint:
+        raise ValueError('A must be the forward operator')
+    P = len(regularisations)
+    if P == 0:
+        return []
+    dev = torch.device('cuda', A.device)
+    host = not isinstance(y, torch.Tensor)
+    yd = torch.as_tensor(np.ascontiguousarray(y, dtype=np.float64) if host else y, dtype=torch.float64).to(dev)
+    yd = yd.contiguous()
+    if yd.numel() != A.nROWS:
+        raise RuntimeError("A.dot(): dimensions do not match")
+    sw = None
+    if confidence_array is not None:
+        c = confidence_array
+        sw = torch.sqrt(torch.as_tensor(np.asarray(c, dtype=np.float64) if not isinstance(c, torch.Tensor) else c,
+                                        dtype=torch.float64).to(dev)).contiguous()
+    specs = []
+    for rp in regularisations:
+        if rp is None:
+            specs.append(_no_reg_spec(A.shape[1]))
+        else:
+            sp = rp.get('_spec') if isinstance(rp, dict) else None
+            specs.append(sp if sp is not None else init_regularisation(rp)['_spec'])
+    for sp in specs:
+        if sp.ncols != A.nCOLS:
+            raise ValueError('regularisation sizes do not match the operator')
+    regs = (_lib.CgbReg * P)()
+    keep = []
+    for p, sp in enumerate(specs):
+        r, k = sp.cstruct(dev)
+        regs[p] = r
+        keep.append(k)
+    xs = []
+    for p in range(P):
+        x0p = x0[p] if isinstance(x0, (list, tuple)) else x0
+        if x0p is None:
+            xs.append(torch.zeros(A.nCOLS, dtype=torch.float64, device=dev))
+        else:
+            xs.append(torch.as_tensor(np.asarray(x0p, dtype=np.float64) if not isinstance(x0p, torch.Tensor) else x0p,
+                                      dtype=torch.float64).to(dev).clone().contiguous())
+    ptrs = (ctypes.c_void_p * P)(*[x.data_ptr() for x in xs])
+    prm = _lib.CgbFistaParams(float(tol_fun), float(tol_x), int(max_iter), 0, _lib.ARITH['bf16'],
+                              int(bool(momentum_reuse)))
+    res = (_lib.CgbFistaResult * P)()
+    st = torch.cuda.current_stream(dev).cuda_stream
+    check(lib().cgb_fista_batch_run(A.handle, ctypes.c_void_p(yd.data_ptr()),
+                                    ctypes.c_void_p(sw.data_ptr()) if sw is not None else None, regs, P,
+                                    ctypes.byref(prm), ptrs, res, ctypes.c_void_p(st)))
+    del keep
+    out = []
+    for p in range(P):
+        r = res[p]
+        det = {'residual': r.residual, 'regterm': r.regterm, 'cost_function': r.cost_function,
+               'abs_cost': r.abs_cost, 'rel_cost': r.rel_cost, 'abs_x': r.abs_x, 'rel_x': r.rel_x,
+               'iterations': int(r.iterations), 'stopping_criterion': _lib.CRITERIA[r.stopping_criterion],
+               'backtracks': int(r.backtracks)}
+        if p == 0:
+            det['batch_operator_calls'] = int(r.operator_calls)
+        out.append((xs[p].cpu().numpy() if host else xs[p], det))
+    return out

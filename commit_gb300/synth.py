@@ -156,6 +156,24 @@ SPECS = {
 }
 
 
+# batched regularisation-path workload: 8 tractograms of uneven size on the full-brain grid
+# and acquisition (seeds 10-17), each fitted for 16 lambda values log-spaced 1e-4..1e-1
+# (fractions of lambda_max) with a nonnegative group lasso over 64 random bundles
+BATCH_FIBERS = (50000, 100000, 150000, 200000, 250000, 300000, 350000, 400000)
+BATCH_LAMBDAS = tuple(float(v) for v in np.logspace(-4, -1, 16))
+
+
+def batch_spec(k: int, n_fibers: int | None = None) -> ProblemSpec:
+    """Tractogram k (0-7) of the batched workload."""
+    return scaled_spec('hcp_1m', n_fibers=int(n_fibers or BATCH_FIBERS[k]), seed=10 + k)
+
+
+def bundle_groups(n_fibers: int, n_groups: int = 64, seed: int = 0) -> list:
+    """A random partition of the streamlines into n_groups bundles (lists of IC columns)."""
+    lab = np.random.default_rng(seed).integers(0, n_groups, size=n_fibers)
+    return [np.flatnonzero(lab == g).astype(np.int64) for g in range(n_groups)]
+
+
 def scaled_spec(name: str, **kw) -> ProblemSpec:
     s = SPECS[name]
     d = dict(s.__dict__)

@@ -212,6 +212,35 @@ typedef struct {
 int cgb_fista_run(cgb_op *op, const double *y, const double *sqrt_w, const cgb_reg *reg,
                   const cgb_fista_params *params, double *x, cgb_fista_result *result, void *stream);
 
+/*
+ * Batched FISTA: nprob problems that share the operator, y and sqrt_w and differ in their
+ * regulariser regs[p] (a regularisation path over lambda).  Each problem follows the same
+ * iteration as cgb_fista_run (own step size, momentum, backtracking, stopping test) with the
+ * operator in BF16-LUT arithmetic (params->arith must be CGB_ARITH_BF16); the A / A' passes of
+ * all problems that need one at the same point run as multi-right-hand-side passes that load
+ * each LUT row once for 2 or 4 vectors.  The vectors per pass are chosen on first use by
+ * timing both widths on the operator (kept on the handle).  x[p] (device pointers) hold x0 on
+ * entry and the solutions on return; results[p] per problem (operator_calls: the batch total
+ * in results[0], 0 elsewhere).  The reference has no batched solver: commit/solvers.py:218-243
+ * solves one problem per call.
+ */
+int cgb_fista_batch_run(cgb_op *op, const double *y, const double *sqrt_w, const cgb_reg *regs, int nprob,
+                        const cgb_fista_params *params, double *const *x, cgb_fista_result *results, void *stream);
+
+/*
+ * A or A' of nvec vectors in one multi-right-hand-side pass per 2 or 4 vectors (BF16 LUT,
+ * FP32 accumulation): forward in[r] = double x[ncols] -> out[r] = float y[nrows]; adjoint
+ * in[r] = float y[nrows] -> out[r] = double x[ncols].  Device pointers, enqueued on `stream`
+ * (the adjoint allocates its per-segment scratch and synchronises `stream` before freeing it).
+ * No reference counterpart: commit/operator/operator.pyx:118-184 applies one vector per call.
+ */
+int cgb_op_apply_batch(cgb_op *op, int adjoint, int nvec, const void *const *in, void *const *out, void *stream);
+
+/* Vectors per multi-right-hand-side pass: set >= 0 stores it (0 = time both widths on the next
+ * batched solve of >= 4 problems, 2 or 4 = fixed), set < 0 only reads; *width (may be NULL)
+ * receives the current value (0 while untuned). */
+int cgb_op_batch_width(cgb_op *op, int set, int *width);
+
 /* ------------------------------------------------------------------ proximal maps */
 /* In-place proximal maps on a DEVICE float64 vector (proximals.pyx:13-77). */
 int cgb_prox_non_negativity(double *x, int64_t start, int64_t size, void *stream);
