@@ -42,6 +42,11 @@ def parse():
     p.add_argument('--arith', default='ff', choices=['ff', 'f64', 'bf16', 'fp16', 'f32'])
     p.add_argument('--fista', action='store_true', help='FISTA time-to-tolerance, plain vs mixed + refinement')
     p.add_argument('--fista-iters', type=int, default=1500)
+    p.add_argument('--batch', action='store_true',
+                   help='regularisation paths: 8 tractograms x 16 lambdas, batched BF16 vs sequential plain solves')
+    p.add_argument('--batch-tracts', type=int, default=8, help='number of tractograms of the batched workload')
+    p.add_argument('--batch-scale', type=float, default=1.0, help='scale of the tractogram sizes (smaller runs)')
+    p.add_argument('--batch-iters', type=int, default=20, help='FISTA iterations per solve (tolerances off)')
     p.add_argument('--sample-frac', type=float, default=1.0 / 16.0, help='CPU sample: fraction of the segments')
     p.add_argument('--no-e2e', action='store_true')
     p.add_argument('--no-cpu', action='store_true')
@@ -388,10 +393,87 @@ def run_fista(args, spec, D, K, dev):
     return 0
 
 
+def run_batch(args):
+    """Regularisation paths on several tractograms: for each of the 8 tractograms (50k-400k
+    streamlines, full-brain grid, nS = 288) 16 nonnegative group-lasso problems (64 random
+    bundles, lambda = 1e-4..1e-1 of lambda_max), each run for the same number of FISTA
+    iterations (tolerances off, so both arms do identical iteration counts).  Arm 1: the
+    batched solver (BF16 LUT, multi-right-hand-side passes, one call per tractogram).  Arm 2:
+    the 128 problems solved one after another by the plain FP64-accurate solver.  Prints one
+    JSON line with both times, solves/s and the distance between the two arms' solutions."""
+    import torch
+    from commit_gb300 import evaluation, solvers, synth
+    from commit_gb300.operator import LinearOperator
+    dev = torch.device('cuda', torch.cuda.current_device())
+    M = args.batch_iters
+    tracts = []
+    tgen = 0.0
+    for k in range(args.batch_tracts):
+        spec = synth.batch_spec(k, int(synth.BATCH_FIBERS[k] * args.batch_scale))
+        t0 = time.perf_counter()
+        D, K = synth.make_dictionary(spec, device='cuda')
+        tgen += time.perf_counter() - t0
+        A = LinearOperator(D, K, None, arith='ff', device=dev.index)
+        y = A.dot(torch.from_numpy(synth.make_x(A.nCOLS, spec.seed + 1)).to(dev))
+        y = torch.from_numpy(synth.make_signal(y.cpu().numpy(), spec.seed + 2)).to(dev)
+        groups = synth.bundle_groups(D['IC']['nSTR'], 64, seed=spec.seed)
+        regs = [evaluation.set_regularisation(
+            A, y, D, K, regularisers=('group_lasso', None, None), lambdas=(lam, None, None),
+            is_nonnegative=(True, True, True),
+            params=({'group_idx': groups, 'group_weights_cardinality': True, 'group_weights_adaptive': False},
+                    None, None)) for lam in synth.BATCH_LAMBDAS]
+        tracts.append({'spec': spec, 'A': A, 'y': y, 'regs': regs, 'n_segments': int(D['IC']['n'])})
+        del D, K
+    # warm-up: reduced LUT copies, width tuning, plain kernels
+    for t in tracts:
+        solvers.solve_batch(t['y'], t['A'], t['regs'][:4], tol_fun=0.0, tol_x=0.0, max_iter=2)
+        solvers.solve(t['y'], t['A'], t['A'].T, tol_fun=0.0, tol_x=0.0, max_iter=2, verbose=0,
+                      regularisation=t['regs'][0])
+    torch.cuda.synchronize()
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    t0 = time.perf_counter()
+    xb = [solvers.solve_batch(t['y'], t['A'], t['regs'], tol_fun=0.0, tol_x=0.0, max_iter=M) for t in tracts]
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    xs = [[solvers.solve(t['y'], t['A'], t['A'].T, tol_fun=0.0, tol_x=0.0, max_iter=M, verbose=0,
+                         regularisation=rp) for rp in t['regs']] for t in tracts]
+    torch.cuda.synchronize()
+    t_seq = time.perf_counter() - t0
+    clk = clocks.stop()
+    dist = []
+    for b, s_ in zip(xb, xs):
+        for (x1, d1), (x2, d2) in zip(b, s_):
+            dist.append(float(torch.linalg.norm(x1 - x2) / torch.linalg.norm(x2)))
+    nsolves = sum(len(t['regs']) for t in tracts)
+    out = {'metric': 'regularisation paths: FISTA solves/s, batched BF16-LUT vs sequential plain',
+           'value': nsolves / t_batch, 'unit': 'solves/s', 'higher_is_better': True, 'n_gpus': 1,
+           'data': 'synthetic', 'dtype': 'bf16 LUT / f32 rows / f64 columns (batched); f64 (plain)',
+           'config': {'workload': f'{len(tracts)} tractograms x {len(synth.BATCH_LAMBDAS)} lambdas '
+                                  f'(1e-4..1e-1 of lambda_max), nonnegative group lasso over 64 random bundles, '
+                                  f'grid 145x174x145, 600k mask voxels, nS=288',
+                      'fibers': [t['spec'].n_fibers for t in tracts],
+                      'segments': [t['n_segments'] for t in tracts],
+                      'iterations_per_solve': M, 'tolerances': 'off (fixed iteration count)'},
+           'batched': {'seconds': t_batch, 'solves_per_s': nsolves / t_batch,
+                       'ms_per_solve_iteration': 1000.0 * t_batch / (nsolves * M),
+                       'widths': [t['A'].batch_width() for t in tracts]},
+           'sequential_plain': {'seconds': t_seq, 'solves_per_s': nsolves / t_seq,
+                                'ms_per_solve_iteration': 1000.0 * t_seq / (nsolves * M)},
+           'speedup': t_seq / t_batch,
+           'x_rel_batched_vs_plain': {'max': max(dist), 'median': statistics.median(dist)},
+           'clocks': clk, 'setup_s': {'generate': tgen}}
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == 'reference':
         return run_reference(args)
+    if args.batch:
+        return run_batch(args)
     return run_ours(args)
 
 

@@ -51,7 +51,7 @@ def test_debias_fit_matches_oracle_flow():
     from commit_gb300.operator import LinearOperator
     D, K, y = _case()
     A = LinearOperator(D, K, None)
-    reg = evaluation.set_regularisation(A, y, D, K, regularisers=('lasso', None, None), lambdas=(0.05, None, None))
+    reg = evaluation.set_regularisation(A, y, D, K, regularisers=('lasso', None, None), lambdas=(1e-3, None, None))
     x, det, Ad = evaluation.fit(D, K, y, regularisation=reg, tol_fun=1e-6, max_iter=150, debias=True)
     # oracle: the same two solves
     P = O.PortOperator(D, K, None)
@@ -62,6 +62,7 @@ def test_debias_fit_matches_oracle_flow():
     nF = D['IC']['nSTR']
     mask = np.ones(nF, dtype=np.uint32)
     mask[x1[:nF] < 1e-15] = 0
+    assert 0 < mask.sum() < nF      # the lasso removes some streamlines and keeps others
     D2 = {'IC': dict(D['IC'], eval=mask), 'EC': D['EC'], 'ISO': D['ISO']}
     P2 = O.PortOperator(D2, K, None)
     xd = x1.copy()
