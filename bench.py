@@ -47,6 +47,7 @@ def parse():
     p.add_argument('--batch-tracts', type=int, default=8, help='number of tractograms of the batched workload')
     p.add_argument('--batch-scale', type=float, default=1.0, help='scale of the tractogram sizes (smaller runs)')
     p.add_argument('--batch-iters', type=int, default=20, help='FISTA iterations per solve (tolerances off)')
+    p.add_argument('--batch-streams', type=int, default=4, help='tractograms solved concurrently (streams)')
     p.add_argument('--sample-frac', type=float, default=1.0 / 16.0, help='CPU sample: fraction of the segments')
     p.add_argument('--no-e2e', action='store_true')
     p.add_argument('--no-cpu', action='store_true')
@@ -433,7 +434,8 @@ def run_batch(args):
     clocks = ClockSampler(dev.index)
     clocks.start()
     t0 = time.perf_counter()
-    xb = [solvers.solve_batch(t['y'], t['A'], t['regs'], tol_fun=0.0, tol_x=0.0, max_iter=M) for t in tracts]
+    xb = solvers.solve_batches([(t['y'], t['A'], t['regs']) for t in tracts], n_streams=args.batch_streams,
+                               tol_fun=0.0, tol_x=0.0, max_iter=M)
     torch.cuda.synchronize()
     t_batch = time.perf_counter() - t0
     t0 = time.perf_counter()
@@ -458,7 +460,7 @@ def run_batch(args):
                       'iterations_per_solve': M, 'tolerances': 'off (fixed iteration count)'},
            'batched': {'seconds': t_batch, 'solves_per_s': nsolves / t_batch,
                        'ms_per_solve_iteration': 1000.0 * t_batch / (nsolves * M),
-                       'widths': [t['A'].batch_width() for t in tracts]},
+                       'widths': [t['A'].batch_width() for t in tracts], 'streams': args.batch_streams},
            'sequential_plain': {'seconds': t_seq, 'solves_per_s': nsolves / t_seq,
                                 'ms_per_solve_iteration': 1000.0 * t_seq / (nsolves * M)},
            'speedup': t_seq / t_batch,

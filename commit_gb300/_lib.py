@@ -83,6 +83,7 @@ def lib() -> ctypes.CDLL:
                                       ctypes.POINTER(c_vp), ctypes.POINTER(CgbFistaResult), P]
     L.cgb_op_batch_width.argtypes = [P, c_i32, ctypes.POINTER(c_i32)]
     L.cgb_op_apply_batch.argtypes = [P, c_i32, c_i32, ctypes.POINTER(c_vp), ctypes.POINTER(c_vp), P]
+    L.cgb_op_voxel_maps.argtypes = [P, P, P, P, P, P, P, P, P, P, P, P, P]
     L.cgb_prox_non_negativity.argtypes = [P, c_i64, c_i64, P]
     L.cgb_prox_soft_thresholding.argtypes = [P, c_f64, c_i64, c_i64, P]
     L.cgb_prox_w_soft_thresholding.argtypes = [P, P, c_f64, c_i64, c_i64, P]

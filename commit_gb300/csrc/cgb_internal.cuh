@@ -93,6 +93,7 @@ struct cgb_op {
     double *d_x64;                  // [ncols] staging for FP32 applies
     void *gstate;                   // LUT-gradient streams (lutgrad.cu), built on first use
     int batch_rhs;                  // vectors per multi-right-hand-side pass (0: not tuned)
+    int batch_reuse;                // batched FISTA momentum reuse chosen by timing (0: not tuned, 1 off, 2 on)
     uint32_t *vox_ptr, *seg_f, *eval, *fib_ptr, *fib_perm, *ec_ptr, *ec_col, *iso_ptr, *iso_col;
     uint16_t *seg_o, *ec_o;
     float *seg_l;

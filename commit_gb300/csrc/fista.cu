@@ -251,17 +251,21 @@ struct FistaWS {
     double *pstats = nullptr, *pgrp = nullptr, *pres = nullptr;
     // reduced-precision path: FP32 copies of y and sqrt(W), FP32 A*x buffers
     float *y32 = nullptr, *sqw32 = nullptr, *ax32[2] = {nullptr, nullptr};
+    cudaStream_t st = nullptr;  // allocations are stream-ordered on the solver's stream
     ~FistaWS() {
         void *ps[] = {xhat, prev, grad, ax[0], ax[1], pstats, pgrp, pres, y32, sqw32, ax32[0], ax32[1]};
         for (void *p : ps)
-            if (p) cudaFree(p);
+            if (p) cudaFreeAsync(p, st);
     }
 };
 
 namespace {
 
-int ws_alloc(double **p, size_t n) {
-    CGB_CUDA(cudaMalloc((void **)p, (n ? n : 1) * sizeof(double)));
+// stream-ordered allocation: no device-wide synchronisation, so solvers on other streams
+// (e.g. one regularisation path per tractogram) keep running
+template <class T>
+int ws_alloc(T **p, size_t n, cudaStream_t st) {
+    CGB_CUDA(cudaMallocAsync((void **)p, (n ? n : 1) * sizeof(T), st));
     return CGB_OK;
 }
 
@@ -287,29 +291,30 @@ struct Solver {
         const int rb = reduction_blocks(op);
         mixed = prm->arith == CGB_ARITH_BF16 || prm->arith == CGB_ARITH_FP16 || prm->arith == CGB_ARITH_F32;
         if (!dsc) dsc = op->dscal;
-        CGB_TRY(ws_alloc(&ws.xhat, nc));
-        CGB_TRY(ws_alloc(&ws.prev, nc));
-        CGB_TRY(ws_alloc(&ws.grad, nc));
+        ws.st = st;
+        CGB_TRY(ws_alloc(&ws.xhat, nc, st));
+        CGB_TRY(ws_alloc(&ws.prev, nc, st));
+        CGB_TRY(ws_alloc(&ws.grad, nc, st));
         if (batch_member) {
         } else if (mixed) {
             CGB_TRY(ensure_reduced(op, prm->arith));
-            CGB_CUDA(cudaMalloc((void **)&ws.y32, (nr > 0 ? nr : 1) * sizeof(float)));
+            CGB_TRY(ws_alloc(&ws.y32, nr, st));
             CGB_TRY(convert_f64_to_f32(y, ws.y32, nr, st));
             if (sqw) {
-                CGB_CUDA(cudaMalloc((void **)&ws.sqw32, (nr > 0 ? nr : 1) * sizeof(float)));
+                CGB_TRY(ws_alloc(&ws.sqw32, nr, st));
                 CGB_TRY(convert_f64_to_f32(sqw, ws.sqw32, nr, st));
             }
             if (prm->momentum_reuse) {
-                CGB_CUDA(cudaMalloc((void **)&ws.ax32[0], (nr > 0 ? nr : 1) * sizeof(float)));
-                CGB_CUDA(cudaMalloc((void **)&ws.ax32[1], (nr > 0 ? nr : 1) * sizeof(float)));
+                CGB_TRY(ws_alloc(&ws.ax32[0], nr, st));
+                CGB_TRY(ws_alloc(&ws.ax32[1], nr, st));
             }
         } else if (prm->momentum_reuse) {
-            CGB_TRY(ws_alloc(&ws.ax[0], nr));
-            CGB_TRY(ws_alloc(&ws.ax[1], nr));
+            CGB_TRY(ws_alloc(&ws.ax[0], nr, st));
+            CGB_TRY(ws_alloc(&ws.ax[1], nr, st));
         }
-        CGB_TRY(ws_alloc(&ws.pstats, (size_t)rb * kRedSlots));
-        CGB_TRY(ws_alloc(&ws.pgrp, (size_t)rb * kRedSlots));
-        CGB_TRY(ws_alloc(&ws.pres, (size_t)rb * kRedSlots));
+        CGB_TRY(ws_alloc(&ws.pstats, (size_t)rb * kRedSlots, st));
+        CGB_TRY(ws_alloc(&ws.pgrp, (size_t)rb * kRedSlots, st));
+        CGB_TRY(ws_alloc(&ws.pres, (size_t)rb * kRedSlots, st));
         // l1 parts of Omega with the reference's slicing (solvers.py:68, 150, 183)
         terms.n = 0;
         auto clamp = [&](int64_t v) { return v < 0 ? 0 : (v > nc ? nc : v); };
@@ -630,40 +635,42 @@ struct BatchSolver {
     float *y32 = nullptr, *sqw32 = nullptr;
     float *scr[4] = {nullptr, nullptr, nullptr, nullptr};
     std::vector<float *> ax32;  // 2 per problem with momentum reuse
-    double *bscal = nullptr, *hb = nullptr, *partials = nullptr;
+    double *bscal = nullptr, *partials = nullptr;
+    std::vector<double> hbv;  // host copy of the scalars (pageable: freeing it needs no device sync)
+    double *hb = nullptr;
     int R = 4;
     int calls = 0;
 
     ~BatchSolver() {
-        if (y32) cudaFree(y32);
-        if (sqw32) cudaFree(sqw32);
+        if (y32) cudaFreeAsync(y32, st);
+        if (sqw32) cudaFreeAsync(sqw32, st);
         for (float *p : scr)
-            if (p) cudaFree(p);
+            if (p) cudaFreeAsync(p, st);
         for (float *p : ax32)
-            if (p) cudaFree(p);
-        if (bscal) cudaFree(bscal);
-        if (partials) cudaFree(partials);
-        if (hb) cudaFreeHost(hb);
+            if (p) cudaFreeAsync(p, st);
+        if (bscal) cudaFreeAsync(bscal, st);
+        if (partials) cudaFreeAsync(partials, st);
     }
 
     int init() {
         const int64_t nr = op->nrows;
         CGB_TRY(ensure_reduced(op, CGB_ARITH_BF16));
-        CGB_CUDA(cudaMalloc((void **)&bscal, (size_t)P * 16 * sizeof(double)));
+        CGB_TRY(ws_alloc(&bscal, (size_t)P * 16, st));
         CGB_CUDA(cudaMemsetAsync(bscal, 0, (size_t)P * 16 * sizeof(double), st));
-        CGB_CUDA(cudaMallocHost((void **)&hb, (size_t)P * 16 * sizeof(double)));
-        CGB_CUDA(cudaMalloc((void **)&partials, (size_t)reduction_blocks(op) * kRedSlots * sizeof(double)));
-        CGB_CUDA(cudaMalloc((void **)&y32, (nr > 0 ? nr : 1) * sizeof(float)));
+        hbv.assign((size_t)P * 16, 0.0);
+        hb = hbv.data();
+        CGB_TRY(ws_alloc(&partials, (size_t)reduction_blocks(op) * kRedSlots, st));
+        CGB_TRY(ws_alloc(&y32, nr, st));
         CGB_TRY(convert_f64_to_f32(y, y32, nr, st));
         if (sqw) {
-            CGB_CUDA(cudaMalloc((void **)&sqw32, (nr > 0 ? nr : 1) * sizeof(float)));
+            CGB_TRY(ws_alloc(&sqw32, nr, st));
             CGB_TRY(convert_f64_to_f32(sqw, sqw32, nr, st));
         }
         const size_t nscr = (size_t)(op->n > 0 ? op->n : 1) * (op->nIC > 0 ? op->nIC : 1);
-        for (int r = 0; r < 4; ++r) CGB_CUDA(cudaMalloc((void **)&scr[r], nscr * sizeof(float)));
-        if (prm->momentum_reuse) {
+        for (int r = 0; r < 4; ++r) CGB_TRY(ws_alloc(&scr[r], nscr, st));
+        if (prm->momentum_reuse && (prm->momentum_reuse != 2 || op->batch_reuse != 1)) {
             ax32.assign((size_t)2 * P, nullptr);
-            for (auto &p : ax32) CGB_CUDA(cudaMalloc((void **)&p, (nr > 0 ? nr : 1) * sizeof(float)));
+            for (auto &p : ax32) CGB_TRY(ws_alloc(&p, nr, st));
         }
         S.resize(P);
         for (int p = 0; p < P; ++p) {
@@ -794,31 +801,66 @@ struct BatchSolver {
         return CGB_OK;
     }
 
-    // multi-right-hand-side width: time one gradient pass of 4 problems as one R = 4 pass
-    // and as two R = 2 passes, keep the faster (stored on the operator)
-    int tune(double *const *xs) {
-        if (op->batch_rhs != 0 || P < 4 || op->nV == 0) return CGB_OK;
-        cudaEvent_t e[3];
+    // Autotuner, run on first use and kept on the handle: the vectors per pass (R = 2 or 4)
+    // and, when params->momentum_reuse is 2 (automatic), whether the gradient takes
+    // A x_hat from the stored A x rows (saves a forward product, costs three FP32 row-sized
+    // transfers per problem) or recomputes it in the fused pass.  Each candidate is timed
+    // on one iteration's operator passes of up to 4 problems (one warm-up round first).
+    bool reuse = false;
+    int tune() {
+        const bool want_r = op->batch_rhs == 0 && P >= 4;
+        const bool want_reuse = prm->momentum_reuse == 2 && op->batch_reuse == 0;
+        if (op->nV == 0 || (!want_r && !want_reuse)) return CGB_OK;
+        std::vector<int> J;
+        for (int p = 0; p < P && p < 4; ++p) J.push_back(p);
+        std::vector<double *> xh(P);
+        for (int p = 0; p < P; ++p) xh[p] = S[p].ws.xhat;
+        std::vector<int> zero(P, 0);
+        std::vector<double> one(P, 1.0), nil(P, 0.0);
+        cudaEvent_t e[2];
         for (auto &ev : e) CGB_CUDA(cudaEventCreate(&ev));
-        std::vector<int> J = {0, 1, 2, 3};
-        float best[2] = {0.f, 0.f};
+        auto timed = [&](auto &&f, float *ms) -> int {
+            CGB_CUDA(cudaEventRecord(e[0], st));
+            CGB_TRY(f());
+            CGB_CUDA(cudaEventRecord(e[1], st));
+            CGB_CUDA(cudaEventSynchronize(e[1]));
+            CGB_CUDA(cudaEventElapsedTime(ms, e[0], e[1]));
+            return CGB_OK;
+        };
         const int widths[2] = {4, 2};
+        const int nw = want_r ? 2 : 1;
+        float cost[2][2] = {{0.f, 0.f}, {0.f, 0.f}};  // [width][reuse]
         for (int rep = 0; rep < 2; ++rep) {
-            for (int k = 0; k < 2; ++k) {
-                R = widths[k];
-                CGB_CUDA(cudaEventRecord(e[0], st));
-                CGB_TRY(gradient(J, false, nullptr, nullptr, nullptr, nullptr));
-                CGB_CUDA(cudaEventRecord(e[1], st));
-                CGB_CUDA(cudaEventSynchronize(e[1]));
-                float ms = 0.f;
-                CGB_CUDA(cudaEventElapsedTime(&ms, e[0], e[1]));
-                if (rep == 1) best[k] = ms;  // first round warms both up
+            for (int k = 0; k < nw; ++k) {
+                R = want_r ? widths[k] : (op->batch_rhs == 2 ? 2 : 4);
+                float t0 = 0.f, t1 = 0.f, t2 = 0.f, t3 = 0.f;
+                CGB_TRY(timed([&] { return forward(J, xh.data(), y32, 0, nullptr); }, &t0));
+                CGB_TRY(timed([&] { return gradient(J, false, nullptr, nullptr, nullptr, nullptr); }, &t1));
+                if (!ax32.empty()) {
+                    CGB_TRY(timed([&] { return forward(J, xh.data(), y32, 0, zero.data()); }, &t2));
+                    CGB_TRY(timed([&] { return gradient(J, true, zero.data(), zero.data(), one.data(), nil.data()); },
+                                  &t3));
+                }
+                if (rep == 1) {
+                    cost[k][0] = t0 + t1;
+                    cost[k][1] = t2 + t3;
+                }
             }
         }
         for (auto &ev : e) cudaEventDestroy(ev);
-        op->batch_rhs = best[1] < best[0] ? 2 : 4;
-        R = op->batch_rhs;
-        (void)xs;
+        int kb = 0;
+        if (want_r) {
+            // reuse: -1 to be chosen, else fixed (by the caller or an earlier tuning)
+            const int ru = want_reuse ? -1 : (prm->momentum_reuse == 2 ? op->batch_reuse == 2 : prm->momentum_reuse != 0);
+            auto best_of = [&](int k) {
+                if (ru >= 0) return cost[k][ru];
+                return cost[k][0] < cost[k][1] ? cost[k][0] : cost[k][1];
+            };
+            kb = best_of(1) < best_of(0) ? 1 : 0;
+            op->batch_rhs = widths[kb];
+        }
+        if (want_reuse) op->batch_reuse = cost[kb][1] < cost[kb][0] ? 2 : 1;
+        R = op->batch_rhs == 2 ? 2 : 4;
         return CGB_OK;
     }
 
@@ -830,7 +872,8 @@ struct BatchSolver {
         for (int p = 0; p < P; ++p) all[p] = p;
         for (int p = 0; p < P; ++p)
             CGB_CUDA(cudaMemcpyAsync(S[p].ws.xhat, xs[p], nc * sizeof(double), cudaMemcpyDeviceToDevice, st));
-        CGB_TRY(tune(xs));
+        CGB_TRY(tune());
+        reuse = prm->momentum_reuse == 2 ? op->batch_reuse == 2 : prm->momentum_reuse != 0;
         // initialisation (solvers.py:260-286), all problems at once
         CGB_TRY(gradient(all, false, nullptr, nullptr, nullptr, nullptr));
         std::vector<double *> gp(P);
@@ -857,7 +900,7 @@ struct BatchSolver {
             step[p] = 1.9 / (Ln * Ln);
             CGB_CUDA(cudaMemcpyAsync(S[p].ws.prev, S[p].ws.xhat, nc * sizeof(double), cudaMemcpyDeviceToDevice, st));
         }
-        const bool reuse_on = prm->momentum_reuse != 0;
+        const bool reuse_on = reuse;
         int have_prev_ax = 0;
         std::vector<int> J = all;
         int it = 1;
@@ -1060,10 +1103,10 @@ int cgb_op_apply_batch(cgb_op *op, int adjoint, int nvec, const void *const *in,
         const size_t nscr = (size_t)(op->n > 0 ? op->n : 1) * (op->nIC > 0 ? op->nIC : 1);
         for (int r = 0; r < W; ++r) {
             float *p = nullptr;
-            const cudaError_t e = cudaMalloc((void **)&p, nscr * sizeof(float));
+            const cudaError_t e = cudaMallocAsync((void **)&p, nscr * sizeof(float), st);
             if (e != cudaSuccess) {
-                for (float *q : scr) cudaFree(q);
-                return cuda_fail(e, "cudaMalloc");
+                for (float *q : scr) cudaFreeAsync(q, st);
+                return cuda_fail(e, "cudaMallocAsync");
             }
             scr.push_back(p);
         }
@@ -1095,10 +1138,7 @@ int cgb_op_apply_batch(cgb_op *op, int adjoint, int nvec, const void *const *in,
         }
         i += take;
     }
-    if (!scr.empty()) {
-        cudaStreamSynchronize(st);
-        for (float *q : scr) cudaFree(q);
-    }
+    for (float *q : scr) cudaFreeAsync(q, st);
     return rc;
 }
 

@@ -221,3 +221,61 @@ def fit(DICTIONARY, KERNELS, y, regularisation=None, tol_fun=1e-3, tol_x=1e-6, m
         x, details = solvers.solve(y2, A, A.T, tol_fun=tol_fun, tol_x=tol_x, max_iter=max_iter, verbose=0, x0=x0,
                                    regularisation=solvers.init_regularisation(rp), confidence_array=confidence_array)
     return x, details, A
+
+
+def voxel_maps(A: LinearOperator, x, y=None, confidence=None, norm_fib=None, normalize_maps=False,
+               DICTIONARY=None) -> dict:
+    """The voxelwise maps of Evaluation.save_results (commit/core.pyx:1614-1750), computed on
+    the device from the operator's voxel-ordered streams (``cgb_op_voxel_maps``).
+
+    x: fitted coefficients (as save_results rescales them); y: the measured signal
+    (nROWS) for the error maps; confidence: the confidence map (nROWS) for the adjusted
+    error maps; norm_fib: per-IC-column weights (the reference's np.kron(ones(nIC), TRK
+    norm) when kernels were normalised).  Returns float32 numpy arrays per mask voxel:
+    'compartment_IC', 'compartment_EC', 'compartment_ISO' (divided by their sum + 1e-16
+    when normalize_maps, as doNormalizeMaps), and with y 'fit_RMSE', 'fit_NRMSE', plus
+    with confidence 'fit_RMSE_adjusted', 'fit_NRMSE_adjusted'.  With DICTIONARY (holding
+    MASK and MASK_ix/iy/iz) each map is also returned as a 3-D volume under '<name>_vol'."""
+    import ctypes
+    from . import _lib
+    dev = torch.device('cuda', A.device)
+
+    def d(a, n):
+        if a is None:
+            return None
+        t = torch.as_tensor(np.asarray(a, dtype=np.float64) if not isinstance(a, torch.Tensor) else a,
+                            dtype=torch.float64).to(dev).contiguous()
+        if t.numel() != n:
+            raise RuntimeError('voxel_maps: dimensions do not match')
+        return t
+
+    nV = A.ICnVOX
+    xd = d(x, A.nCOLS)
+    yd = d(y, A.nROWS)
+    cd = d(confidence, A.nROWS)
+    nf = d(norm_fib, A.ICnSTR * A.ICnRF)
+    names = ['compartment_IC', 'compartment_EC', 'compartment_ISO']
+    if yd is not None:
+        names += ['fit_RMSE', 'fit_NRMSE']
+        if cd is not None:
+            names += ['fit_RMSE_adjusted', 'fit_NRMSE_adjusted']
+    out = {k: torch.zeros(nV, dtype=torch.float64, device=dev) for k in names}
+    p = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else None  # noqa: E731
+    st = torch.cuda.current_stream(dev).cuda_stream
+    _lib.check(_lib.lib().cgb_op_voxel_maps(
+        A.handle, p(xd), p(yd), p(cd), p(nf), p(out['compartment_IC']), p(out['compartment_EC']),
+        p(out['compartment_ISO']), p(out.get('fit_RMSE')), p(out.get('fit_NRMSE')),
+        p(out.get('fit_RMSE_adjusted')), p(out.get('fit_NRMSE_adjusted')), ctypes.c_void_p(st)))
+    res = {k: v.cpu().numpy().astype(np.float32) for k, v in out.items()}
+    if normalize_maps:   # core.pyx:1752-1755, FP32 as the reference's float32 images
+        tot = res['compartment_IC'] + res['compartment_EC'] + res['compartment_ISO']
+        for k in ('compartment_IC', 'compartment_EC', 'compartment_ISO'):
+            res[k] = res[k] / (tot + np.float32(1e-16))
+    if DICTIONARY is not None and 'MASK' in DICTIONARY:
+        dim = np.asarray(DICTIONARY['MASK']).shape
+        ix, iy, iz = DICTIONARY['MASK_ix'], DICTIONARY['MASK_iy'], DICTIONARY['MASK_iz']
+        for k in list(res):
+            vol = np.zeros(dim, dtype=np.float32)
+            vol[ix, iy, iz] = res[k]
+            res[k + '_vol'] = vol
+    return res

@@ -326,7 +326,7 @@ def solve_mixed(y, A, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, verbose=0, x0=Non
 
 
 def solve_batch(y, A, regularisations, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, x0=None, confidence_array=None,
-                momentum_reuse=True):
+                momentum_reuse='auto'):
     """Several problems on one operator and one y, e.g. a regularisation path over lambda.
 
     ``regularisations`` is a list of regularisation dicts (as for ``solve``; None for no
@@ -335,7 +335,9 @@ def solve_batch(y, A, regularisations, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, 
     the products of all problems at the same stage share multi-right-hand-side passes
     (``cgb_fista_batch_run``).  Returns a list of (x, opt_details), x on the device of A when
     y is a CUDA tensor, numpy otherwise.  Polish a solution with ``solve(..., x0=x)`` in FP64
-    where the BF16 operator's bias matters (as ``solve_mixed`` does for one problem)."""
+    where the BF16 operator's bias matters (as ``solve_mixed`` does for one problem).
+    ``momentum_reuse``: True, False, or 'auto' (chosen by timing on the first batched solve
+    on this operator, together with the vectors per pass)."""
     if not isinstance(A, LinearOperator):
         raise TypeError('A must be a commit_gb300.operator.LinearOperator')
     if A.adjoint:
@@ -379,8 +381,8 @@ def solve_batch(y, A, regularisations, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, 
             xs.append(torch.as_tensor(np.asarray(x0p, dtype=np.float64) if not isinstance(x0p, torch.Tensor) else x0p,
                                       dtype=torch.float64).to(dev).clone().contiguous())
     ptrs = (ctypes.c_void_p * P)(*[x.data_ptr() for x in xs])
-    prm = _lib.CgbFistaParams(float(tol_fun), float(tol_x), int(max_iter), 0, _lib.ARITH['bf16'],
-                              int(bool(momentum_reuse)))
+    mr = 2 if momentum_reuse == 'auto' else int(bool(momentum_reuse))
+    prm = _lib.CgbFistaParams(float(tol_fun), float(tol_x), int(max_iter), 0, _lib.ARITH['bf16'], mr)
     res = (_lib.CgbFistaResult * P)()
     st = torch.cuda.current_stream(dev).cuda_stream
     check(lib().cgb_fista_batch_run(A.handle, ctypes.c_void_p(yd.data_ptr()),
@@ -398,3 +400,40 @@ def solve_batch(y, A, regularisations, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, 
             det['batch_operator_calls'] = int(r.operator_calls)
         out.append((xs[p].cpu().numpy() if host else xs[p], det))
     return out
+
+
+def solve_batches(jobs, n_streams: int = 4, **kw):
+    """Regularisation paths on several operators (e.g. tractograms of uneven size) at once.
+
+    jobs: list of (y, A, regularisations).  Each job runs ``solve_batch`` on its own CUDA
+    stream from its own host thread (the library releases the GIL and allocates
+    stream-ordered), up to n_streams at a time, so the device overlaps one job's host
+    decisions and small passes with another job's work.  Returns one list of (x, details)
+    per job, in order."""
+    from concurrent.futures import ThreadPoolExecutor
+    if not jobs:
+        return []
+    n_streams = max(1, min(int(n_streams), len(jobs)))
+    devs = [torch.device('cuda', A.device) for _, A, _ in jobs]
+    streams = [torch.cuda.Stream(device=devs[0]) for _ in range(n_streams)]
+    for s in streams:
+        s.wait_stream(torch.cuda.current_stream(devs[0]))
+
+    def run(k):
+        y, A, regs = jobs[k]
+        s = streams[k % n_streams]
+        with torch.cuda.device(devs[k]), torch.cuda.stream(s):
+            out = solve_batch(y, A, regs, **kw)
+        s.synchronize()
+        return out
+
+    if n_streams == 1:
+        return [run(k) for k in range(len(jobs))]
+    # job k uses stream k % n_streams: a worker per stream keeps each stream's jobs in order
+    with ThreadPoolExecutor(max_workers=n_streams) as ex:
+        futs = [ex.submit(lambda w=w: [(k, run(k)) for k in range(w, len(jobs), n_streams)])
+                for w in range(n_streams)]
+        res = {}
+        for f in futs:
+            res.update(dict(f.result()))
+    return [res[k] for k in range(len(jobs))]

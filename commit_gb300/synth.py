@@ -350,6 +350,8 @@ def make_dictionary(spec: ProblemSpec, device: str = 'cpu') -> tuple[dict, dict]
                   'TRK': {'kept': kept, 'norm': norm},
                   'ndirs': spec.ndirs, 'nV': nV, 'dim': spec.dim,
                   'MASK': tdi.reshape(spec.dim, order='F')}
+    # mask voxel k sits at (MASK_ix[k], MASK_iy[k], MASK_iz[k]) (Fortran order, core.pyx:571-574)
+    DICTIONARY['MASK_ix'], DICTIONARY['MASK_iy'], DICTIONARY['MASK_iz'] = np.unravel_index(tdi_lin, spec.dim, order='F')
     return DICTIONARY, KERNELS
 
 

@@ -187,7 +187,8 @@ typedef struct {
     int max_iter;
     int verbose;          /* 0: quiet                                                    */
     int arith;            /* CGB_ARITH_F64 / CGB_ARITH_FF                                 */
-    int momentum_reuse;   /* 1: A*xhat from A*x and A*prev_x (exact in exact arithmetic) */
+    int momentum_reuse;   /* 1: A*xhat from A*x and A*prev_x (exact in exact arithmetic);   */
+                          /* 2 (cgb_fista_batch_run only): on or off as timed on first use */
     /* optional convergence trace: with x_ref (DEVICE, ncols) and trace (HOST, 2*trace_len
        doubles) set, accepted iteration k (k < trace_len) records trace[2k] = seconds since
        the call started and trace[2k+1] = |x_k - x_ref| / |x_ref| */
@@ -231,7 +232,7 @@ int cgb_fista_batch_run(cgb_op *op, const double *y, const double *sqrt_w, const
  * A or A' of nvec vectors in one multi-right-hand-side pass per 2 or 4 vectors (BF16 LUT,
  * FP32 accumulation): forward in[r] = double x[ncols] -> out[r] = float y[nrows]; adjoint
  * in[r] = float y[nrows] -> out[r] = double x[ncols].  Device pointers, enqueued on `stream`
- * (the adjoint allocates its per-segment scratch and synchronises `stream` before freeing it).
+ * (the adjoint's per-segment scratch is allocated and freed stream-ordered on `stream`).
  * No reference counterpart: commit/operator/operator.pyx:118-184 applies one vector per call.
  */
 int cgb_op_apply_batch(cgb_op *op, int adjoint, int nvec, const void *const *in, void *const *out, void *stream);
@@ -240,6 +241,21 @@ int cgb_op_apply_batch(cgb_op *op, int adjoint, int nvec, const void *const *in,
  * batched solve of >= 4 problems, 2 or 4 = fixed), set < 0 only reads; *width (may be NULL)
  * receives the current value (0 while untuned). */
 int cgb_op_batch_width(cgb_op *op, int set, int *width);
+
+/* ------------------------------------------------------------------ voxelwise maps */
+/*
+ * The maps of Evaluation.save_results (commit/core.pyx:1614-1750) for a fitted x (device
+ * f64[ncols]); every output is a device f64[nV] (mask voxel order) or NULL to skip it.
+ *   ic / ec / iso: compartment maps (core.pyx:1717-1750).  IC sums len * (sum over the
+ *     streamline's responses of x * norm_fib) over the voxel's segments; norm_fib is
+ *     f64[nF*nIC] or NULL for ones.  EC / ISO sum the voxel's coefficients.
+ *   rmse / nrmse (core.pyx:1662-1680) and rmse_conf / nrmse_conf (core.pyx:1682-1705, need
+ *     conf f64[nrows]) compare y_mea (f64[nrows]) with A x, both rounded to FP32 as the
+ *     reference does; sums are FP64.  A x is formed in a temporary device buffer.
+ */
+int cgb_op_voxel_maps(cgb_op *op, const double *x, const double *y_mea, const double *conf, const double *norm_fib,
+                      double *ic, double *ec, double *iso, double *rmse, double *nrmse, double *rmse_conf,
+                      double *nrmse_conf, void *stream);
 
 /* ------------------------------------------------------------------ proximal maps */
 /* In-place proximal maps on a DEVICE float64 vector (proximals.pyx:13-77). */

@@ -598,3 +598,57 @@ def reg_params(D: dict, K: dict, regularisers=(None, None, None), is_nonnegative
     rp['nnIC'], rp['nnEC'], rp['nnISO'] = is_nonnegative
     rp['dictIC_params'] = rp['dictEC_params'] = rp['dictISO_params'] = None
     return rp
+
+
+def voxel_maps(D: dict, K: dict, x, y_est, y_mea=None, conf=None, norm_fib=None) -> dict:
+    """Maps of Evaluation.save_results (commit/core.pyx:1662-1750), numpy restatement.
+    y_est = A x.  Error maps compare FP32-rounded signals (core.pyx:1664-1665) with FP64
+    sums; bincount lengths are the number of mask voxels."""
+    nV = int(D['IC']['nVOX'])
+    nSTR = int(D['IC']['nSTR'])
+    nE = int(D['EC']['n'])
+    nIC, nEC, nISO = K['wmr'].shape[0], K['wmh'].shape[0], K['iso'].shape[0]
+    x = np.asarray(x, dtype=np.float64)
+    out = {}
+    if nIC > 0:                                                  # core.pyx:1717-1725
+        off = nSTR * nIC
+        w = np.ones(off) if norm_fib is None else np.asarray(norm_fib, dtype=np.float64)
+        tmp = (x[:off].reshape((-1, nSTR)) * w.reshape((-1, nSTR))).sum(axis=0)
+        out['compartment_IC'] = np.bincount(D['IC']['vox'], minlength=nV,
+                                            weights=tmp[D['IC']['str']] * D['IC']['len'])
+    else:
+        out['compartment_IC'] = np.zeros(nV)
+    if nEC > 0 and nE > 0:                                       # core.pyx:1731-1736
+        off = nSTR * nIC
+        tmp = x[off:off + nE * nEC].reshape((-1, nE)).sum(axis=0)
+        out['compartment_EC'] = np.bincount(D['EC']['vox'], weights=tmp, minlength=nV)
+    else:
+        out['compartment_EC'] = np.zeros(nV)
+    nI = int(D['ISO']['n'])
+    if nISO > 0 and nI > 0:                                      # core.pyx:1742-1748
+        off = nSTR * nIC + nE * nEC
+        tmp = x[off:off + nI * nISO].reshape((-1, nI)).sum(axis=0)
+        out['compartment_ISO'] = np.bincount(D['ISO']['vox'], weights=tmp, minlength=nV)
+    else:
+        out['compartment_ISO'] = np.zeros(nV)
+    if y_mea is not None:                                        # core.pyx:1662-1680
+        ym = np.asarray(y_mea).astype(np.float32).reshape((nV, -1))
+        ye = np.asarray(y_est).astype(np.float32).reshape((nV, -1))
+        d2 = ((ym - ye).astype(np.float64)) ** 2
+        y2 = ym.astype(np.float64) ** 2
+        out['fit_RMSE'] = np.sqrt(d2.mean(axis=1))
+        tmp = y2.sum(axis=1)
+        idx = np.where(tmp < 1e-12)
+        tmp[idx] = 1
+        tmp = np.sqrt(d2.sum(axis=1) / tmp)
+        tmp[idx] = 0
+        out['fit_NRMSE'] = tmp
+        if conf is not None:                                     # core.pyx:1682-1705
+            c = np.asarray(conf).astype(np.float32).astype(np.float64).reshape((nV, -1))
+            for name, den in (('fit_RMSE_adjusted', c.sum(axis=1)), ('fit_NRMSE_adjusted', (c * y2).sum(axis=1))):
+                idx = np.where(den < 1e-12)
+                den[idx] = 1
+                t = np.sqrt((c * d2).sum(axis=1) / den)
+                t[idx] = 0
+                out[name] = t
+    return out

@@ -139,3 +139,25 @@ def test_batch_rejects_bad_arguments():
     rc = _lib.lib().cgb_fista_batch_run(A.handle, ctypes.c_void_p(y.data_ptr()), None, ctypes.byref(reg), 1,
                                         ctypes.byref(prm), ptrs, res, None)
     assert rc == _lib.CGB_ERR_UNSUPPORTED
+
+
+def test_concurrent_paths_match_one_at_a_time():
+    """solve_batches runs each operator's path on its own stream and thread; with the
+    width and momentum reuse fixed the results are bitwise those of solve_batch."""
+    from commit_gb300 import solvers, synth
+    from commit_gb300.operator import LinearOperator
+    jobs = []
+    for seed in (21, 22, 23):
+        D, K = synth.make_dictionary(synth.scaled_spec('demo_5k', seed=seed, n_fibers=3000))
+        P = O.PortOperator(D, K, None, nthreads=8)
+        y = synth.make_signal(P.dot(synth.make_x(P.nCOLS, 1)), 2)
+        A = LinearOperator(D, K, None)
+        A.batch_width(2)
+        jobs.append((y, A, _path_regs(A, D, K, y, [1e-4, 1e-3, 1e-2])))
+    kw = dict(tol_fun=1e-5, tol_x=1e-7, max_iter=60, momentum_reuse=True)
+    seq = [solvers.solve_batch(y, A, regs, **kw) for y, A, regs in jobs]
+    con = solvers.solve_batches(jobs, n_streams=3, **kw)
+    for a, b in zip(seq, con):
+        for (x1, d1), (x2, d2) in zip(a, b):
+            assert d1['iterations'] == d2['iterations']
+            assert np.array_equal(x1, x2)
