@@ -44,6 +44,21 @@ class CgbFistaResult(ctypes.Structure):
                 ('stopping_criterion', c_i32), ('backtracks', c_i32), ('operator_calls', c_i32)]
 
 
+class CgbT2DParams(ctypes.Structure):
+    _fields_ = [('dim', c_i32 * 3), ('pixdim', ctypes.c_float * 3), ('fiber_shift', ctypes.c_float * 3),
+                ('min_seg_len', ctypes.c_float), ('min_fiber_len', ctypes.c_float), ('max_fiber_len', ctypes.c_float),
+                ('do_intersect', c_i32), ('n_replicas', c_i32), ('blur_rho', c_vp), ('blur_angle', c_vp),
+                ('blur_weights', c_vp), ('n_peaks', c_i32), ('vf_thr', ctypes.c_float), ('flip', c_i32 * 3),
+                ('peaks_affine', c_f64 * 9)]
+
+
+class CgbT2DResult(ctypes.Structure):
+    _fields_ = [('n_fibers', c_i64), ('n_kept', c_i64), ('n_segments', c_i64), ('n_ec', c_i64), ('n_iso', c_i64),
+                ('ic_f', c_vp), ('ic_v', c_vp), ('ic_o', c_vp), ('ic_len', c_vp), ('trk_norm', c_vp),
+                ('trk_len', c_vp), ('trk_lentot', c_vp), ('trk_kept', c_vp), ('ec_v', c_vp), ('ec_o', c_vp),
+                ('iso_v', c_vp), ('tdi', c_vp)]
+
+
 _lib = None
 
 
@@ -84,6 +99,8 @@ def lib() -> ctypes.CDLL:
     L.cgb_op_batch_width.argtypes = [P, c_i32, ctypes.POINTER(c_i32)]
     L.cgb_op_apply_batch.argtypes = [P, c_i32, c_i32, ctypes.POINTER(c_vp), ctypes.POINTER(c_vp), P]
     L.cgb_op_voxel_maps.argtypes = [P, P, P, P, P, P, P, P, P, P, P, P, P]
+    L.cgb_trk2dict.argtypes = [ctypes.POINTER(CgbT2DParams), P, P, c_i64, P, P, P, P, P, ctypes.POINTER(CgbT2DResult), P]
+    L.cgb_trk2dict_free.argtypes = [ctypes.POINTER(CgbT2DResult)]
     L.cgb_prox_non_negativity.argtypes = [P, c_i64, c_i64, P]
     L.cgb_prox_soft_thresholding.argtypes = [P, c_f64, c_i64, c_i64, P]
     L.cgb_prox_w_soft_thresholding.argtypes = [P, P, c_f64, c_i64, c_i64, P]

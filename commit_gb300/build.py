@@ -26,6 +26,11 @@ NVCC_FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '-Xcompil
               '--expt-relaxed-constexpr', '-diag-suppress', '128', '-I', os.path.join(ROOT, 'include')]
 
 
+# per-file extra flags: the voxeliser reproduces the reference's FP64 geometry operation
+# by operation, so no multiply-add may be fused there
+FILE_FLAGS = {'trk2dict.cu': ['-fmad=false']}
+
+
 def nvcc() -> str:
     for cand in (os.environ.get('NVCC'), shutil.which('nvcc'), '/usr/local/cuda/bin/nvcc'):
         if cand and os.path.exists(cand):
@@ -60,7 +65,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
 
     def compile_one(so):
         s, o = so
-        cmd = [nv] + GENCODE + NVCC_FLAGS + ['-c', s, '-o', o + '.tmp']
+        cmd = [nv] + GENCODE + NVCC_FLAGS + FILE_FLAGS.get(os.path.basename(s), []) + ['-c', s, '-o', o + '.tmp']
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f'nvcc failed on {os.path.basename(s)}:\n{r.stderr[-4000:]}')

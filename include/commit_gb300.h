@@ -257,6 +257,51 @@ int cgb_op_voxel_maps(cgb_op *op, const double *x, const double *y_mea, const do
                       double *ic, double *ec, double *iso, double *rmse, double *nrmse, double *rmse_conf,
                       double *nrmse_conf, void *stream);
 
+/* ------------------------------------------------------------------ trk2dictionary */
+/*
+ * Streamline voxelisation (commit/trk2dictionary/trk2dictionary_c.cpp:111-440) on the device.
+ * All arrays are DEVICE pointers.  Streamline f has the points pts[3*offsets[f] ..
+ * 3*offsets[f+1]) (x, y, z in mm of the image grid, i.e. the .trk "voxmm" space).  The
+ * grids (mask, iso_mask: u8, peaks: f32 [.. , n_peaks, 3], tdi: f64) are C-order arrays over
+ * (x, y, z) as the reference reads them; mask / iso_mask / peaks / blur_apply may be NULL.
+ * hash: the 181 x 181 table from (colatitude, longitude) in whole degrees to a direction
+ * index.  Outputs are allocated on the device by the call and released by
+ * cgb_trk2dict_free; they are the arrays of the dictionary_*.dict files (IC_f counts kept
+ * streamlines, voxel ids x + X*(y + Y*z)).  Geometry in FP64 without fused multiply-adds
+ * and FP32 per-key sums, as the reference.
+ */
+typedef struct {
+    int dim[3];
+    float pixdim[3];
+    float fiber_shift[3];          /* in voxels, as the reference's fiber_shift */
+    float min_seg_len, min_fiber_len, max_fiber_len;
+    int do_intersect;
+    int n_replicas;                /* blur replicas (1: none); rho / angle / weights on the device */
+    const double *blur_rho, *blur_angle, *blur_weights;
+    int n_peaks;                   /* EC: peaks per voxel, relative threshold, axis flips, affine */
+    float vf_thr;
+    int flip[3];
+    double peaks_affine[9];
+} cgb_t2d_params;
+
+typedef struct {
+    int64_t n_fibers, n_kept, n_segments, n_ec, n_iso;
+    uint32_t *ic_f, *ic_v;
+    uint16_t *ic_o;
+    float *ic_len;
+    float *trk_norm, *trk_len, *trk_lentot; /* per kept streamline */
+    uint8_t *trk_kept;                      /* per input streamline */
+    uint32_t *ec_v;
+    uint16_t *ec_o;
+    uint32_t *iso_v;
+    double *tdi;                            /* track density (sum of segment lengths), C order */
+} cgb_t2d_result;
+
+int cgb_trk2dict(const cgb_t2d_params *prm, const float *pts, const int64_t *offsets, int64_t nfib,
+                 const uint8_t *blur_apply, const int16_t *hash, const uint8_t *mask, const float *peaks,
+                 const uint8_t *iso_mask, cgb_t2d_result *out, void *stream);
+int cgb_trk2dict_free(cgb_t2d_result *res);
+
 /* ------------------------------------------------------------------ proximal maps */
 /* In-place proximal maps on a DEVICE float64 vector (proximals.pyx:13-77). */
 int cgb_prox_non_negativity(double *x, int64_t start, int64_t size, void *stream);

@@ -13,7 +13,13 @@ CPU baseline.  Outputs go to ``oracle/_ref/`` only (git-ignored).
 2. gcc compiles it with the reference's flags (setup.py:38-43: ``-w -O3 -Ofast``) into
    ``oracle/_ref/libcommit_ref_operator.so``; rebuilt when the library is missing or was
    built for another machine architecture.
-3. With ``--python`` (needs Cython and the reference tree): Cython-compiles
+3. ``oracle/_ref/libt2d_ref.so``: the reference's streamline voxeliser
+   (commit/trk2dictionary/trk2dictionary_c.cpp, compiled from the reference tree with its
+   Vector.h / ProgressBar.h and the numpy / Python headers it includes, no libpython
+   needed) plus ``oracle/t2d_ref_driver.cpp``, a C entry point that runs it on a .trk
+   file.  ``-ffp-contract=off`` keeps the FP64 geometry free of fused multiply-adds on
+   every architecture.  Needs the reference tree; skipped without it.
+4. With ``--python`` (needs Cython and the reference tree): Cython-compiles
    commit/proximals.pyx into ``oracle/_ref/py/commit/`` and writes a two-function
    ``dicelib.ui`` logger stub, so the reference ``commit/solvers.py`` can be imported
    for golden-vector generation (``tests/golden/make_golden.py``).
@@ -110,10 +116,37 @@ def build_python() -> bool:
     return True
 
 
+T2D_LIB = os.path.join(REF_OUT, 'libt2d_ref.so')
+
+
+def compile_trk2dictionary() -> bool:
+    root = reference_root()
+    if root is None:
+        return False
+    try:
+        import numpy
+    except ImportError:
+        return False
+    src_dir = os.path.join(root, 'commit', 'trk2dictionary')
+    src = os.path.join(src_dir, 'trk2dictionary_c.cpp')
+    drv = os.path.join(HERE, 't2d_ref_driver.cpp')
+    if not os.path.exists(src):
+        return False
+    os.makedirs(REF_OUT, exist_ok=True)
+    inc = sysconfig.get_paths()['include']
+    cmd = ['g++', '-O2', '-ffp-contract=off', '-w', '-shared', '-fPIC', '-I', numpy.get_include(), '-I', inc,
+           '-I', src_dir, '-o', T2D_LIB + '.tmp', src, drv, '-lpthread']
+    if subprocess.run(cmd).returncode != 0:
+        return False
+    os.replace(T2D_LIB + '.tmp', T2D_LIB)
+    return True
+
+
 def main(argv=None) -> int:
     argv = sys.argv[1:] if argv is None else argv
     ok = generate() and compile_operator()
     print('oracle/_ref operator:', 'built' if ok else 'unavailable (no reference tree and no generated source)')
+    print('oracle/_ref trk2dictionary:', 'built' if compile_trk2dictionary() else 'unavailable (no reference tree)')
     if '--python' in argv:
         print('oracle/_ref python modules:', 'built' if build_python() else 'unavailable')
     return 0

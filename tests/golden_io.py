@@ -11,7 +11,9 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'golden')
 
 
 def case_names():
-    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, '*.npz')))
+    """Operator / solver cases (the voxeliser's t2d_*.npz fixtures have their own loader)."""
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, '*.npz'))
+                  if not os.path.basename(p).startswith('t2d_'))
 
 
 def load_case(name: str) -> dict:
