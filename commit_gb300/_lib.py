@@ -35,7 +35,8 @@ class CgbReg(ctypes.Structure):
 
 class CgbFistaParams(ctypes.Structure):
     _fields_ = [('tol_fun', c_f64), ('tol_x', c_f64), ('max_iter', c_i32), ('verbose', c_i32),
-                ('arith', c_i32), ('momentum_reuse', c_i32), ('x_ref', c_vp), ('trace', c_vp), ('trace_len', c_i32)]
+                ('arith', c_i32), ('momentum_reuse', c_i32), ('x_ref', c_vp), ('trace', c_vp), ('trace_len', c_i32),
+                ('graph', c_i32)]
 
 
 class CgbFistaResult(ctypes.Structure):

@@ -23,6 +23,9 @@ STAMP = os.path.join(BUILD, 'arch.txt')
 
 GENCODE = ['-gencode', 'arch=compute_103a,code=sm_103a']
 NVCC_FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '-Xcompiler', '-O2',
+              # host code: no fused multiply-adds, so the solver's host-side FP64 decisions are the
+              # same bits on every host architecture (and equal to the graph mode's device ones)
+              '-Xcompiler', '-ffp-contract=off',
               '--expt-relaxed-constexpr', '-diag-suppress', '128', '-I', os.path.join(ROOT, 'include')]
 
 

@@ -114,7 +114,8 @@ __device__ __forceinline__ double warp_sum(double v) {
 // proximals.pyx:103-134 for the pairwise-disjoint groups [g0, g1): warp per group
 __global__ void k_group_prox(double *__restrict__ x, int64_t nx, const int32_t *__restrict__ gidx,
                              const int64_t *__restrict__ gptr, const double *__restrict__ gw, int64_t g0, int64_t g1,
-                             double lam) {
+                             double lam, const double *__restrict__ plam) {
+    if (plam) lam = *plam;  // graph mode: lam follows the device step
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -242,6 +243,123 @@ int finalize(const double *partials, int nblocks, int nslots, double *out, cudaS
     return CGB_OK;
 }
 
+// ------------------------------------------------------------------ graph-captured FISTA
+// The whole iteration loop as one CUDA graph: a WHILE node runs the iterations, a nested
+// WHILE node the backtracking steps, an IF node the momentum + gradient of a continuing
+// iteration.  The decisions the host takes in Solver::run are taken by one-thread
+// controller kernels on device scalars (same expressions, no fused multiply-adds, so the
+// same bits), which set the conditional handles.  The host launches the graph once and
+// reads the final scalars.
+struct GState {
+    double step, told, prev_obj, qfval, curr_obj, reg_x, res_norm, abs_obj, rel_obj, abs_x, rel_x, c;
+    double tol_fun, tol_x;
+    double l1coef[4];
+    double group_coef;
+    int nterms, group_in_omega;
+    int it, crit, backtracks, max_iter;
+};
+
+__device__ __forceinline__ double g_omega(const GState &S, const double *h) {
+    double om = 0.0;
+    for (int k = 0; k < S.nterms; ++k) om = __dadd_rn(om, __dmul_rn(S.l1coef[k], h[5 + k]));
+    if (S.group_in_omega) om = __dadd_rn(om, __dmul_rn(S.group_coef, h[11]));
+    return om;
+}
+
+// qfval of the iteration (solvers.py:309-313): the residual of the gradient pass
+__global__ void k_ctl_begin(GState *S, const double *h) {
+    const double r = __dsqrt_rn(h[12]);
+    S->qfval = S->it == 1 ? S->prev_obj : __dmul_rn(__dmul_rn(0.5, r), r);
+}
+
+// objective and quadratic model of the evaluated x (solvers.py:315-333); on failure of the
+// sufficient-decrease test shrink the step and ask for another evaluation
+__global__ void k_ctl_judge(GState *S, const double *h, cudaGraphConditionalHandle bt) {
+    const double reg = g_omega(*S, h);
+    const double d2 = __dsqrt_rn(h[2]);
+    const double q = __dadd_rn(__dadd_rn(__dadd_rn(S->qfval, h[1]), __dmul_rn(__ddiv_rn(0.5, S->step), __dmul_rn(d2, d2))),
+                               reg);
+    const double rn = __dsqrt_rn(h[0]);
+    const double cur = __dadd_rn(__dmul_rn(__dmul_rn(0.5, rn), rn), reg);
+    S->reg_x = reg;
+    S->res_norm = rn;
+    S->curr_obj = cur;
+    if (cur > q) {
+        S->step = __dmul_rn(0.9, S->step);
+        S->backtracks += 1;
+        cudaGraphSetConditional(bt, 1);
+    } else {
+        cudaGraphSetConditional(bt, 0);
+    }
+}
+
+// stopping tests (solvers.py:335-357) and the FISTA coefficients (solvers.py:359-368)
+__global__ void k_ctl_stop(GState *S, const double *h, cudaGraphConditionalHandle hmain,
+                           cudaGraphConditionalHandle hcont) {
+    const double eps = 2.220446049250313e-16;
+    const double a = fabs(__dsub_rn(S->curr_obj, S->prev_obj));
+    S->abs_obj = a;
+    S->rel_obj = __ddiv_rn(a, S->curr_obj);
+    S->abs_x = __dsqrt_rn(h[3]);
+    S->rel_x = __ddiv_rn(S->abs_x, __dadd_rn(__dsqrt_rn(h[4]), eps));
+    int crit = -1;
+    if (S->abs_obj < eps) crit = 0;
+    else if (S->rel_obj < S->tol_fun) crit = 1;
+    else if (S->abs_x < eps) crit = 2;
+    else if (S->rel_x < S->tol_x) crit = 3;
+    else if (S->it >= S->max_iter) crit = 4;
+    if (crit >= 0) {
+        S->crit = crit;
+        cudaGraphSetConditional(hmain, 0);
+        cudaGraphSetConditional(hcont, 0);
+        return;
+    }
+    const double t = __dmul_rn(0.5, __dadd_rn(1.0, __dsqrt_rn(__dadd_rn(1.0, __dmul_rn(__dmul_rn(4.0, S->told), S->told)))));
+    S->c = __ddiv_rn(__dsub_rn(S->told, 1.0), t);
+    S->told = t;
+    S->prev_obj = S->curr_obj;
+    S->it += 1;
+    cudaGraphSetConditional(hcont, 1);
+}
+
+__global__ void k_prox_elem_dev(double *__restrict__ xo, const double *__restrict__ xi, const double *__restrict__ grad,
+                                const GState *__restrict__ S, RegDev R, int64_t n) {
+    const double s = S->step;
+    R.lam_ic = __dmul_rn(s, R.lam_ic);
+    R.lam_ec = __dmul_rn(s, R.lam_ec);
+    R.lam_iso = __dmul_rn(s, R.lam_iso);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double v = __dsub_rn(xi[i], __dmul_rn(s, grad[i]));
+        if (i >= R.sISO && i < R.sISO + R.nISO) {
+            if (R.reg_iso == CGB_REG_LASSO) v = soft(v, R.weighted_iso ? R.w[i] * R.lam_iso : R.lam_iso);
+            if (R.nn_iso && v <= 0.0) v = 0.0;
+        } else if (i >= R.sEC && i < R.sEC + R.nEC) {
+            if (R.reg_ec == CGB_REG_LASSO) v = soft(v, R.lam_ec);
+            if (R.nn_ec && v <= 0.0) v = 0.0;
+        } else if (i >= R.sIC && i < R.sIC + R.nIC) {
+            if (R.reg_ic == CGB_REG_LASSO || R.reg_ic == CGB_REG_SPARSE_GROUP_LASSO)
+                v = soft(v, R.weighted_ic ? R.w[i] * R.lam_ic : R.lam_ic);
+            if (R.nn_ic && (R.reg_ic == CGB_REG_NONE || R.reg_ic == CGB_REG_LASSO) && v <= 0.0) v = 0.0;
+        }
+        xo[i] = v;
+    }
+}
+
+__global__ void k_momentum_dev(double *__restrict__ xh, const double *__restrict__ x, double *__restrict__ p,
+                               const GState *__restrict__ S, int64_t n) {
+    const double c = S->c;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double xi = x[i];
+        xh[i] = __dadd_rn(xi, __dmul_rn(c, __dsub_rn(xi, p[i])));
+        p[i] = xi;
+    }
+}
+
+// lam = lam_base * step for the group prox of the graph (the host path passes it directly)
+__global__ void k_scale_lam(const GState *__restrict__ S, double lam_base, double *__restrict__ out) {
+    *out = __dmul_rn(S->step, lam_base);
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ solver workspace
@@ -285,6 +403,8 @@ struct Solver {
     bool mixed = false;
     bool batch_member = false;  // one problem of a batch: row buffers belong to the batch
     double *dsc = nullptr;      // this problem's 16 device scalars
+    const GState *gdev = nullptr;  // graph mode: the device-side state (step) kernels read
+    double *glam = nullptr;        // graph mode: device copy of the group-prox lambda
 
     int init() {
         const int64_t nc = op->ncols, nr = op->nrows;
@@ -377,11 +497,21 @@ struct Solver {
     int prox(double *xo, const double *xi, const double *grad, double a, double s) {
         const int64_t nc = op->ncols;
         if (nc == 0) return CGB_OK;
-        k_prox_elem<<<elem_grid(op, nc), kBlock, 0, st>>>(xo, xi, grad, a, regdev(s), nc);
+        if (gdev) {
+            // graph mode: step (= a = s) read on the device
+            k_prox_elem_dev<<<elem_grid(op, nc), kBlock, 0, st>>>(xo, xi, grad, gdev, regdev(1.0), nc);
+        } else {
+            k_prox_elem<<<elem_grid(op, nc), kBlock, 0, st>>>(xo, xi, grad, a, regdev(s), nc);
+        }
         CGB_CUDA(cudaGetLastError());
         const cgb_reg &R = *reg;
         if (has_group_prox) {
-            const double lam = s * (R.reg_ic == CGB_REG_GROUP_LASSO ? R.lambda_ic : R.lambda_ic_group);
+            const double lam_base = R.reg_ic == CGB_REG_GROUP_LASSO ? R.lambda_ic : R.lambda_ic_group;
+            const double lam = gdev ? lam_base : s * lam_base;
+            if (gdev && lam_base != 0.0) {
+                k_scale_lam<<<1, 1, 0, st>>>(gdev, lam_base, glam);
+                CGB_CUDA(cudaGetLastError());
+            }
             if (lam != 0.0) {
                 for (int64_t k = 0; k < R.nlevels; ++k) {
                     const int64_t g0 = R.level_ptr[k], g1 = R.level_ptr[k + 1];
@@ -389,7 +519,7 @@ struct Solver {
                     int64_t blocks = ((g1 - g0) * 32 + kBlock - 1) / kBlock;
                     if (blocks > op->nsm * 8) blocks = op->nsm * 8;
                     k_group_prox<<<(int)blocks, kBlock, 0, st>>>(xo, op->ncols, R.group_idx, R.group_ptr, R.group_w, g0, g1,
-                                                                lam);
+                                                                lam, gdev ? glam : nullptr);
                     CGB_CUDA(cudaGetLastError());
                 }
             }
@@ -602,6 +732,185 @@ struct Solver {
         res->backtracks = backtracks;
         res->operator_calls = calls;
         CGB_CUDA(cudaStreamSynchronize(st));
+        return CGB_OK;
+    }
+
+    // --------------------------------------------------------------- graph mode
+    // One evaluation of x = prox(xhat - step*grad) with its statistics and objective.
+    int eval_dev(double *x) {
+        CGB_TRY(prox(x, ws.xhat, ws.grad, 0.0, 0.0));
+        CGB_TRY(stats(x, ws.xhat, ws.grad, ws.prev));
+        return objective(x, -1);
+    }
+
+    // add a conditional node at the current point of the capture on `cap`, capture its body
+    // on `body_st` with f(), and continue the capture after the node
+    template <class F>
+    int conditional(cudaStream_t cap, cudaStream_t body_st, cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type,
+                    F &&f) {
+        cudaStreamCaptureStatus status;
+        cudaGraph_t cg;
+        const cudaGraphNode_t *deps = nullptr;
+        size_t ndeps = 0;
+        CGB_CUDA(cudaStreamGetCaptureInfo(cap, &status, nullptr, &cg, &deps, nullptr, &ndeps));
+        cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+        np.conditional.handle = h;
+        np.conditional.type = type;
+        np.conditional.size = 1;
+        cudaGraphNode_t node;
+        CGB_CUDA(cudaGraphAddNode(&node, cg, deps, nullptr, ndeps, &np));
+        cudaGraph_t body = np.conditional.phGraph_out[0];
+        const cudaStream_t outer = st;
+        st = body_st;
+        CGB_CUDA(cudaStreamBeginCaptureToGraph(body_st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        int rc = f();
+        cudaGraph_t done = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(body_st, &done);
+        st = outer;
+        CGB_TRY(rc);
+        CGB_CUDA(e);
+        CGB_CUDA(cudaStreamUpdateCaptureDependencies(cap, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+        return CGB_OK;
+    }
+
+    // FISTA with the iteration loop as one graph launch (no momentum reuse, no trace).
+    int run_graph(double *x, cgb_fista_result *res) {
+        const int64_t nc = op->ncols;
+        double *h = op->h_scal;
+        // initialisation on the host path (solvers.py:260-286), as in run()
+        CGB_CUDA(cudaMemcpyAsync(ws.xhat, x, nc * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        CGB_TRY(gradient(ws.xhat, ws.grad, -1, -1, 0.0, 0.0));
+        CGB_TRY(prox(ws.xhat, ws.xhat, nullptr, 0.0, 1.0));
+        CGB_TRY(stats(ws.xhat, nullptr, nullptr, nullptr));
+        CGB_TRY(fetch(h));
+        double res_norm = sqrt(h[12]);
+        const double prev_obj = 0.5 * res_norm * res_norm + omega_from(h);
+        CGB_CUDA(cudaMemcpyAsync(ws.prev, ws.xhat, nc * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        {
+            int g = 0;
+            k_dot<<<elem_grid(op, nc), kBlock, 0, st>>>(ws.grad, ws.grad, nc, ws.pstats);
+            CGB_CUDA(cudaGetLastError());
+            CGB_TRY(finalize(ws.pstats, elem_grid(op, nc), 1, op->dscal + 13, st));
+            if (mixed) {
+                CGB_TRY(launch_resnorm_mix(op, ws.grad, nullptr, ws.sqw32, op->partials, nullptr, nullptr, st,
+                                           prm->arith, &g));
+            } else {
+                CGB_TRY(launch_resnorm_grid(op, ws.grad, nullptr, sqw, op->partials, nullptr, st, prm->arith, &g));
+            }
+            calls++;
+            if (g > 0) {
+                CGB_TRY(finalize(op->partials, g, 1, op->dscal + 14, st));
+            } else {
+                CGB_CUDA(cudaMemsetAsync(op->dscal + 14, 0, sizeof(double), st));
+            }
+            CGB_TRY(fetch(h));
+        }
+        const double Ln = sqrt(h[14]) / sqrt(h[13]);
+        GState G;
+        memset(&G, 0, sizeof(G));
+        G.step = 1.9 / (Ln * Ln);
+        G.told = 1.0;
+        G.prev_obj = prev_obj;
+        G.tol_fun = prm->tol_fun;
+        G.tol_x = prm->tol_x;
+        G.nterms = terms.n;
+        for (int k = 0; k < terms.n; ++k) G.l1coef[k] = l1coef[k];
+        G.group_in_omega = group_in_omega;
+        G.group_coef = group_omega_coef;
+        G.it = 1;
+        G.crit = 4;
+        G.max_iter = prm->max_iter;
+        GState *gs = nullptr;
+        CGB_TRY(ws_alloc(&gs, 1, st));
+        CGB_TRY(ws_alloc(&glam, 1, st));
+        CGB_CUDA(cudaMemcpyAsync(gs, &G, sizeof(G), cudaMemcpyHostToDevice, st));
+        CGB_CUDA(cudaStreamSynchronize(st));
+        gdev = gs;
+        // graph: WHILE(main) { begin; eval; judge; WHILE(bt) { eval; judge }; stop; IF(cont) { momentum; gradient } }
+        cudaStream_t s0 = nullptr, s1 = nullptr, s2 = nullptr;
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        const cudaStream_t user = st;
+        double *d = op->dscal;
+        auto build = [&]() -> int {
+            CGB_CUDA(cudaStreamCreateWithFlags(&s0, cudaStreamNonBlocking));
+            CGB_CUDA(cudaStreamCreateWithFlags(&s1, cudaStreamNonBlocking));
+            CGB_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+            CGB_CUDA(cudaGraphCreate(&graph, 0));
+            cudaGraphConditionalHandle hmain, hbt, hcont;
+            CGB_CUDA(cudaGraphConditionalHandleCreate(&hmain, graph, 1, cudaGraphCondAssignDefault));
+            CGB_CUDA(cudaGraphConditionalHandleCreate(&hbt, graph, 0, cudaGraphCondAssignDefault));
+            CGB_CUDA(cudaGraphConditionalHandleCreate(&hcont, graph, 0, cudaGraphCondAssignDefault));
+            cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+            np.conditional.handle = hmain;
+            np.conditional.type = cudaGraphCondTypeWhile;
+            np.conditional.size = 1;
+            cudaGraphNode_t wnode;
+            CGB_CUDA(cudaGraphAddNode(&wnode, graph, nullptr, nullptr, 0, &np));
+            cudaGraph_t body = np.conditional.phGraph_out[0];
+            st = s0;
+            CGB_CUDA(cudaStreamBeginCaptureToGraph(s0, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+            int rc = [&]() -> int {
+                k_ctl_begin<<<1, 1, 0, s0>>>(gs, d);
+                CGB_CUDA(cudaGetLastError());
+                CGB_TRY(eval_dev(x));
+                k_ctl_judge<<<1, 1, 0, s0>>>(gs, d, hbt);
+                CGB_CUDA(cudaGetLastError());
+                CGB_TRY(conditional(s0, s1, hbt, cudaGraphCondTypeWhile, [&]() -> int {
+                    CGB_TRY(eval_dev(x));
+                    k_ctl_judge<<<1, 1, 0, st>>>(gs, d, hbt);
+                    CGB_CUDA(cudaGetLastError());
+                    return CGB_OK;
+                }));
+                k_ctl_stop<<<1, 1, 0, s0>>>(gs, d, hmain, hcont);
+                CGB_CUDA(cudaGetLastError());
+                CGB_TRY(conditional(s0, s2, hcont, cudaGraphCondTypeIf, [&]() -> int {
+                    k_momentum_dev<<<elem_grid(op, nc), kBlock, 0, st>>>(ws.xhat, x, ws.prev, gs, nc);
+                    CGB_CUDA(cudaGetLastError());
+                    return gradient(ws.xhat, ws.grad, -1, -1, 0.0, 0.0);
+                }));
+                return CGB_OK;
+            }();
+            cudaGraph_t done = nullptr;
+            const cudaError_t e = cudaStreamEndCapture(s0, &done);
+            st = user;
+            CGB_TRY(rc);
+            CGB_CUDA(e);
+            CGB_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+            return CGB_OK;
+        };
+        int rc = build();
+        st = user;
+        if (rc == CGB_OK) {
+            const cudaError_t e = cudaGraphLaunch(exec, st);
+            if (e != cudaSuccess) rc = cuda_fail(e, "cudaGraphLaunch");
+        }
+        if (rc == CGB_OK) {
+            cudaMemcpyAsync(&G, gs, sizeof(G), cudaMemcpyDeviceToHost, st);
+            const cudaError_t e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) rc = cuda_fail(e, "graph FISTA");
+        }
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        for (cudaStream_t q : {s0, s1, s2})
+            if (q) cudaStreamDestroy(q);
+        gdev = nullptr;
+        cudaFreeAsync(gs, st);
+        cudaFreeAsync(glam, st);
+        glam = nullptr;
+        CGB_TRY(rc);
+        res->residual = 0.5 * G.res_norm * G.res_norm;
+        res->regterm = G.reg_x;
+        res->cost_function = G.curr_obj;
+        res->abs_cost = G.abs_obj;
+        res->rel_cost = G.rel_obj;
+        res->abs_x = G.abs_x;
+        res->rel_x = G.rel_x;
+        res->iterations = G.it;
+        res->stopping_criterion = G.crit;
+        res->backtracks = G.backtracks;
+        // init: 2 (gradient) + 1 (Rayleigh quotient); per evaluation 1; per gradient 2
+        res->operator_calls = calls + (G.it + G.backtracks) + 2 * (G.it - 1);
         return CGB_OK;
     }
 };
@@ -1033,6 +1342,8 @@ int cgb_fista_run(cgb_op *op, const double *y, const double *sqrt_w, const cgb_r
     if ((reg->reg_ic == CGB_REG_GROUP_LASSO || reg->reg_ic == CGB_REG_SPARSE_GROUP_LASSO) && reg->ngroups > 0 &&
         (!reg->level_ptr || reg->nlevels < 1))
         return fail(CGB_ERR_INVALID, "group regulariser needs a level schedule");
+    if (params->graph && (params->momentum_reuse || (params->trace && params->x_ref) || params->verbose == 4))
+        return fail(CGB_ERR_UNSUPPORTED, "graph mode runs without momentum reuse, trace or verbose output");
     DevGuard g(op->device);
     Solver S;
     S.op = op;
@@ -1042,7 +1353,7 @@ int cgb_fista_run(cgb_op *op, const double *y, const double *sqrt_w, const cgb_r
     S.prm = params;
     S.st = (cudaStream_t)stream;
     CGB_TRY(S.init());
-    return S.run(x, result);
+    return params->graph ? S.run_graph(x, result) : S.run(x, result);
 }
 
 int cgb_fista_batch_run(cgb_op *op, const double *y, const double *sqrt_w, const cgb_reg *regs, int nprob,
@@ -1215,7 +1526,7 @@ int cgb_prox_group_lasso(double *x, int64_t nx, const int32_t *group_idx, const 
         if (g1 <= g0) continue;
         int64_t blocks = ((g1 - g0) * 32 + kBlock - 1) / kBlock;
         if (blocks > 4096) blocks = 4096;
-        k_group_prox<<<(int)blocks, kBlock, 0, st>>>(x, nx, group_idx, group_ptr, group_w, g0, g1, lam);
+        k_group_prox<<<(int)blocks, kBlock, 0, st>>>(x, nx, group_idx, group_ptr, group_w, g0, g1, lam, nullptr);
         CGB_CUDA(cudaGetLastError());
     }
     return CGB_OK;

@@ -204,8 +204,12 @@ def evaluate_model(y, A, x, regularisation=None):
 
 
 def solve(y, A, At, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, verbose=True, x0=None, regularisation=None,
-          confidence_array=None, arith=None, momentum_reuse=True, x_ref=None):
-    """solvers.py:218-241: regularised least squares by FISTA, on the GPU."""
+          confidence_array=None, arith=None, momentum_reuse=True, x_ref=None, graph=False):
+    """solvers.py:218-241: regularised least squares by FISTA, on the GPU.
+
+    graph=True runs the iteration loop as one CUDA graph launch whose backtracking and
+    stopping decisions are taken on the device (conditional graph nodes); it implies
+    momentum_reuse=False and takes no x_ref / verbose output."""
     if regularisation is None:
         spec = _no_reg_spec(A.shape[1])
     else:
@@ -216,7 +220,9 @@ def solve(y, A, At, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, verbose=True, x0=No
     if confidence_array is not None:
         sqrt_W = np.sqrt(np.asarray(confidence_array)) if not isinstance(confidence_array, torch.Tensor) \
             else torch.sqrt(confidence_array)
-    return _fista(y, A, spec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, arith, momentum_reuse, x_ref)
+    if graph:
+        momentum_reuse = False
+    return _fista(y, A, spec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, arith, momentum_reuse, x_ref, graph)
 
 
 def fista(y, A, At, omega, prox, sqrt_W=None, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, verbose=False, x0=None,
@@ -240,7 +246,8 @@ def _is_identity(prox, n) -> bool:
     return out is not None and np.array_equal(np.asarray(out), probe)
 
 
-def _fista(y, A, spec: RegSpec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, arith, momentum_reuse, x_ref=None):
+def _fista(y, A, spec: RegSpec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, arith, momentum_reuse, x_ref=None,
+           graph=False):
     """With x_ref given, details['trace'] holds, per accepted iteration, the seconds since
     the solve started and |x_k - x_ref| / |x_ref|."""
     if not isinstance(A, LinearOperator):
@@ -267,6 +274,9 @@ def _fista(y, A, spec: RegSpec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, a
     reg, keep = spec.cstruct(dev)
     prm = _lib.CgbFistaParams(float(tol_fun), float(tol_x), int(max_iter), int(verbose) if verbose is not True else 1,
                               _lib.ARITH[arith or A.arith], int(bool(momentum_reuse)))
+    prm.graph = int(bool(graph))
+    if graph and (x_ref is not None or verbose == 4):
+        raise ValueError('graph mode takes no x_ref and no verbose output')
     trace = None
     if x_ref is not None:
         xr = torch.as_tensor(np.asarray(x_ref, dtype=np.float64) if not isinstance(x_ref, torch.Tensor) else x_ref,

@@ -195,6 +195,8 @@ typedef struct {
     const double *x_ref;
     double *trace;
     int trace_len;
+    int graph;            /* 1: the iteration loop runs as one CUDA graph launch with device-side */
+                          /* decisions (conditional nodes); needs momentum_reuse 0, no trace    */
 } cgb_fista_params;
 
 typedef struct {

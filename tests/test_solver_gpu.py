@@ -98,3 +98,26 @@ def test_mixed_fista_and_refinement(arith, tol):
                                  arith=arith, refine_max_iter=n2)
     assert dm['iterations'] == n1 + n2
     assert dm['cost_function'] <= d_ref['cost_function'] * (1 + 1e-9)
+
+
+@pytest.mark.parametrize('name,variant', [(n, v) for n, v in _fit_cases() if n in ('szb', 'multi_rf', 'eval_gaps')])
+def test_graph_mode_matches_host_loop(name, variant):
+    """The iteration loop as one CUDA graph (device-side backtracking and stopping) gives the
+    host-driven loop's iterates bit for bit, and the reference's fit."""
+    from commit_gb300 import solvers
+    from commit_gb300.operator import LinearOperator
+    c = G.load_case(name)
+    f = c['fits'][variant]
+    A = LinearOperator(c['D'], c['K'], None, nolut=c['nolut'])
+    kw = dict(tol_fun=1e-5, tol_x=1e-7, max_iter=f['details']['iterations'], verbose=0,
+              confidence_array=f['conf'], momentum_reuse=False)
+    xh, dh = solvers.solve(c['y_obs'], A, A.T, regularisation=solvers.init_regularisation(G.fresh_reg(f['reg'])), **kw)
+    xg, dg = solvers.solve(c['y_obs'], A, A.T, regularisation=solvers.init_regularisation(G.fresh_reg(f['reg'])),
+                           graph=True, **kw)
+    assert dg['iterations'] == dh['iterations'] == f['details']['iterations']
+    assert dg['stopping_criterion'] == dh['stopping_criterion'] == f['details']['stopping_criterion']
+    assert dg['backtracks'] == dh['backtracks']
+    assert np.array_equal(xg, xh)
+    assert G.rel(xg, f['x']) <= 1e-8
+    for k in ('residual', 'regterm', 'cost_function', 'abs_cost', 'rel_cost', 'abs_x', 'rel_x'):
+        assert dg[k] == dh[k], k
