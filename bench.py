@@ -42,6 +42,9 @@ def parse():
     p.add_argument('--arith', default='ff', choices=['ff', 'f64', 'bf16', 'fp16', 'f32'])
     p.add_argument('--fista', action='store_true', help='FISTA time-to-tolerance, plain vs mixed + refinement')
     p.add_argument('--fista-iters', type=int, default=1500)
+    p.add_argument('--demo', action='store_true',
+                   help='demo-scale case (5k streamlines, nS=66): A*x, A\'y and 200 FISTA nnls iterations, '
+                        'host-driven loop vs graph-captured loop, next to the reference CPU operator')
     p.add_argument('--batch', action='store_true',
                    help='regularisation paths: 8 tractograms x 16 lambdas, batched BF16 vs sequential plain solves')
     p.add_argument('--batch-tracts', type=int, default=8, help='number of tractograms of the batched workload')
@@ -470,10 +473,74 @@ def run_batch(args):
     return 0
 
 
+def run_demo(args):
+    """The 5k-streamline demo case (grid 32x32x16, nS = 66): operator pair time, and 200 FISTA
+    nnls iterations with the host-driven loop (momentum reuse off and on) and with the loop
+    captured as one CUDA graph.  Prints one JSON line."""
+    import torch
+    from commit_gb300 import solvers, synth
+    from commit_gb300.operator import LinearOperator
+    dev = torch.device('cuda', torch.cuda.current_device())
+    spec = synth.SPECS['demo_5k']
+    D, K = synth.make_dictionary(spec, device='cuda')
+    A = LinearOperator(D, K, None, device=dev.index)
+    x = torch.from_numpy(synth.make_x(A.nCOLS, 1)).to(dev)
+    y = torch.from_numpy(synth.make_signal(A.dot(x).cpu().numpy(), 2)).to(dev)
+    yy = torch.empty(A.nROWS, dtype=torch.float64, device=dev)
+    g = torch.empty(A.nCOLS, dtype=torch.float64, device=dev)
+    st = torch.cuda.current_stream(dev)
+    for _ in range(max(3, args.warmup)):
+        A.dot(x, out=yy)
+        A.T.dot(yy, out=g)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    n = 200
+    for _ in range(n):
+        A.dot(x, out=yy)
+        A.T.dot(yy, out=g)
+    e1.record(st)
+    torch.cuda.synchronize()
+    pair_ms = e0.elapsed_time(e1) / n
+    rp = {'startIC': 0, 'sizeIC': A.ICnSTR * A.ICnRF, 'startEC': A.ICnSTR * A.ICnRF, 'sizeEC': A.ECn * A.ECnRF,
+          'startISO': A.ICnSTR * A.ICnRF + A.ECn * A.ECnRF, 'sizeISO': A.ISOn * A.ISOnRF,
+          'regIC': None, 'regEC': None, 'regISO': None, 'nnIC': True, 'nnEC': True, 'nnISO': True,
+          'dictIC_params': None, 'dictEC_params': None, 'dictISO_params': None}
+    out = {}
+    for name, kw in (('host_loop_reuse', dict(momentum_reuse=True)), ('host_loop', dict(momentum_reuse=False)),
+                     ('graph', dict(graph=True))):
+        solvers.solve(y, A, A.T, tol_fun=0.0, tol_x=0.0, max_iter=5, verbose=0,
+                      regularisation=solvers.init_regularisation(dict(rp)), **kw)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        xs, d = solvers.solve(y, A, A.T, tol_fun=0.0, tol_x=0.0, max_iter=n, verbose=0,
+                              regularisation=solvers.init_regularisation(dict(rp)), **kw)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        out[name] = {'seconds': dt, 'ms_per_iteration': 1000.0 * dt / n, 'iterations': d['iterations'],
+                     'cost_function': d['cost_function']}
+    cpu = None
+    if not args.no_cpu:
+        cpu = cpu_reference(D, K, 1.0, 20, 2)
+    res = {'metric': 'demo case: A*x+A\'y pair time and FISTA ms/iteration (host loop vs CUDA graph)',
+           'unit': 'ms', 'higher_is_better': False, 'data': 'synthetic',
+           'config': {'workload': f'demo_5k: {spec.n_fibers} streamlines, grid 32x32x16, '
+                                  f'{int(D["IC"]["nVOX"])} voxels, {int(D["IC"]["n"])} segments, nS=66',
+                      'fista': '200 nnls iterations, tolerances off'},
+           'pair_ms': pair_ms, 'pairs_per_s': 1000.0 / pair_ms, 'fista': out,
+           'graph_speedup_vs_host_loop': out['host_loop']['seconds'] / out['graph']['seconds']}
+    if cpu is not None:
+        res['cpu_baseline'] = cpu
+    print(json.dumps(res))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == 'reference':
         return run_reference(args)
+    if args.demo:
+        return run_demo(args)
     if args.batch:
         return run_batch(args)
     return run_ours(args)
