@@ -30,6 +30,13 @@ sys.path.insert(0, ROOT)
 
 METRIC = 'A·x+Aᵀx operator pairs/s (1M-streamline workload)'
 
+# DRAM bytes (read + write) per launch from one ncu capture of the same command
+# (`ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum
+# --clock-control none -k regex:"k_(forward_p|adjoint_p|fibre_sum)" ... python bench.py --steps 1
+# --warmup 1 --no-e2e --no-cpu`, one pass, full workload; profiles/operator_ff_hcp1m.md).
+# Keyed by (workload, streamlines, arith); the A' entry is pass 1 + pass 2.
+MEASURED_TRAFFIC = {('hcp_1m', 1000000, 'ff'): {'forward': 2642033408, 'adjoint': None}}
+
 
 def parse():
     p = argparse.ArgumentParser()
@@ -228,6 +235,13 @@ def workload_config(spec, D, K, args):
             'arith': args.arith, 'l2': 'inputs larger than L2 (y is nV*nS f64), no flush'}
 
 
+def traffic_for(args, spec, dom: str):
+    t = MEASURED_TRAFFIC.get((args.workload, spec.n_fibers, args.arith))
+    if not t:
+        return None
+    return t['adjoint'] if dom.startswith('adjoint') else t['forward']
+
+
 def run_reference(args):
     ws, rank, local = dist_env()
     if rank != 0:
@@ -308,10 +322,11 @@ def run_ours(args):
            'data': 'synthetic', 'config': workload_config(spec, D, K, args),
            'roofline': {'bound': 'hbm', 'kernel': dom, 'achieved': achieved, 'peak': peaks['hbm_gbs'],
                         'unit': 'GB/s', 'frac': achieved / peaks['hbm_gbs'], 'peak_src': peaks['src'],
-                        'traffic': None, 'algorithmic_bytes_per_launch': nbytes,
+                        'traffic': traffic_for(args, spec, dom), 'algorithmic_bytes_per_launch': nbytes,
                         'forward_ms': fwd_ms, 'adjoint_ms': adj_ms,
                         'fma_per_product': nfma, 'achieved_gfma_s': nfma / (dom_ms / 1000.0) / 1e9},
-           'clocks': clk, 'gpu_launches': args.steps * (1 + 2), 'setup_s': {'generate': tgen}}
+           'clocks': clk, 'gpu_launches': args.steps * (1 + 2), 'setup_s': {'generate': tgen},
+           'occupancy_tuning': A.occupancy()}
     # end to end through the public API on pinned host buffers
     if not args.no_e2e and not reduced:
         xh = torch.empty(ncols, dtype=torch.float64, pin_memory=True).numpy()

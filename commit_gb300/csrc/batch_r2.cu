@@ -55,9 +55,9 @@ struct AdjR {
     double *partials;
     cudaStream_t st;
     int *grid_out;
-    template <int L, int N>
-    int run() {
-        auto kern = k_adjoint_R<LT, L, N, 2>;
+    template <int L, int N, int MINB>
+    int launch() {
+        auto kern = k_adjoint_R<LT, L, N, 2, MINB>;
         int g = 0;
         CGB_TRY(grid_for_kernel(kern, 0, op->nsm, op->nV, kBlock / L, &g));
         if (g > reduction_blocks(op)) g = reduction_blocks(op);
@@ -65,6 +65,10 @@ struct AdjR {
         CGB_CUDA(cudaGetLastError());
         if (grid_out) *grid_out = g;
         return CGB_OK;
+    }
+    template <int L, int N>
+    int run() {
+        return occ_launch(op, kOccAdjR2, st, [&] { return launch<L, N, 1>(); }, [&] { return launch<L, N, 3>(); });
     }
 };
 

@@ -94,6 +94,8 @@ struct cgb_op {
     void *gstate;                   // LUT-gradient streams (lutgrad.cu), built on first use
     int batch_rhs;                  // vectors per multi-right-hand-side pass (0: not tuned)
     int batch_reuse;                // batched FISTA momentum reuse chosen by timing (0: not tuned, 1 off, 2 on)
+    int occ_choice[16];             // occupancy build per tuned kernel (0: not tuned, 1 or 2), see occ_launch
+    float occ_ms[16][2];            // the two builds' times measured by the tuning
     uint32_t *vox_ptr, *seg_f, *eval, *fib_ptr, *fib_perm, *ec_ptr, *ec_col, *iso_ptr, *iso_col;
     uint16_t *seg_o, *ec_o;
     float *seg_l;
@@ -143,4 +145,44 @@ int launch_adjoint_R(cgb_op *op, int R, const RhsPtrs &V, int in_mode, const flo
                      double *partials, cudaStream_t st, int *grid);
 int fibre_sum32_from(cgb_op *op, const float *scr, double *xout, cudaStream_t st);
 int convert_f32_to_f64(const float *in, double *out, int64_t n, cudaStream_t st);
+
+// ------------------------------------------------------------------ occupancy autotuning
+// A tuned kernel has two builds: __launch_bounds__ min-blocks 1 (registers as the compiler
+// wants) and a higher min-blocks (fewer registers, more resident warps, possibly a few
+// spills).  On the first call for a handle, outside stream capture, both builds run twice
+// on the call's own arguments (every output is overwritten by the real launch that
+// follows) and the faster build of the second round is kept on the handle.  Both builds
+// do the same arithmetic in the same order, so results do not depend on the choice.
+enum OccSlot { kOccFwdFF = 0, kOccAdjFF = 1, kOccAdjMix = 2 /* + arith - BF16 */, kOccAdjR2 = 5, kOccSlots = 16 };
+
+template <class FA, class FB>
+int occ_launch(cgb_op *op, int slot, cudaStream_t st, FA &&a, FB &&b) {
+    int &c = op->occ_choice[slot];
+    if (c == 0) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        CGB_CUDA(cudaStreamIsCapturing(st, &cs));
+        if (cs != cudaStreamCaptureStatusNone) return a();
+        cudaEvent_t e[3];
+        for (auto &ev : e) CGB_CUDA(cudaEventCreate(&ev));
+        float ta = 0.f, tb = 0.f;
+        int rc = CGB_OK;
+        for (int rep = 0; rep < 2 && rc == CGB_OK; ++rep) {
+            cudaEventRecord(e[0], st);
+            rc = a();
+            cudaEventRecord(e[1], st);
+            if (rc == CGB_OK) rc = b();
+            cudaEventRecord(e[2], st);
+            cudaEventSynchronize(e[2]);
+            cudaEventElapsedTime(&ta, e[0], e[1]);
+            cudaEventElapsedTime(&tb, e[1], e[2]);
+        }
+        for (auto &ev : e) cudaEventDestroy(ev);
+        CGB_TRY(rc);
+        op->occ_ms[slot][0] = ta;
+        op->occ_ms[slot][1] = tb;
+        c = tb < ta ? 2 : 1;
+    }
+    return c == 2 ? b() : a();
+}
+
 }  // namespace cgb

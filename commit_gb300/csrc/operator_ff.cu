@@ -15,11 +15,11 @@ struct FwdPair {
     double *partials;
     cudaStream_t st;
     int *grid_out;
-    template <int L, int N>
-    int run() {
+    template <int L, int N, int MINB>
+    int launch() {
         const OpDev P = op->dev();
         const Comps C = make_comps(op);
-        auto kern = k_forward_p<L, N>;
+        auto kern = k_forward_p<L, N, MINB>;
         int g = 0;
         CGB_TRY(grid_for_kernel(kern, 0, op->nsm, op->nV, kBlock / L, &g));
         if (g > reduction_blocks(op)) g = reduction_blocks(op);
@@ -28,6 +28,10 @@ struct FwdPair {
         CGB_CUDA(cudaGetLastError());
         if (grid_out) *grid_out = g;
         return CGB_OK;
+    }
+    template <int L, int N>
+    int run() {
+        return occ_launch(op, kOccFwdFF, st, [&] { return launch<L, N, 1>(); }, [&] { return launch<L, N, 3>(); });
     }
 };
 
@@ -40,11 +44,11 @@ struct AdjPair {
     double *xout, *partials;
     cudaStream_t st;
     int *grid_out;
-    template <int L, int N>
-    int run() {
+    template <int L, int N, int MINB>
+    int launch() {
         const OpDev P = op->dev();
         const Comps C = make_comps(op);
-        auto kern = k_adjoint_p<L, N>;
+        auto kern = k_adjoint_p<L, N, MINB>;
         int g = 0;
         CGB_TRY(grid_for_kernel(kern, 0, op->nsm, op->nV, kBlock / L, &g));
         if (g > reduction_blocks(op)) g = reduction_blocks(op);
@@ -52,6 +56,10 @@ struct AdjPair {
         CGB_CUDA(cudaGetLastError());
         if (grid_out) *grid_out = g;
         return CGB_OK;
+    }
+    template <int L, int N>
+    int run() {
+        return occ_launch(op, kOccAdjFF, st, [&] { return launch<L, N, 1>(); }, [&] { return launch<L, N, 2>(); });
     }
 };
 

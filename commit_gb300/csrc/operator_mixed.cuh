@@ -203,8 +203,8 @@ __device__ __forceinline__ float batch_dots_mix(const Group<LPV> &G, const LT *_
 
 // A' pass 1.  in_mode 0: z = yin; 1: z = sqw*r, r = sqw*(A x - yobs) (FP64 norm partials);
 // 2: as 1 with A x = ca*ax_a + cb*ax_b.  IC terms -> scr (FP32), EC/ISO -> xout (FP64).
-template <class LT, int LPV, int NP>
-__global__ void __launch_bounds__(kBlock) k_adjoint_mix(const int nV, const int nS, const int64_t n,
+template <class LT, int LPV, int NP, int MINB = 1>
+__global__ void __launch_bounds__(kBlock, MINB) k_adjoint_mix(const int nV, const int nS, const int64_t n,
                                                         const __grid_constant__ CompsM<LT> C,
                                                         const float *__restrict__ yin, int in_mode,
                                                         const double *__restrict__ x, const float *__restrict__ yobs,

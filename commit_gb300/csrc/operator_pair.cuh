@@ -249,8 +249,8 @@ __device__ __forceinline__ void forward_row_p(const Comps &C, const Group<LPV> &
     }
 }
 
-template <int LPV, int NP>
-__global__ void __launch_bounds__(kBlock) k_forward_p(const OpDev P, const __grid_constant__ Comps C,
+template <int LPV, int NP, int MINB = 1>
+__global__ void __launch_bounds__(kBlock, MINB) k_forward_p(const OpDev P, const __grid_constant__ Comps C,
                                                       const double *__restrict__ x,
                                                       double *__restrict__ yout, double *__restrict__ axout,
                                                       const double *__restrict__ yobs, const double *__restrict__ sqw,
@@ -349,8 +349,8 @@ __device__ __forceinline__ double batch_dots_p(const Group<LPV> &G, const float 
 // A' pass 1 over all compartments.  Per batch, one dot product per run of equal
 // orientation; every item of the run takes that total: IC items write l*<L,z> to the
 // per-segment scratch stream, EC / ISO items write their column of xout.
-template <int LPV, int NP>
-__global__ void __launch_bounds__(kBlock) k_adjoint_p(const OpDev P, const __grid_constant__ Comps C,
+template <int LPV, int NP, int MINB = 1>
+__global__ void __launch_bounds__(kBlock, MINB) k_adjoint_p(const OpDev P, const __grid_constant__ Comps C,
                                                       const double *__restrict__ yin,
                                                       int in_mode, const double *__restrict__ x,
                                                       const double *__restrict__ yobs, const double *__restrict__ sqw,

@@ -176,6 +176,20 @@ class LinearOperator:
                 check(lib().cgb_op_set_arith(self._h.ptr, _lib.ARITH[self.arith]))
         return res
 
+    OCC_SLOTS = {'ff_forward': 0, 'ff_adjoint': 1, 'bf16_adjoint': 2, 'fp16_adjoint': 3, 'f32_adjoint': 4,
+                 'bf16x2_adjoint': 5}
+
+    def occupancy(self, set_to: dict | None = None) -> dict:
+        """Occupancy autotuning state per tuned kernel: {name: (choice, ms_build1, ms_build2)}
+        (choice 0 = not tuned yet).  ``set_to`` {name: 0|1|2} fixes (or resets) choices."""
+        out = {}
+        for name, slot in self.OCC_SLOTS.items():
+            c, a, b = ctypes.c_int32(), ctypes.c_float(), ctypes.c_float()
+            st = -1 if not set_to or name not in set_to else int(set_to[name])
+            check(lib().cgb_op_occupancy(self._h.ptr, slot, st, ctypes.byref(c), ctypes.byref(a), ctypes.byref(b)))
+            out[name] = (int(c.value), float(a.value), float(b.value))
+        return out
+
     def batch_width(self, set_to: int | None = None) -> int:
         """Vectors per multi-right-hand-side pass (0: chosen by timing on the next batched
         solve); ``set_to`` 0, 2 or 4 stores a value."""

@@ -158,3 +158,30 @@ def test_reduced_precision_operator(arith, tol):
     lhs = float(np.dot(A.dot(torch.from_numpy(xs).float().cuda(), arith=arith).double().cpu().numpy(), ys))
     rhs = float(np.dot(xs, A.T.dot(torch.from_numpy(ys).float().cuda(), arith=arith).double().cpu().numpy()))
     assert abs(lhs - rhs) <= 1e-4 * (abs(lhs) + abs(rhs))
+
+
+def test_occupancy_builds_give_identical_results():
+    """Both register builds of each tuned kernel compute the same operations in the same
+    order: forcing either gives bitwise-equal products (FP64 float-float and BF16 paths)."""
+    import torch
+    from commit_gb300 import synth
+    from commit_gb300.operator import LinearOperator
+    D, K = synth.make_dictionary(synth.scaled_spec('demo_5k', n_fibers=2000, n_b0=18,
+                                                   shells=[(1000.0, 90), (2000.0, 90), (3000.0, 90)]))
+    A = LinearOperator(D, K, None)
+    rng = np.random.default_rng(0)
+    x = torch.from_numpy(rng.uniform(0, 1, A.nCOLS)).cuda()
+    w = torch.from_numpy(rng.normal(size=A.nROWS)).cuda()
+    w32 = w.float()
+    res = {}
+    for c in (1, 2):
+        A.occupancy({k: c for k in A.OCC_SLOTS})
+        res[c] = (A.dot(x).cpu().numpy(), A.T.dot(w).cpu().numpy(), A.T.dot(w32, arith='bf16').cpu().numpy())
+    for a, b in zip(res[1], res[2]):
+        assert np.array_equal(a, b)
+    A.occupancy({k: 0 for k in A.OCC_SLOTS})
+    A.dot(x)
+    A.T.dot(w)
+    st = A.occupancy()
+    assert st['ff_forward'][0] in (1, 2) and st['ff_adjoint'][0] in (1, 2)
+    assert st['ff_forward'][1] > 0 and st['ff_forward'][2] > 0
