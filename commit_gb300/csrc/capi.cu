@@ -23,6 +23,56 @@ int check_lengths(const cgb_op *op, int adjoint, int64_t in_len, int64_t out_len
 }
 }  // namespace
 
+// Host-buffer pipeline for the float-float operator on large problems: the voxels are cut
+// into kPipe ranges; A writes the rows of range k while the rows of range k-1 are copied to
+// the host on a second stream, and A' copies the rows of range k+1 in while pass 1 runs on
+// range k (pass 2 follows once all ranges are in).  The copies of the row vector (the
+// large one) hide behind the computation.  Results are those of the one-shot path (the
+// same per-voxel computation).
+static constexpr int kPipe = 8;
+
+static bool pipelined(const cgb_op *op) {
+    return op->arith == CGB_ARITH_FF && op->ff_variant != 0 && !op->nolut && op->nV >= 4 * kPipe &&
+           op->nrows >= ((int64_t)1 << 22);
+}
+
+static int apply_host_pipelined(cgb_op *op, int adjoint, const double *in, int64_t in_len, double *out,
+                                int64_t out_len) {
+    if (!op->pipe_st[0]) {
+        for (int i = 0; i < 2; ++i) CGB_CUDA(cudaStreamCreateWithFlags(&op->pipe_st[i], cudaStreamNonBlocking));
+        for (int k = 0; k < kPipe; ++k) CGB_CUDA(cudaEventCreateWithFlags(&op->pipe_ev[k], cudaEventDisableTiming));
+    }
+    cudaStream_t sc = op->pipe_st[0], sx = op->pipe_st[1];
+    const int nS = op->nS;
+    auto vb = [&](int k) { return (int)((int64_t)op->nV * k / kPipe); };
+    if (!adjoint) {
+        CGB_CUDA(cudaMemcpyAsync(op->d_in, in, in_len * sizeof(double), cudaMemcpyHostToDevice, sc));
+        for (int k = 0; k < kPipe; ++k) {
+            const int v0 = vb(k), v1 = vb(k + 1);
+            CGB_TRY(forward_ff_range(op, op->d_in, op->d_out, v0, v1, sc));
+            CGB_CUDA(cudaEventRecord(op->pipe_ev[k], sc));
+            CGB_CUDA(cudaStreamWaitEvent(sx, op->pipe_ev[k], 0));
+            const size_t r0 = (size_t)v0 * nS, nr = (size_t)(v1 - v0) * nS;
+            if (nr) CGB_CUDA(cudaMemcpyAsync(out + r0, op->d_out + r0, nr * sizeof(double), cudaMemcpyDeviceToHost, sx));
+        }
+        CGB_CUDA(cudaStreamSynchronize(sx));
+        CGB_CUDA(cudaStreamSynchronize(sc));
+        return CGB_OK;
+    }
+    for (int k = 0; k < kPipe; ++k) {
+        const int v0 = vb(k), v1 = vb(k + 1);
+        const size_t r0 = (size_t)v0 * nS, nr = (size_t)(v1 - v0) * nS;
+        if (nr) CGB_CUDA(cudaMemcpyAsync(op->d_in + r0, in + r0, nr * sizeof(double), cudaMemcpyHostToDevice, sx));
+        CGB_CUDA(cudaEventRecord(op->pipe_ev[k], sx));
+        CGB_CUDA(cudaStreamWaitEvent(sc, op->pipe_ev[k], 0));
+        CGB_TRY(adjoint_ff_range(op, op->d_in, op->d_out, v0, v1, sc));
+    }
+    CGB_TRY(fibre_sum(op, op->d_out, sc));
+    CGB_CUDA(cudaMemcpyAsync(out, op->d_out, out_len * sizeof(double), cudaMemcpyDeviceToHost, sc));
+    CGB_CUDA(cudaStreamSynchronize(sc));
+    return CGB_OK;
+}
+
 extern "C" {
 
 int cgb_op_apply(cgb_op *op, int adjoint, const void *in, int64_t in_len, void *out, int64_t out_len, int dtype,
@@ -74,6 +124,7 @@ int cgb_op_apply_host(cgb_op *op, int adjoint, const double *in, int64_t in_len,
         CGB_CUDA(cudaMalloc((void **)&op->d_out, need * sizeof(double)));
         op->d_in_len = op->d_out_len = need;
     }
+    if (in_len > 0 && pipelined(op)) return apply_host_pipelined(op, adjoint, in, in_len, out, out_len);
     cudaStream_t st = nullptr;
     if (in_len > 0) CGB_CUDA(cudaMemcpyAsync(op->d_in, in, in_len * sizeof(double), cudaMemcpyHostToDevice, st));
     CGB_TRY(cgb_op_apply(op, adjoint, op->d_in, in_len, op->d_out, out_len, CGB_DTYPE_F64, op->arith, st));

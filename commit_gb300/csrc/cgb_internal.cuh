@@ -39,6 +39,7 @@ constexpr int kRedSlots = 16;        // doubles reduced per block in the FISTA p
 // ------------------------------------------------------------------ device view of a handle
 struct OpDev {
     int nS, ndirs, nF, nE, nV, nISOv, nIC, nEC, nISO;
+    int v0;                         // first voxel of the launch (voxels v0 .. nV-1; 0 for a full pass)
     int64_t n;
     int64_t ec_base, iso_base;      // first EC / ISO column
     const float *lutIC, *lutEC, *lutISO;          // float32 LUTs
@@ -106,6 +107,8 @@ struct cgb_op {
     double *h_scal;                 // pinned host scalars
     double *d_in, *d_out;           // staging for cgb_op_apply_host
     int64_t d_in_len, d_out_len;
+    cudaStream_t pipe_st[2];        // host-buffer pipeline: compute and copy streams (created on first use)
+    cudaEvent_t pipe_ev[8];
     size_t bytes;
     int nsm;
     cgb::OpDev dev() const;
@@ -144,6 +147,11 @@ int launch_forward_R(cgb_op *op, int R, const RhsPtrs &V, const float *yobs, con
 int launch_adjoint_R(cgb_op *op, int R, const RhsPtrs &V, int in_mode, const float *yobs, const float *sqw,
                      double *partials, cudaStream_t st, int *grid);
 int fibre_sum32_from(cgb_op *op, const float *scr, double *xout, cudaStream_t st);
+// float-float packed kernels over the voxel range [v0, v1) (host-buffer pipeline); A' pass 1
+// only (the fibre pass follows once all ranges are done)
+int forward_ff_range(cgb_op *op, const double *x, double *y, int v0, int v1, cudaStream_t st);
+int adjoint_ff_range(cgb_op *op, const double *yin, double *xout, int v0, int v1, cudaStream_t st);
+int fibre_sum(cgb_op *op, double *xout, cudaStream_t st);
 int convert_f32_to_f64(const float *in, double *out, int64_t n, cudaStream_t st);
 
 // ------------------------------------------------------------------ occupancy autotuning

@@ -168,7 +168,7 @@ int reduction_blocks(const cgb_op *op) { return op->nsm * 8; }
 
 cgb::OpDev cgb_op::dev() const {
     cgb::OpDev d;
-    d.nS = nS; d.ndirs = ndirs; d.nF = nF; d.nE = nE; d.nV = nV; d.nISOv = nISOv;
+    d.nS = nS; d.ndirs = ndirs; d.nF = nF; d.nE = nE; d.nV = nV; d.nISOv = nISOv; d.v0 = 0;
     d.nIC = nIC; d.nEC = nEC; d.nISO = nISO; d.n = n;
     d.ec_base = (int64_t)nF * nIC;
     d.iso_base = d.ec_base + (int64_t)nE * nEC;
@@ -193,6 +193,10 @@ static void free_op(cgb_op *op) {
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (op->h_scal) cudaFreeHost(op->h_scal);
+    for (cudaStream_t s : op->pipe_st)
+        if (s) cudaStreamDestroy(s);
+    for (cudaEvent_t e : op->pipe_ev)
+        if (e) cudaEventDestroy(e);
     delete op;
 }
 

@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_forward_p(const OpDev P, const
     // 16-byte row stores need an even row length and 16-byte aligned outputs
     const bool even = (nS & 1) == 0 && vec_ok;
     double nrm = 0.0;
-    for (int v = blockIdx.x * gpb + (int)threadIdx.x / LPV; v < P.nV; v += ngroups) {
+    for (int v = P.v0 + blockIdx.x * gpb + (int)threadIdx.x / LPV; v < P.nV; v += ngroups) {
         DD2 acc[NP];
         forward_row_p<LPV, NP>(C, G, v, x, acc);
 #pragma unroll
@@ -364,7 +364,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_adjoint_p(const OpDev P, const
     const int ngroups = gridDim.x * gpb;
     const int nS = P.nS;
     double nrm = 0.0;
-    for (int v = blockIdx.x * gpb + (int)threadIdx.x / LPV; v < P.nV; v += ngroups) {
+    for (int v = P.v0 + blockIdx.x * gpb + (int)threadIdx.x / LPV; v < P.nV; v += ngroups) {
         double a[2 * NP];
         if (in_mode == 1) {
             DD2 acc[NP];

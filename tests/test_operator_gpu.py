@@ -185,3 +185,24 @@ def test_occupancy_builds_give_identical_results():
     st = A.occupancy()
     assert st['ff_forward'][0] in (1, 2) and st['ff_adjoint'][0] in (1, 2)
     assert st['ff_forward'][1] > 0 and st['ff_forward'][2] > 0
+
+
+def test_host_pipeline_matches_device_path():
+    """Host-buffer products on a problem large enough for the copy/compute pipeline
+    (nROWS >= 2^22) equal the device-buffer products bit for bit."""
+    import torch
+    from commit_gb300 import synth
+    from commit_gb300.operator import LinearOperator
+    D, K = synth.make_dictionary(synth.scaled_spec('demo_5k', dim=(64, 64, 32), n_mask=80000, n_fibers=20000,
+                                                   n_b0=18, shells=[(1000.0, 90)]))
+    A = LinearOperator(D, K, None)
+    assert A.nROWS >= 1 << 22
+    rng = np.random.default_rng(5)
+    x = rng.uniform(0, 1, A.nCOLS)
+    w = rng.normal(size=A.nROWS)
+    yh = A.dot(x)
+    xh = A.T.dot(w)
+    yd = A.dot(torch.from_numpy(x).cuda()).cpu().numpy()
+    xd = A.T.dot(torch.from_numpy(w).cuda()).cpu().numpy()
+    assert np.array_equal(yh, yd)
+    assert np.array_equal(xh, xd)
