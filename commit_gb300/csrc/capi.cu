@@ -36,6 +36,14 @@ static bool pipelined(const cgb_op *op) {
            op->nrows >= ((int64_t)1 << 22);
 }
 
+namespace cgb {
+int forward_ff(cgb_op *op, const double *x, double *y, double *ax, const double *yobs, const double *sqw,
+               double *partials, cudaStream_t st, int *grid);
+int adjoint_ff(cgb_op *op, const double *yin, int in_mode, const double *x, const double *yobs, const double *sqw,
+               const double *ax_a, const double *ax_b, double ca, double cb, double *xout, double *partials,
+               cudaStream_t st, int *grid);
+}  // namespace cgb
+
 static int apply_host_pipelined(cgb_op *op, int adjoint, const double *in, int64_t in_len, double *out,
                                 int64_t out_len) {
     if (!op->pipe_st[0]) {
@@ -44,14 +52,21 @@ static int apply_host_pipelined(cgb_op *op, int adjoint, const double *in, int64
     }
     cudaStream_t sc = op->pipe_st[0], sx = op->pipe_st[1];
     const int nS = op->nS;
-    auto vb = [&](int k) { return (int)((int64_t)op->nV * k / kPipe); };
+    // ranges: the adjoint slabs when the handle has them (the fibre pass of a range then
+    // runs right after its voxel pass), else kPipe equal voxel ranges
+    const bool slabs = adjoint && op->nslab > 1;
+    const int K = slabs ? op->nslab : kPipe;
+    auto vb = [&](int k) { return slabs ? op->slab_v[k] : (int)((int64_t)op->nV * k / kPipe); };
     if (!adjoint) {
         CGB_CUDA(cudaMemcpyAsync(op->d_in, in, in_len * sizeof(double), cudaMemcpyHostToDevice, sc));
-        for (int k = 0; k < kPipe; ++k) {
+        for (int k = 0; k < K; ++k) {
             const int v0 = vb(k), v1 = vb(k + 1);
-            CGB_TRY(forward_ff_range(op, op->d_in, op->d_out, v0, v1, sc));
-            CGB_CUDA(cudaEventRecord(op->pipe_ev[k], sc));
-            CGB_CUDA(cudaStreamWaitEvent(sx, op->pipe_ev[k], 0));
+            if (v1 > v0) {
+                VoxelRange vr(op, v0, v1);
+                CGB_TRY(forward_ff(op, op->d_in, op->d_out, nullptr, nullptr, nullptr, nullptr, sc, nullptr));
+            }
+            CGB_CUDA(cudaEventRecord(op->pipe_ev[k % kPipe], sc));
+            CGB_CUDA(cudaStreamWaitEvent(sx, op->pipe_ev[k % kPipe], 0));
             const size_t r0 = (size_t)v0 * nS, nr = (size_t)(v1 - v0) * nS;
             if (nr) CGB_CUDA(cudaMemcpyAsync(out + r0, op->d_out + r0, nr * sizeof(double), cudaMemcpyDeviceToHost, sx));
         }
@@ -59,15 +74,20 @@ static int apply_host_pipelined(cgb_op *op, int adjoint, const double *in, int64
         CGB_CUDA(cudaStreamSynchronize(sc));
         return CGB_OK;
     }
-    for (int k = 0; k < kPipe; ++k) {
+    for (int k = 0; k < K; ++k) {
         const int v0 = vb(k), v1 = vb(k + 1);
         const size_t r0 = (size_t)v0 * nS, nr = (size_t)(v1 - v0) * nS;
         if (nr) CGB_CUDA(cudaMemcpyAsync(op->d_in + r0, in + r0, nr * sizeof(double), cudaMemcpyHostToDevice, sx));
-        CGB_CUDA(cudaEventRecord(op->pipe_ev[k], sx));
-        CGB_CUDA(cudaStreamWaitEvent(sc, op->pipe_ev[k], 0));
-        CGB_TRY(adjoint_ff_range(op, op->d_in, op->d_out, v0, v1, sc));
+        CGB_CUDA(cudaEventRecord(op->pipe_ev[k % kPipe], sx));
+        CGB_CUDA(cudaStreamWaitEvent(sc, op->pipe_ev[k % kPipe], 0));
+        if (v1 > v0) {
+            VoxelRange vr(op, v0, v1);
+            CGB_TRY(adjoint_ff(op, op->d_in, 0, nullptr, nullptr, nullptr, nullptr, nullptr, 0.0, 0.0, op->d_out,
+                               nullptr, sc, nullptr));
+        }
+        if (slabs) CGB_TRY(fibre_sum_slab(op, op->d_out, k, sc));
     }
-    CGB_TRY(fibre_sum(op, op->d_out, sc));
+    if (!slabs) CGB_TRY(fibre_sum(op, op->d_out, sc));
     CGB_CUDA(cudaMemcpyAsync(out, op->d_out, out_len * sizeof(double), cudaMemcpyDeviceToHost, sc));
     CGB_CUDA(cudaStreamSynchronize(sc));
     return CGB_OK;

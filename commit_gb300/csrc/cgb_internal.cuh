@@ -108,6 +108,12 @@ struct cgb_op {
     double *d_in, *d_out;           // staging for cgb_op_apply_host
     int64_t d_in_len, d_out_len;
     cudaStream_t pipe_st[2];        // host-buffer pipeline: compute and copy streams (created on first use)
+    int vr0, vr1;                   // voxel range [vr0, vr1) of the next voxel-kernel launches (vr1 0: all)
+    // adjoint slabs: voxel ranges whose per-segment terms fit in L2, so the fibre pass of a
+    // slab gathers them from L2 right after the voxel pass wrote them (see run_adjoint)
+    int nslab;                      // 1: no slabs
+    int *slab_v;                    // host [nslab+1] voxel boundaries
+    uint32_t *fib_slab;             // device [(nslab+1) * nF]: fibre f's fib_perm index where slab s starts
     cudaEvent_t pipe_ev[8];
     size_t bytes;
     int nsm;
@@ -149,9 +155,26 @@ int launch_adjoint_R(cgb_op *op, int R, const RhsPtrs &V, int in_mode, const flo
 int fibre_sum32_from(cgb_op *op, const float *scr, double *xout, cudaStream_t st);
 // float-float packed kernels over the voxel range [v0, v1) (host-buffer pipeline); A' pass 1
 // only (the fibre pass follows once all ranges are done)
-int forward_ff_range(cgb_op *op, const double *x, double *y, int v0, int v1, cudaStream_t st);
-int adjoint_ff_range(cgb_op *op, const double *yin, double *xout, int v0, int v1, cudaStream_t st);
 int fibre_sum(cgb_op *op, double *xout, cudaStream_t st);
+// fibre pass of one adjoint slab (sums continue across slabs in fibre order; the last slab
+// applies eval), FP64 / FP32 terms
+int fibre_sum_slab(cgb_op *op, double *xout, int s, cudaStream_t st);
+int fibre_sum32_slab(cgb_op *op, const float *scr, double *xout, int s, cudaStream_t st);
+// blocks of partial sums an adjoint may write (one grid per slab)
+int partial_blocks(const cgb_op *op);
+
+// restricts the voxel kernels launched while it lives to voxels [v0, v1)
+struct VoxelRange {
+    cgb_op *op;
+    VoxelRange(cgb_op *o, int v0, int v1) : op(o) {
+        op->vr0 = v0;
+        op->vr1 = v1;
+    }
+    ~VoxelRange() {
+        op->vr0 = 0;
+        op->vr1 = 0;
+    }
+};
 int convert_f32_to_f64(const float *in, double *out, int64_t n, cudaStream_t st);
 
 // ------------------------------------------------------------------ occupancy autotuning

@@ -408,7 +408,7 @@ struct Solver {
 
     int init() {
         const int64_t nc = op->ncols, nr = op->nrows;
-        const int rb = reduction_blocks(op);
+        const int rb = partial_blocks(op);
         mixed = prm->arith == CGB_ARITH_BF16 || prm->arith == CGB_ARITH_FP16 || prm->arith == CGB_ARITH_F32;
         if (!dsc) dsc = op->dscal;
         ws.st = st;
@@ -968,7 +968,7 @@ struct BatchSolver {
         CGB_CUDA(cudaMemsetAsync(bscal, 0, (size_t)P * 16 * sizeof(double), st));
         hbv.assign((size_t)P * 16, 0.0);
         hb = hbv.data();
-        CGB_TRY(ws_alloc(&partials, (size_t)reduction_blocks(op) * kRedSlots, st));
+        CGB_TRY(ws_alloc(&partials, (size_t)partial_blocks(op) * kRedSlots, st));
         CGB_TRY(ws_alloc(&y32, nr, st));
         CGB_TRY(convert_f64_to_f32(y, y32, nr, st));
         if (sqw) {

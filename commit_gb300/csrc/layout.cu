@@ -14,6 +14,9 @@
 #include <mutex>
 #include <vector>
 
+#include <algorithm>
+#include <vector>
+
 #include "cgb_internal.cuh"
 #include "operator_pair.cuh"
 
@@ -163,6 +166,7 @@ int bits_for(uint64_t maxval) {
 }  // namespace
 
 int reduction_blocks(const cgb_op *op) { return op->nsm * 8; }
+int partial_blocks(const cgb_op *op) { return reduction_blocks(op) * (op->nslab > 1 ? op->nslab : 1); }
 
 }  // namespace cgb
 
@@ -183,18 +187,82 @@ cgb::OpDev cgb_op::dev() const {
 
 using namespace cgb;
 
+// Adjoint slabs.  The voxel pass writes one term per segment in voxel order and the fibre
+// pass gathers them in fibre order: a gather over the whole term stream (≈ 1 GB for 1M
+// streamlines) misses L2 on almost every access.  Cutting the voxels into slabs of about
+// kSlabTermBytes of terms and running the fibre pass of each slab right after its voxel
+// pass keeps the gathers in L2.  fib_slab[s*nF + f] is the first entry of fibre f's
+// (ascending) position list that lies in slab s.
+constexpr double kSlabTermBytes = 40.0 * (1 << 20);
+
+__global__ void k_fib_slabs(const uint32_t *__restrict__ fib_ptr, const uint32_t *__restrict__ fib_perm, int nF,
+                            int S, const uint32_t *__restrict__ slab_pos, uint32_t *__restrict__ fib_slab) {
+    const int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (f >= nF) return;
+    uint32_t k = fib_ptr[f];
+    const uint32_t end = fib_ptr[f + 1];
+    for (int s = 0; s <= S; ++s) {
+        while (k < end && fib_perm[k] < slab_pos[s]) ++k;
+        fib_slab[(size_t)s * nF + f] = k;
+    }
+}
+
+static int build_slabs(cgb_op *op, int want = 0) {
+    op->nslab = 1;
+    delete[] op->slab_v;
+    op->slab_v = new int[2]{0, op->nV};
+    if (op->fib_slab) {
+        cudaFree(op->fib_slab);
+        op->fib_slab = nullptr;
+    }
+    const double bytes = (double)op->n * (op->nIC > 0 ? op->nIC : 1) * sizeof(double);
+    int S = want > 0 ? want : (int)(bytes / kSlabTermBytes + 0.5);
+    if (S > 64) S = 64;
+    if (S < 2 || op->nV < 2 * S || op->nF == 0 || op->nolut) return CGB_OK;
+    std::vector<uint32_t> vp((size_t)op->nV + 1);
+    CGB_CUDA(cudaMemcpy(vp.data(), op->vox_ptr, vp.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    std::vector<int> sv(S + 1);
+    std::vector<uint32_t> pos(S + 1);
+    for (int s = 0; s <= S; ++s) {
+        const uint64_t target = (uint64_t)op->n * s / S;
+        sv[s] = s == S ? op->nV : (int)(std::lower_bound(vp.begin(), vp.end(), (uint32_t)target) - vp.begin());
+        if (s > 0 && sv[s] < sv[s - 1]) sv[s] = sv[s - 1];
+        pos[s] = vp[sv[s]];
+    }
+    uint32_t *dpos = nullptr;
+    CGB_CUDA(cudaMalloc((void **)&dpos, pos.size() * sizeof(uint32_t)));
+    CGB_CUDA(cudaMemcpy(dpos, pos.data(), pos.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    const cudaError_t e = cudaMalloc((void **)&op->fib_slab, (size_t)(S + 1) * op->nF * sizeof(uint32_t));
+    if (e != cudaSuccess) {
+        cudaFree(dpos);
+        op->fib_slab = nullptr;
+        return cuda_fail(e, "cudaMalloc");
+    }
+    k_fib_slabs<<<(op->nF + 255) / 256, 256>>>(op->fib_ptr, op->fib_perm, op->nF, S, dpos, op->fib_slab);
+    const cudaError_t e2 = cudaGetLastError();
+    cudaDeviceSynchronize();
+    cudaFree(dpos);
+    if (e2 != cudaSuccess) return cuda_fail(e2, "k_fib_slabs");
+    delete[] op->slab_v;
+    op->slab_v = new int[S + 1];
+    for (int s = 0; s <= S; ++s) op->slab_v[s] = sv[s];
+    op->nslab = S;
+    return CGB_OK;
+}
+
 static void free_op(cgb_op *op) {
     if (!op) return;
     free_grad_state(op);
     void *ptrs[] = {op->lutIC, op->lutEC, op->lutISO, op->lutIC_p, op->lutEC_p, op->lutISO_p, op->lutIC_r, op->lutEC_r, op->lutISO_r, op->seg_l16, op->vox_ptr,
                     op->seg_f, op->eval, op->fib_ptr, op->fib_perm, op->ec_ptr, op->ec_col, op->iso_ptr,
                     op->iso_col, op->seg_o, op->ec_o, op->seg_l, op->scratch, op->scratch32, op->partials,
-                    op->dscal, op->d_in, op->d_out, op->d_x64};
+                    op->dscal, op->d_in, op->d_out, op->d_x64, op->fib_slab};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (op->h_scal) cudaFreeHost(op->h_scal);
     for (cudaStream_t s : op->pipe_st)
         if (s) cudaStreamDestroy(s);
+    delete[] op->slab_v;
     for (cudaEvent_t e : op->pipe_ev)
         if (e) cudaEventDestroy(e);
     delete op;
@@ -372,9 +440,11 @@ static int create_impl(int device, int nS, int ndirs, int nF, int64_t n, int nE,
         CGB_CUDA(cudaMemset(op->iso_ptr, 0, ((size_t)nV + 1) * sizeof(uint32_t)));
     }
 
+    CGB_TRY(build_slabs(op));
+
     // work buffers
     CGB_TRY(dalloc(op, &op->scratch, (size_t)n * (nIC > 0 ? nIC : 1)));
-    CGB_TRY(dalloc(op, &op->partials, (size_t)reduction_blocks(op) * kRedSlots));
+    CGB_TRY(dalloc(op, &op->partials, (size_t)partial_blocks(op) * kRedSlots));
     CGB_TRY(dalloc(op, &op->dscal, 64));
     CGB_CUDA(cudaMallocHost((void **)&op->h_scal, 64 * sizeof(double)));
     CGB_CUDA(cudaDeviceSynchronize());
@@ -453,6 +523,27 @@ int cgb_op_set_lut(cgb_op *op, const float *lutIC, const float *lutEC, const flo
                               cudaMemcpyDefault));
     }
     op->lut_r_kind = 0;  // reduced-precision copies are rebuilt on their next use
+    return CGB_OK;
+}
+
+int cgb_op_set_slabs(cgb_op *op, int nslab, int *out) {
+    if (!op) return fail(CGB_ERR_INVALID, "null handle");
+    if (nslab < 0 || nslab > 64) return fail(CGB_ERR_INVALID, "nslab must be 0..64");
+    DeviceGuard g(op->device);
+    CGB_CUDA(cudaDeviceSynchronize());
+    CGB_TRY(build_slabs(op, nslab == 0 ? 0 : nslab));
+    if (nslab == 1) {
+        // a single slab is the plain two-pass adjoint
+        delete[] op->slab_v;
+        op->slab_v = new int[2]{0, op->nV};
+        if (op->fib_slab) cudaFree(op->fib_slab);
+        op->fib_slab = nullptr;
+        op->nslab = 1;
+    }
+    if (op->partials) cudaFree(op->partials);
+    op->partials = nullptr;
+    CGB_CUDA(cudaMalloc((void **)&op->partials, (size_t)partial_blocks(op) * kRedSlots * sizeof(double)));
+    if (out) *out = op->nslab;
     return CGB_OK;
 }
 

@@ -87,6 +87,33 @@ int fibre_sum32(cgb_op *op, double *xout, cudaStream_t st) {
 
 }  // namespace
 
+__global__ void k_fibre_sum32_slab(const OpDev P, const float *__restrict__ scr, double *__restrict__ xout,
+                                   const uint32_t *__restrict__ fib_slab, int s, int S) {
+    const int64_t total = (int64_t)P.nF * P.nIC;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(q / P.nF);
+        const uint32_t f = (uint32_t)(q - (int64_t)i * P.nF);
+        const uint32_t beg = fib_slab[(size_t)s * P.nF + f], end = fib_slab[(size_t)(s + 1) * P.nF + f];
+        if (s > 0 && s < S - 1 && beg == end) continue;
+        const float *T = scr + (size_t)i * P.n;
+        double acc = s == 0 ? 0.0 : xout[q];
+        for (uint32_t k = beg; k < end; ++k) acc += (double)T[P.fib_perm[k]];
+        xout[q] = s == S - 1 ? acc * (double)P.eval[q] : acc;
+    }
+}
+
+int fibre_sum32_slab(cgb_op *op, const float *scr, double *xout, int s, cudaStream_t st) {
+    if (op->nIC > 0 && op->nF > 0) {
+        const int64_t total = (int64_t)op->nF * op->nIC;
+        int gb = (int)((total + 255) / 256);
+        if (gb > op->nsm * 16) gb = op->nsm * 16;
+        k_fibre_sum32_slab<<<gb, 256, 0, st>>>(op->dev(), scr, xout, op->fib_slab, s, op->nslab);
+        CGB_CUDA(cudaGetLastError());
+    }
+    return CGB_OK;
+}
+
 int fibre_sum32_from(cgb_op *op, const float *scr, double *xout, cudaStream_t st) {
     if (op->nIC > 0 && op->nF > 0) {
         const int64_t total = (int64_t)op->nF * op->nIC;
@@ -212,6 +239,30 @@ static int adj_mix(cgb_op *op, int arith, const float *yin, int mode, const doub
     return adjoint_mix_f32(op, yin, mode, x, yobs, sqw, ax_a, ax_b, ca, cb, xout, partials, st, grid);
 }
 
+// A' in reduced precision: voxel pass and fibre pass, slab by slab when the handle has
+// slabs (the fibre pass then gathers each slab's terms from L2)
+static int adj_mix_slabs(cgb_op *op, int arith, const float *yin, int mode, const double *x, const float *yobs,
+                         const float *sqw, const float *ax_a, const float *ax_b, float ca, float cb, double *xout,
+                         double *partials, cudaStream_t st, int *grid) {
+    if (op->nslab <= 1) {
+        CGB_TRY(adj_mix(op, arith, yin, mode, x, yobs, sqw, ax_a, ax_b, ca, cb, xout, partials, st, grid));
+        return fibre_sum32(op, xout, st);
+    }
+    int g = 0;
+    for (int sl = 0; sl < op->nslab; ++sl) {
+        {
+            VoxelRange vr(op, op->slab_v[sl], op->slab_v[sl + 1]);
+            int gs = 0;
+            CGB_TRY(adj_mix(op, arith, yin, mode, x, yobs, sqw, ax_a, ax_b, ca, cb, xout,
+                            partials ? partials + (size_t)sl * g * kRedSlots : nullptr, st, &gs));
+            if (sl == 0) g = gs;
+        }
+        CGB_TRY(fibre_sum32_slab(op, op->scratch32, xout, sl, st));
+    }
+    if (grid) *grid = g * op->nslab;
+    return CGB_OK;
+}
+
 int launch_resnorm_mix(cgb_op *op, const double *x, const float *y, const float *sqw, double *partials,
                        float *ax_out, float *yout, cudaStream_t st, int arith, int *grid) {
     if (grid) *grid = 0;
@@ -229,8 +280,7 @@ int launch_gradient_mix(cgb_op *op, const double *x, const float *y, const float
         if (op->ncols > 0) CGB_CUDA(cudaMemsetAsync(grad, 0, op->ncols * sizeof(double), st));
         return CGB_OK;
     }
-    CGB_TRY(adj_mix(op, arith, nullptr, ax_a ? 2 : 1, x, y, sqw, ax_a, ax_b, ca, cb, grad, partials, st, grid));
-    return fibre_sum32(op, grad, st);
+    return adj_mix_slabs(op, arith, nullptr, ax_a ? 2 : 1, x, y, sqw, ax_a, ax_b, ca, cb, grad, partials, st, grid);
 }
 
 int launch_adjoint_mix(cgb_op *op, const float *yin, double *xout, cudaStream_t st, int arith) {
@@ -239,9 +289,8 @@ int launch_adjoint_mix(cgb_op *op, const float *yin, double *xout, cudaStream_t 
         if (op->ncols > 0) CGB_CUDA(cudaMemsetAsync(xout, 0, op->ncols * sizeof(double), st));
         return CGB_OK;
     }
-    CGB_TRY(adj_mix(op, arith, yin, 0, nullptr, nullptr, nullptr, nullptr, nullptr, 0.f, 0.f, xout, nullptr, st,
-                    nullptr));
-    return fibre_sum32(op, xout, st);
+return adj_mix_slabs(op, arith, yin, 0, nullptr, nullptr, nullptr, nullptr, nullptr, 0.f, 0.f, xout, nullptr, st,
+                         nullptr);
 }
 
 }  // namespace cgb

@@ -105,9 +105,40 @@ __global__ void k_adjoint_nolut(const OpDev P, const double *__restrict__ yin, i
     if (partials) block_sum_store(nrm, partials + (size_t)blockIdx.x * kRedSlots);
 }
 
+// fibre pass of slab s: the running sums of the fibres continue from xout (slab 0 starts
+// at 0), terms in the fibre's position order, so the sums are those of k_fibre_sum; the
+// last slab applies eval
+__global__ void k_fibre_sum_slab(const OpDev P, const double *__restrict__ scratch, double *__restrict__ xout,
+                                 const uint32_t *__restrict__ fib_slab, int s, int S) {
+    const int64_t total = (int64_t)P.nF * P.nIC;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(q / P.nF);
+        const uint32_t f = (uint32_t)(q - (int64_t)i * P.nF);
+        const uint32_t beg = fib_slab[(size_t)s * P.nF + f], end = fib_slab[(size_t)(s + 1) * P.nF + f];
+        if (s > 0 && s < S - 1 && beg == end) continue;
+        const double *T = scratch + (size_t)i * P.n;
+        double acc = s == 0 ? 0.0 : xout[q];
+        for (uint32_t k = beg; k < end; ++k) acc += T[P.fib_perm[k]];
+        xout[q] = s == S - 1 ? acc * (double)P.eval[q] : acc;
+    }
+}
+
 }  // namespace detail
 
 using namespace detail;
+
+int fibre_sum_slab(cgb_op *op, double *xout, int s, cudaStream_t st) {
+    if (op->nIC > 0 && op->nF > 0) {
+        const OpDev P = op->dev();
+        const int64_t total = (int64_t)op->nF * op->nIC;
+        int gb = (int)((total + 255) / 256);
+        if (gb > op->nsm * 16) gb = op->nsm * 16;
+        k_fibre_sum_slab<<<gb, 256, 0, st>>>(P, op->scratch, xout, op->fib_slab, s, op->nslab);
+        CGB_CUDA(cudaGetLastError());
+    }
+    return CGB_OK;
+}
 
 int fibre_sum(cgb_op *op, double *xout, cudaStream_t st) {
     if (op->nIC > 0 && op->nF > 0) {
@@ -159,6 +190,22 @@ static int run_adjoint(cgb_op *op, const double *yin, int in_mode, const double 
         CGB_TRY(adjoint_f64(op, yin, in_mode, x, yobs, sqw, ax_a, ax_b, ca, cb, xout, partials, st, grid_out));
     } else if (op->ff_variant == 0) {
         CGB_TRY(adjoint_ffs(op, yin, in_mode, x, yobs, sqw, ax_a, ax_b, ca, cb, xout, partials, st, grid_out));
+    } else if (op->nslab > 1) {
+        // slab by slab: voxel pass, then the fibre pass while the slab's terms are in L2;
+        // slab s writes its norm partials after the s * grid blocks of the earlier slabs
+        int g = 0;
+        for (int sl = 0; sl < op->nslab; ++sl) {
+            {
+                VoxelRange vr(op, op->slab_v[sl], op->slab_v[sl + 1]);
+                int gs = 0;
+                CGB_TRY(adjoint_ff(op, yin, in_mode, x, yobs, sqw, ax_a, ax_b, ca, cb, xout,
+                                   partials ? partials + (size_t)sl * g * kRedSlots : nullptr, st, &gs));
+                if (sl == 0) g = gs;
+            }
+            CGB_TRY(fibre_sum_slab(op, xout, sl, st));
+        }
+        if (grid_out) *grid_out = g * op->nslab;
+        return CGB_OK;
     } else {
         CGB_TRY(adjoint_ff(op, yin, in_mode, x, yobs, sqw, ax_a, ax_b, ca, cb, xout, partials, st, grid_out));
     }

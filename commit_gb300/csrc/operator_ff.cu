@@ -15,18 +15,17 @@ struct FwdPair {
     double *partials;
     cudaStream_t st;
     int *grid_out;
-    int v0 = 0, v1 = -1;  // voxel range (v1 < 0: all voxels)
     template <int L, int N, int MINB>
     int launch() {
         OpDev P = op->dev();
-        if (v1 >= 0) {
-            P.v0 = v0;
-            P.nV = v1;
+        if (op->vr1 > 0) {
+            P.v0 = op->vr0;
+            P.nV = op->vr1;
         }
         const Comps C = make_comps(op);
         auto kern = k_forward_p<L, N, MINB>;
-        int g = 0;
-        CGB_TRY(grid_for_kernel(kern, 0, op->nsm, P.nV - P.v0, kBlock / L, &g));
+        int g = 0;  // sized for all voxels, so every range launch has the same grid
+        CGB_TRY(grid_for_kernel(kern, 0, op->nsm, op->nV, kBlock / L, &g));
         if (g > reduction_blocks(op)) g = reduction_blocks(op);
         const int vec_ok = ((uintptr_t)y % 16 == 0) && ((uintptr_t)ax % 16 == 0);
         kern<<<g, kBlock, 0, st>>>(P, C, x, y, ax, yobs, sqw, partials, vec_ok);
@@ -49,18 +48,17 @@ struct AdjPair {
     double *xout, *partials;
     cudaStream_t st;
     int *grid_out;
-    int v0 = 0, v1 = -1;
     template <int L, int N, int MINB>
     int launch() {
         OpDev P = op->dev();
-        if (v1 >= 0) {
-            P.v0 = v0;
-            P.nV = v1;
+        if (op->vr1 > 0) {
+            P.v0 = op->vr0;
+            P.nV = op->vr1;
         }
         const Comps C = make_comps(op);
         auto kern = k_adjoint_p<L, N, MINB>;
-        int g = 0;
-        CGB_TRY(grid_for_kernel(kern, 0, op->nsm, P.nV - P.v0, kBlock / L, &g));
+        int g = 0;  // sized for all voxels, so every range launch has the same grid
+        CGB_TRY(grid_for_kernel(kern, 0, op->nsm, op->nV, kBlock / L, &g));
         if (g > reduction_blocks(op)) g = reduction_blocks(op);
         kern<<<g, kBlock, 0, st>>>(P, C, yin, in_mode, x, yobs, sqw, ax_a, ax_b, ca, cb, op->scratch, xout, partials);
         CGB_CUDA(cudaGetLastError());
@@ -85,18 +83,6 @@ int adjoint_ff(cgb_op *op, const double *yin, int in_mode, const double *x, cons
                const double *ax_a, const double *ax_b, double ca, double cb, double *xout, double *partials,
                cudaStream_t st, int *grid) {
     AdjPair L{op, yin, in_mode, x, yobs, sqw, ax_a, ax_b, ca, cb, xout, partials, st, grid};
-    return dispatch_pair_shape(pick_pair_shape(op->nS), L);
-}
-
-int forward_ff_range(cgb_op *op, const double *x, double *y, int v0, int v1, cudaStream_t st) {
-    if (v1 <= v0) return CGB_OK;
-    FwdPair L{op, x, y, nullptr, nullptr, nullptr, nullptr, st, nullptr, v0, v1};
-    return dispatch_pair_shape(pick_pair_shape(op->nS), L);
-}
-
-int adjoint_ff_range(cgb_op *op, const double *yin, double *xout, int v0, int v1, cudaStream_t st) {
-    if (v1 <= v0) return CGB_OK;
-    AdjPair L{op, yin, 0, nullptr, nullptr, nullptr, nullptr, nullptr, 0.0, 0.0, xout, nullptr, st, nullptr, v0, v1};
     return dispatch_pair_shape(pick_pair_shape(op->nS), L);
 }
 

@@ -65,8 +65,8 @@ struct AdjMix {
         int g = 0;
         CGB_TRY(grid_for_kernel(kern, 0, op->nsm, op->nV, kBlock / L, &g));
         if (g > reduction_blocks(op)) g = reduction_blocks(op);
-        kern<<<g, kBlock, 0, st>>>(op->nV, op->nS, op->n, comps(op), yin, in_mode, x, yobs, sqw, ax_a, ax_b, ca, cb,
-                                   op->scratch32, xout, partials);
+        kern<<<g, kBlock, 0, st>>>(op->vr1 > 0 ? op->vr0 : 0, op->vr1 > 0 ? op->vr1 : op->nV, op->nS, op->n, comps(op),
+                                   yin, in_mode, x, yobs, sqw, ax_a, ax_b, ca, cb, op->scratch32, xout, partials);
         CGB_CUDA(cudaGetLastError());
         if (grid_out) *grid_out = g;
         return CGB_OK;

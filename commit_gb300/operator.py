@@ -190,6 +190,12 @@ class LinearOperator:
             out[name] = (int(c.value), float(a.value), float(b.value))
         return out
 
+    def set_slabs(self, nslab: int = 0) -> int:
+        """Adjoint slab count (0: automatic, 1: off); returns the count in use."""
+        out = ctypes.c_int32()
+        check(lib().cgb_op_set_slabs(self._h.ptr, int(nslab), ctypes.byref(out)))
+        return int(out.value)
+
     def batch_width(self, set_to: int | None = None) -> int:
         """Vectors per multi-right-hand-side pass (0: chosen by timing on the next batched
         solve); ``set_to`` 0, 2 or 4 stores a value."""
