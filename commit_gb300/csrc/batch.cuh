@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(kBlock) k_forward_R(const int nV, const int nS
 // A' pass 1 for R vectors.  in_mode 0: z_r = yin_r; 1: z_r from the fused forward
 // (r = sqw*(A x_r - yobs), FP64 norm partials per vector); 2: A x_r = ca_r*axa_r + cb_r*axb_r.
 template <class LT, int LPV, int NP, int R, int MINB = 1>
-__global__ void __launch_bounds__(kBlock, MINB) k_adjoint_R(const int nV, const int nS, const int64_t n,
+__global__ void __launch_bounds__(kBlock, MINB) k_adjoint_R(const int v0, const int nV, const int nS, const int64_t n,
                                                       const __grid_constant__ CompsM<LT> C,
                                                       const __grid_constant__ RhsPtrs V, int in_mode,
                                                       const float *__restrict__ yobs, const float *__restrict__ sqw,
@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_adjoint_R(const int nV, const 
     double nrm[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) nrm[r] = 0.0;
-    for (int v = blockIdx.x * gpb + (int)threadIdx.x / LPV; v < nV; v += ngroups) {
+    for (int v = v0 + blockIdx.x * gpb + (int)threadIdx.x / LPV; v < nV; v += ngroups) {
         f2 z[R][NP];
         {
             f2 acc[R][NP];

@@ -61,7 +61,8 @@ struct AdjR {
         int g = 0;
         CGB_TRY(grid_for_kernel(kern, 0, op->nsm, op->nV, kBlock / L, &g));
         if (g > reduction_blocks(op)) g = reduction_blocks(op);
-        kern<<<g, kBlock, 0, st>>>(op->nV, op->nS, op->n, comps_bf16(op), *V, in_mode, yobs, sqw, partials);
+        kern<<<g, kBlock, 0, st>>>(op->vr1 > 0 ? op->vr0 : 0, op->vr1 > 0 ? op->vr1 : op->nV, op->nS, op->n,
+                                   comps_bf16(op), *V, in_mode, yobs, sqw, partials);
         CGB_CUDA(cudaGetLastError());
         if (grid_out) *grid_out = g;
         return CGB_OK;

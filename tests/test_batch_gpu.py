@@ -161,3 +161,19 @@ def test_concurrent_paths_match_one_at_a_time():
         for (x1, d1), (x2, d2) in zip(a, b):
             assert d1['iterations'] == d2['iterations']
             assert np.array_equal(x1, x2)
+
+
+def test_batched_path_with_adjoint_slabs_is_bitwise_unchanged():
+    from commit_gb300 import solvers
+    from commit_gb300.operator import LinearOperator
+    D, K, P, y = _demo()
+    A = LinearOperator(D, K, None)
+    A.batch_width(2)
+    regs = _path_regs(A, D, K, y, [1e-4, 1e-3, 1e-2])
+    out = {}
+    for s in (1, 4):
+        assert A.set_slabs(s) == s
+        out[s] = solvers.solve_batch(y, A, regs, tol_fun=1e-5, tol_x=1e-7, max_iter=40, momentum_reuse=False)
+    for (x1, d1), (x4, d4) in zip(out[1], out[4]):
+        assert d1['iterations'] == d4['iterations']
+        assert np.array_equal(x1, x4)
