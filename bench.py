@@ -47,6 +47,8 @@ def parse():
     p.add_argument('--workload', default='hcp_1m')
     p.add_argument('--fibers', type=int, default=0, help='override the number of streamlines (smaller runs)')
     p.add_argument('--arith', default='ff', choices=['ff', 'f64', 'bf16', 'fp16', 'f32'])
+    p.add_argument('--slabs', type=int, default=-1,
+                   help='adjoint slab count (0 automatic, 1 off; default: the handle\'s own choice)')
     p.add_argument('--fista', action='store_true', help='FISTA time-to-tolerance, plain vs mixed + refinement')
     p.add_argument('--fista-iters', type=int, default=1500)
     p.add_argument('--demo', action='store_true',
@@ -274,6 +276,8 @@ def run_ours(args):
         return run_fista(args, spec, D, K, dev)
     reduced = args.arith in ('bf16', 'fp16', 'f32')
     A = LinearOperator(D, K, None, arith='ff' if reduced else args.arith, device=dev.index)
+    if args.slabs >= 0:
+        A.set_slabs(args.slabs)
     At = A.T
     nbytes, nfma, nrows, ncols = algorithmic(D, K, reduced)
     vdt = torch.float32 if reduced else torch.float64
@@ -326,7 +330,7 @@ def run_ours(args):
                         'forward_ms': fwd_ms, 'adjoint_ms': adj_ms,
                         'fma_per_product': nfma, 'achieved_gfma_s': nfma / (dom_ms / 1000.0) / 1e9},
            'clocks': clk, 'gpu_launches': args.steps * (1 + 2), 'setup_s': {'generate': tgen},
-           'occupancy_tuning': A.occupancy()}
+           'occupancy_tuning': A.occupancy(), 'adjoint_slabs': A.set_slabs(None)}
     # end to end through the public API on pinned host buffers
     if not args.no_e2e and not reduced:
         xh = torch.empty(ncols, dtype=torch.float64, pin_memory=True).numpy()

@@ -114,6 +114,8 @@ struct cgb_op {
     int nslab;                      // 1: no slabs
     int *slab_v;                    // host [nslab+1] voxel boundaries
     uint32_t *fib_slab;             // device [(nslab+1) * nF]: fibre f's fib_perm index where slab s starts
+    cudaStream_t slab_st[3];        // slab schedule streams (created on first use)
+    cudaEvent_t slab_ev[68];
     cudaEvent_t pipe_ev[8];
     size_t bytes;
     int nsm;
@@ -162,6 +164,47 @@ int fibre_sum_slab(cgb_op *op, double *xout, int s, cudaStream_t st);
 int fibre_sum32_slab(cgb_op *op, const float *scr, double *xout, int s, cudaStream_t st);
 // blocks of partial sums an adjoint may write (one grid per slab)
 int partial_blocks(const cgb_op *op);
+
+// Slab schedule of an adjoint: the voxel passes of consecutive slabs alternate between two
+// streams (they touch disjoint voxels, rows and terms, so they overlap and hide each
+// other's tail), the fibre passes run in slab order on a third stream, each after its
+// slab's voxel pass.  The three streams fork from `st` and join back into it.  Inside a
+// stream capture the same steps run in order on `st`.  pass1(s, stream) / pass2(s, stream)
+// return a status.
+template <class P1, class P2>
+int slab_schedule(cgb_op *op, cudaStream_t st, P1 &&pass1, P2 &&pass2) {
+    const int S = op->nslab;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CGB_CUDA(cudaStreamIsCapturing(st, &cs));
+    if (cs != cudaStreamCaptureStatusNone || S + 4 > 68) {
+        for (int s = 0; s < S; ++s) {
+            CGB_TRY(pass1(s, st));
+            CGB_TRY(pass2(s, st));
+        }
+        return CGB_OK;
+    }
+    if (!op->slab_st[0]) {
+        for (auto &q : op->slab_st) CGB_CUDA(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
+        for (auto &e : op->slab_ev) CGB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    cudaEvent_t fork = op->slab_ev[64], *join = op->slab_ev + 65;
+    CGB_CUDA(cudaEventRecord(fork, st));
+    for (auto &q : op->slab_st) CGB_CUDA(cudaStreamWaitEvent(q, fork, 0));
+    int rc = CGB_OK;
+    for (int s = 0; s < S && rc == CGB_OK; ++s) {
+        cudaStream_t a = op->slab_st[s & 1];
+        rc = pass1(s, a);
+        if (rc != CGB_OK) break;
+        CGB_CUDA(cudaEventRecord(op->slab_ev[s], a));
+        CGB_CUDA(cudaStreamWaitEvent(op->slab_st[2], op->slab_ev[s], 0));
+        rc = pass2(s, op->slab_st[2]);
+    }
+    for (int i = 0; i < 3; ++i) {
+        cudaEventRecord(join[i], op->slab_st[i]);
+        cudaStreamWaitEvent(st, join[i], 0);
+    }
+    return rc;
+}
 
 // restricts the voxel kernels launched while it lives to voxels [v0, v1)
 struct VoxelRange {

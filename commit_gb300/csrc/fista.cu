@@ -1095,17 +1095,21 @@ struct BatchSolver {
                 if (op->nslab > 1) {
                     // slab by slab, the fibre passes right after each voxel pass (terms in L2)
                     int g0 = 0;
-                    for (int sl = 0; sl < op->nslab; ++sl) {
-                        {
+                    CGB_TRY(slab_schedule(
+                        op, st,
+                        [&](int sl, cudaStream_t q) {
                             VoxelRange vr(op, op->slab_v[sl], op->slab_v[sl + 1]);
                             int gs = 0;
-                            CGB_TRY(launch_adjoint_R(op, rr, V, reuse ? 2 : 1, y32, sqw32,
-                                                     partials + (size_t)sl * g0 * kRedSlots, st, &gs));
+                            const int rc = launch_adjoint_R(op, rr, V, reuse ? 2 : 1, y32, sqw32,
+                                                            partials + (size_t)sl * g0 * kRedSlots, q, &gs);
                             if (sl == 0) g0 = gs;
-                        }
-                        for (int r = 0; r < take; ++r)
-                            CGB_TRY(fibre_sum32_slab(op, scr[r], S[pp[r]].ws.grad, sl, st));
-                    }
+                            return rc;
+                        },
+                        [&](int sl, cudaStream_t q) {
+                            for (int r = 0; r < take; ++r)
+                                CGB_TRY(fibre_sum32_slab(op, scr[r], S[pp[r]].ws.grad, sl, q));
+                            return CGB_OK;
+                        }));
                     g = g0 * op->nslab;
                 } else {
                     CGB_TRY(launch_adjoint_R(op, rr, V, reuse ? 2 : 1, y32, sqw32, partials, st, &g));

@@ -262,6 +262,10 @@ static void free_op(cgb_op *op) {
     if (op->h_scal) cudaFreeHost(op->h_scal);
     for (cudaStream_t s : op->pipe_st)
         if (s) cudaStreamDestroy(s);
+    for (cudaStream_t s : op->slab_st)
+        if (s) cudaStreamDestroy(s);
+    for (cudaEvent_t e : op->slab_ev)
+        if (e) cudaEventDestroy(e);
     delete[] op->slab_v;
     for (cudaEvent_t e : op->pipe_ev)
         if (e) cudaEventDestroy(e);
@@ -528,7 +532,11 @@ int cgb_op_set_lut(cgb_op *op, const float *lutIC, const float *lutEC, const flo
 
 int cgb_op_set_slabs(cgb_op *op, int nslab, int *out) {
     if (!op) return fail(CGB_ERR_INVALID, "null handle");
-    if (nslab < 0 || nslab > 64) return fail(CGB_ERR_INVALID, "nslab must be 0..64");
+    if (nslab < 0) {  // read only
+        if (out) *out = op->nslab;
+        return CGB_OK;
+    }
+    if (nslab > 64) return fail(CGB_ERR_INVALID, "nslab must be 0..64");
     DeviceGuard g(op->device);
     CGB_CUDA(cudaDeviceSynchronize());
     CGB_TRY(build_slabs(op, nslab == 0 ? 0 : nslab));

@@ -249,16 +249,17 @@ static int adj_mix_slabs(cgb_op *op, int arith, const float *yin, int mode, cons
         return fibre_sum32(op, xout, st);
     }
     int g = 0;
-    for (int sl = 0; sl < op->nslab; ++sl) {
-        {
+    CGB_TRY(slab_schedule(
+        op, st,
+        [&](int sl, cudaStream_t q) {
             VoxelRange vr(op, op->slab_v[sl], op->slab_v[sl + 1]);
             int gs = 0;
-            CGB_TRY(adj_mix(op, arith, yin, mode, x, yobs, sqw, ax_a, ax_b, ca, cb, xout,
-                            partials ? partials + (size_t)sl * g * kRedSlots : nullptr, st, &gs));
+            const int rc = adj_mix(op, arith, yin, mode, x, yobs, sqw, ax_a, ax_b, ca, cb, xout,
+                                   partials ? partials + (size_t)sl * g * kRedSlots : nullptr, q, &gs);
             if (sl == 0) g = gs;
-        }
-        CGB_TRY(fibre_sum32_slab(op, op->scratch32, xout, sl, st));
-    }
+            return rc;
+        },
+        [&](int sl, cudaStream_t q) { return fibre_sum32_slab(op, op->scratch32, xout, sl, q); }));
     if (grid) *grid = g * op->nslab;
     return CGB_OK;
 }

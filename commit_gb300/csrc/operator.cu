@@ -194,16 +194,17 @@ static int run_adjoint(cgb_op *op, const double *yin, int in_mode, const double 
         // slab by slab: voxel pass, then the fibre pass while the slab's terms are in L2;
         // slab s writes its norm partials after the s * grid blocks of the earlier slabs
         int g = 0;
-        for (int sl = 0; sl < op->nslab; ++sl) {
-            {
+        CGB_TRY(slab_schedule(
+            op, st,
+            [&](int sl, cudaStream_t q) {
                 VoxelRange vr(op, op->slab_v[sl], op->slab_v[sl + 1]);
                 int gs = 0;
-                CGB_TRY(adjoint_ff(op, yin, in_mode, x, yobs, sqw, ax_a, ax_b, ca, cb, xout,
-                                   partials ? partials + (size_t)sl * g * kRedSlots : nullptr, st, &gs));
+                const int rc = adjoint_ff(op, yin, in_mode, x, yobs, sqw, ax_a, ax_b, ca, cb, xout,
+                                          partials ? partials + (size_t)sl * g * kRedSlots : nullptr, q, &gs);
                 if (sl == 0) g = gs;
-            }
-            CGB_TRY(fibre_sum_slab(op, xout, sl, st));
-        }
+                return rc;
+            },
+            [&](int sl, cudaStream_t q) { return fibre_sum_slab(op, xout, sl, q); }));
         if (grid_out) *grid_out = g * op->nslab;
         return CGB_OK;
     } else {

@@ -190,10 +190,10 @@ class LinearOperator:
             out[name] = (int(c.value), float(a.value), float(b.value))
         return out
 
-    def set_slabs(self, nslab: int = 0) -> int:
-        """Adjoint slab count (0: automatic, 1: off); returns the count in use."""
+    def set_slabs(self, nslab: int | None = 0) -> int:
+        """Adjoint slab count (0: automatic, 1: off, None: only read); returns the count in use."""
         out = ctypes.c_int32()
-        check(lib().cgb_op_set_slabs(self._h.ptr, int(nslab), ctypes.byref(out)))
+        check(lib().cgb_op_set_slabs(self._h.ptr, -1 if nslab is None else int(nslab), ctypes.byref(out)))
         return int(out.value)
 
     def batch_width(self, set_to: int | None = None) -> int:

@@ -106,7 +106,7 @@ int cgb_op_lut_grad(cgb_op *op, const double *x, const double *g, double *g_ic, 
  * Adjoint slabs: A' runs its voxel pass and fibre pass slab by slab (voxel ranges whose
  * per-segment terms fit in L2, so the fibre pass gathers them from L2).  nslab 0 chooses
  * the count from the problem size (the default at creation), 1 turns slabs off, 2..64
- * fixes it; *out (may be NULL) receives the count in use.  The sums are the same in every
+ * fixes it, a negative value only reads; *out (may be NULL) receives the count in use.  The sums are the same in every
  * case (each fibre's terms are added in the same order).
  */
 int cgb_op_set_slabs(cgb_op *op, int nslab, int *out);
