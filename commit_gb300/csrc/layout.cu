@@ -189,11 +189,12 @@ using namespace cgb;
 
 // Adjoint slabs.  The voxel pass writes one term per segment in voxel order and the fibre
 // pass gathers them in fibre order: a gather over the whole term stream (≈ 1 GB for 1M
-// streamlines) misses L2 on almost every access.  Cutting the voxels into slabs of about
-// kSlabTermBytes of terms and running the fibre pass of each slab right after its voxel
-// pass keeps the gathers in L2.  fib_slab[s*nF + f] is the first entry of fibre f's
+// streamlines) misses L2 on almost every access (ncu: 15.6 GB of DRAM reads for a 1.5 GB
+// pass).  Cutting the voxels into slabs of about kSlabTermBytes of FP64 terms and running
+// the fibre pass of each slab right after its voxel pass (overlapped, see slab_schedule)
+// keeps most gathers in L2.  fib_slab[s*nF + f] is the first entry of fibre f's
 // (ascending) position list that lies in slab s.
-constexpr double kSlabTermBytes = 40.0 * (1 << 20);
+constexpr double kSlabTermBytes = 128.0 * (1 << 20);  // measured best band: 8-12 slabs at 1M streamlines
 
 __global__ void k_fib_slabs(const uint32_t *__restrict__ fib_ptr, const uint32_t *__restrict__ fib_perm, int nF,
                             int S, const uint32_t *__restrict__ slab_pos, uint32_t *__restrict__ fib_slab) {
