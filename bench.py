@@ -30,12 +30,13 @@ sys.path.insert(0, ROOT)
 
 METRIC = 'A·x+Aᵀx operator pairs/s (1M-streamline workload)'
 
-# DRAM bytes (read + write) per launch from one ncu capture of the same command
+# DRAM bytes (read + write) per product from one ncu capture of the same workload
 # (`ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum
-# --clock-control none -k regex:"k_(forward_p|adjoint_p|fibre_sum)" ... python bench.py --steps 1
-# --warmup 1 --no-e2e --no-cpu`, one pass, full workload; profiles/operator_ff_hcp1m.md).
-# Keyed by (workload, streamlines, arith); the A' entry is pass 1 + pass 2.
-MEASURED_TRAFFIC = {('hcp_1m', 1000000, 'ff'): {'forward': 2642033408, 'adjoint': None}}
+# --clock-control none -k regex:"k_(forward_p|adjoint_p|fibre_sum)" --csv python bench.py
+# --steps 1 --warmup 1 --no-e2e --no-cpu`, one pass, full workload; summarised in
+# profiles/operator_ff_hcp1m.md).  Keyed by (workload, streamlines, arith); the A' entry
+# is the 7 slab voxel passes plus the 7 slab fibre passes of one product.
+MEASURED_TRAFFIC = {('hcp_1m', 1000000, 'ff'): {'forward': 2636454144, 'adjoint': 11855195392}}
 
 
 def parse():
@@ -237,6 +238,13 @@ def workload_config(spec, D, K, args):
             'arith': args.arith, 'l2': 'inputs larger than L2 (y is nV*nS f64), no flush'}
 
 
+def launches_per_pair(A, reduced: bool) -> int:
+    """Kernels of one A + A' pair: the forward, then per adjoint slab a voxel pass and a fibre
+    pass (one of each without slabs); the FP32-vector path adds two conversions."""
+    ns = max(1, A.set_slabs(None))
+    return 1 + 2 * ns + (2 if reduced else 0)
+
+
 def traffic_for(args, spec, dom: str):
     t = MEASURED_TRAFFIC.get((args.workload, spec.n_fibers, args.arith))
     if not t:
@@ -329,7 +337,7 @@ def run_ours(args):
                         'traffic': traffic_for(args, spec, dom), 'algorithmic_bytes_per_launch': nbytes,
                         'forward_ms': fwd_ms, 'adjoint_ms': adj_ms,
                         'fma_per_product': nfma, 'achieved_gfma_s': nfma / (dom_ms / 1000.0) / 1e9},
-           'clocks': clk, 'gpu_launches': args.steps * (1 + 2), 'setup_s': {'generate': tgen},
+           'clocks': clk, 'gpu_launches': args.steps * launches_per_pair(A, reduced), 'setup_s': {'generate': tgen},
            'occupancy_tuning': A.occupancy(), 'adjoint_slabs': A.set_slabs(None)}
     # end to end through the public API on pinned host buffers
     if not args.no_e2e and not reduced:
