@@ -546,6 +546,19 @@ def run_demo(args):
         dt = time.perf_counter() - t0
         out[name] = {'seconds': dt, 'ms_per_iteration': 1000.0 * dt / n, 'iterations': d['iterations'],
                      'cost_function': d['cost_function']}
+    # reduced-precision operator: errors of y = A x, of the FISTA solution x and of its cost
+    # against the float-float FP64 path (same 200 iterations)
+    xf, df = solvers.solve(y, A, A.T, tol_fun=0.0, tol_x=0.0, max_iter=n, verbose=0,
+                           regularisation=solvers.init_regularisation(dict(rp)))
+    yf = A.dot(x)
+    errs = {}
+    for ar in ('bf16', 'fp16', 'f32'):
+        yr = A.dot(x.float(), arith=ar).double()
+        xr, dr = solvers.solve(y, A, A.T, tol_fun=0.0, tol_x=0.0, max_iter=n, verbose=0,
+                               regularisation=solvers.init_regularisation(dict(rp)), arith=ar)
+        errs[ar] = {'y_rel': float(torch.linalg.norm(yr - yf) / torch.linalg.norm(yf)),
+                    'x_rel': float(torch.linalg.norm(xr - xf) / torch.linalg.norm(xf)),
+                    'cost_rel': abs(dr['cost_function'] - df['cost_function']) / df['cost_function']}
     cpu = None
     if not args.no_cpu:
         cpu = cpu_reference(D, K, 1.0, 20, 2)
@@ -555,7 +568,8 @@ def run_demo(args):
                                   f'{int(D["IC"]["nVOX"])} voxels, {int(D["IC"]["n"])} segments, nS=66',
                       'fista': '200 nnls iterations, tolerances off'},
            'pair_ms': pair_ms, 'pairs_per_s': 1000.0 / pair_ms, 'fista': out,
-           'graph_speedup_vs_host_loop': out['host_loop']['seconds'] / out['graph']['seconds']}
+           'graph_speedup_vs_host_loop': out['host_loop']['seconds'] / out['graph']['seconds'],
+           'reduced_precision_errors_vs_fp64': errs}
     if cpu is not None:
         res['cpu_baseline'] = cpu
     print(json.dumps(res))

@@ -121,3 +121,20 @@ def test_graph_mode_matches_host_loop(name, variant):
     assert G.rel(xg, f['x']) <= 1e-8
     for k in ('residual', 'regterm', 'cost_function', 'abs_cost', 'rel_cost', 'abs_x', 'rel_x'):
         assert dg[k] == dh[k], k
+
+
+def test_graph_mode_with_adjoint_slabs():
+    """Inside the graph capture the slab schedule runs its steps in order on one stream; the
+    iterates stay bit-identical to the host loop's (three-stream schedule)."""
+    from commit_gb300 import solvers, synth
+    from commit_gb300.operator import LinearOperator
+    D, K = synth.make_dictionary(synth.scaled_spec('demo_5k', n_fibers=8000))
+    A = LinearOperator(D, K, None)
+    assert A.set_slabs(4) == 4
+    x0 = synth.make_x(A.nCOLS, 1)
+    y = synth.make_signal(A.dot(x0), 2)
+    kw = dict(tol_fun=1e-6, tol_x=1e-8, max_iter=60, verbose=0, momentum_reuse=False)
+    xh, dh = solvers.solve(y, A, A.T, **kw)
+    xg, dg = solvers.solve(y, A, A.T, graph=True, **kw)
+    assert dg['iterations'] == dh['iterations']
+    assert np.array_equal(xg, xh)
