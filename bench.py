@@ -75,6 +75,24 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(value: float, device=None) -> float:
+    """The largest of the ranks' values (the job's time is its slowest replica's); the
+    value itself with one rank."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(units_per_rank: float, seconds_max: float, world: int) -> float:
+    """Whole-job throughput of N independent replicas: all ranks' units over the slowest
+    rank's time (weak scaling)."""
+    return units_per_rank * world / seconds_max
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
     FIELDS = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
@@ -317,14 +335,12 @@ def run_ours(args):
     torch.cuda.synchronize()
     ms = e_start.elapsed_time(e_end)
     if ws > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = max_over_ranks(ms, dev)
         torch.distributed.barrier()
-        ms = float(t.item())
     clk = clocks.stop()
     fwd_ms = statistics.mean(a.elapsed_time(b) for a, b, _ in ev)
     adj_ms = statistics.mean(b.elapsed_time(c) for _, b, c in ev)
-    value = args.steps * ws / (ms / 1000.0)
+    value = replica_value(args.steps, ms / 1000.0, ws)
     peaks = measured_peaks()
     dom, dom_ms = ('adjoint (voxel pass + fibre sum)', adj_ms) if adj_ms >= fwd_ms else ('forward k_forward', fwd_ms)
     achieved = nbytes / (dom_ms / 1000.0) / 1e9
@@ -356,10 +372,8 @@ def run_ours(args):
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
         if ws > 1:
-            t = torch.tensor([dt], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            dt = float(t.item())
-        out['e2e'] = {'value': args.steps * ws / dt, 'unit': 'pairs/s', 'h2d_bytes_per_step': (ncols + nrows) * 8,
+            dt = max_over_ranks(dt, dev)
+        out['e2e'] = {'value': replica_value(args.steps, dt, ws), 'unit': 'pairs/s', 'h2d_bytes_per_step': (ncols + nrows) * 8,
                       'd2h_bytes_per_step': (nrows + ncols) * 8}
     if rank == 0 and ws == 1 and not args.no_cpu:
         out['cpu_baseline'] = cpu_reference(D, K, args.sample_frac, 3, 1)
