@@ -31,6 +31,40 @@ int check_lengths(const cgb_op *op, int adjoint, int64_t in_len, int64_t out_len
 // same per-voxel computation).
 static constexpr int kPipe = 8;
 
+// Direct row access: when the caller's row vector (y, the large one) is in page-locked host
+// memory, the voxel kernels read or write it in place through its device mapping (on
+// GB300 the host memory sits behind NVLink-C2C), so no row-sized copy or staging buffer is
+// needed; the column vector (gathered at random by A) is still copied.  Used when the
+// handle's host mode is automatic (0) or direct (2).
+static bool direct_rows(const cgb_op *op, const double *rows) {
+    if (op->host_mode == 1 || op->nolut || op->nrows < ((int64_t)1 << 20)) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, rows) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost && a.devicePointer != nullptr;
+}
+
+static int apply_host_direct(cgb_op *op, int adjoint, const double *in, int64_t in_len, double *out,
+                             int64_t out_len) {
+    cudaStream_t st = nullptr;
+    cudaPointerAttributes a;
+    if (!adjoint) {
+        CGB_CUDA(cudaPointerGetAttributes(&a, out));
+        double *yd = (double *)a.devicePointer;
+        CGB_CUDA(cudaMemcpyAsync(op->d_in, in, in_len * sizeof(double), cudaMemcpyHostToDevice, st));
+        CGB_TRY(cgb_op_apply(op, 0, op->d_in, in_len, yd, out_len, CGB_DTYPE_F64, op->arith, st));
+    } else {
+        CGB_CUDA(cudaPointerGetAttributes(&a, in));
+        const double *yd = (const double *)a.devicePointer;
+        CGB_TRY(cgb_op_apply(op, 1, yd, in_len, op->d_out, out_len, CGB_DTYPE_F64, op->arith, st));
+        CGB_CUDA(cudaMemcpyAsync(out, op->d_out, out_len * sizeof(double), cudaMemcpyDeviceToHost, st));
+    }
+    CGB_CUDA(cudaStreamSynchronize(st));
+    return CGB_OK;
+}
+
 static bool pipelined(const cgb_op *op) {
     return op->arith == CGB_ARITH_FF && op->ff_variant != 0 && !op->nolut && op->nV >= 4 * kPipe &&
            op->nrows >= ((int64_t)1 << 22);
@@ -144,6 +178,8 @@ int cgb_op_apply_host(cgb_op *op, int adjoint, const double *in, int64_t in_len,
         CGB_CUDA(cudaMalloc((void **)&op->d_out, need * sizeof(double)));
         op->d_in_len = op->d_out_len = need;
     }
+    if (in_len > 0 && direct_rows(op, adjoint ? in : out))
+        return apply_host_direct(op, adjoint, in, in_len, out, out_len);
     if (in_len > 0 && pipelined(op)) return apply_host_pipelined(op, adjoint, in, in_len, out, out_len);
     cudaStream_t st = nullptr;
     if (in_len > 0) CGB_CUDA(cudaMemcpyAsync(op->d_in, in, in_len * sizeof(double), cudaMemcpyHostToDevice, st));
@@ -165,5 +201,13 @@ extern "C" int cgb_op_occupancy(cgb_op *op, int slot, int set, int *choice, floa
     if (choice) *choice = op->occ_choice[slot];
     if (ms_a) *ms_a = op->occ_ms[slot][0];
     if (ms_b) *ms_b = op->occ_ms[slot][1];
+    return CGB_OK;
+}
+
+extern "C" int cgb_op_host_mode(cgb_op *op, int mode, int *out) {
+    if (!op) return fail(CGB_ERR_INVALID, "null handle");
+    if (mode > 2) return fail(CGB_ERR_INVALID, "host mode must be 0 (automatic), 1 (staged) or 2 (direct)");
+    if (mode >= 0) op->host_mode = mode;
+    if (out) *out = op->host_mode;
     return CGB_OK;
 }

@@ -109,6 +109,7 @@ struct cgb_op {
     int64_t d_in_len, d_out_len;
     cudaStream_t pipe_st[2];        // host-buffer pipeline: compute and copy streams (created on first use)
     int vr0, vr1;                   // voxel range [vr0, vr1) of the next voxel-kernel launches (vr1 0: all)
+    int host_mode;                  // host-buffer products: 0 automatic, 1 staged copies, 2 direct row access
     // adjoint slabs: voxel ranges whose per-segment terms fit in L2, so the fibre pass of a
     // slab gathers them from L2 right after the voxel pass wrote them (see run_adjoint)
     int nslab;                      // 1: no slabs

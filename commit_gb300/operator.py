@@ -190,6 +190,13 @@ class LinearOperator:
             out[name] = (int(c.value), float(a.value), float(b.value))
         return out
 
+    def host_mode(self, mode: int | None = None) -> int:
+        """Host-buffer products: 0 automatic (direct row access for page-locked rows),
+        1 staged copies, 2 direct; None only reads."""
+        out = ctypes.c_int32()
+        check(lib().cgb_op_host_mode(self._h.ptr, -1 if mode is None else int(mode), ctypes.byref(out)))
+        return int(out.value)
+
     def set_slabs(self, nslab: int | None = 0) -> int:
         """Adjoint slab count (0: automatic, 1: off, None: only read); returns the count in use."""
         out = ctypes.c_int32()

@@ -111,6 +111,15 @@ int cgb_op_lut_grad(cgb_op *op, const double *x, const double *g, double *g_ic, 
  */
 int cgb_op_set_slabs(cgb_op *op, int nslab, int *out);
 
+/*
+ * Host-buffer products (cgb_op_apply_host): mode 0 (default) reads / writes a page-locked
+ * row vector in place through its device mapping and copies only the column vector, else
+ * stages both through device buffers with the copies pipelined against the kernels; 1
+ * always stages; 2 is the same as 0.  A negative mode only reads; *out (may be NULL)
+ * receives the mode.  Results are identical in every mode.
+ */
+int cgb_op_host_mode(cgb_op *op, int mode, int *out);
+
 /* Select the arithmetic used by later FP64 applies (CGB_ARITH_F64 / CGB_ARITH_FF). */
 int cgb_op_set_arith(cgb_op *op, int arith);
 
