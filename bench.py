@@ -373,7 +373,7 @@ def run_ours(args):
         dt = time.perf_counter() - t0
         if ws > 1:
             dt = max_over_ranks(dt, dev)
-out['e2e'] = {'value': replica_value(args.steps, dt, ws), 'unit': 'pairs/s', 'h2d_bytes_per_step': (ncols + nrows) * 8,
+        out['e2e'] = {'value': replica_value(args.steps, dt, ws), 'unit': 'pairs/s', 'h2d_bytes_per_step': (ncols + nrows) * 8,
                       'd2h_bytes_per_step': (nrows + ncols) * 8,
                       'host_path': ('page-locked host vectors through LinearOperator.dot (cgb_op_apply_host): '
                                     'x copied to and from the device, the row vector read / written in place '
