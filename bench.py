@@ -55,6 +55,9 @@ def parse():
     p.add_argument('--demo', action='store_true',
                    help='demo-scale case (5k streamlines, nS=66): A*x, A\'y and 200 FISTA nnls iterations, '
                         'host-driven loop vs graph-captured loop, next to the reference CPU operator')
+    p.add_argument('--trk2dict', action='store_true',
+                   help='streamline voxelisation (trk2dictionary) on the device vs the CPU restatement')
+    p.add_argument('--t2d-fibers', type=int, default=200000)
     p.add_argument('--batch', action='store_true',
                    help='regularisation paths: 8 tractograms x 16 lambdas, batched BF16 vs sequential plain solves')
     p.add_argument('--batch-tracts', type=int, default=8, help='number of tractograms of the batched workload')
@@ -594,12 +597,76 @@ def run_demo(args):
     return 0
 
 
+def run_trk2dict(args):
+    """Voxelisation of synthetic streamlines (random smooth curves of 1-300 points, 0.7 mm
+    steps) on the 145x174x145 grid at 1.25 mm with the 500-direction hash table: streamlines
+    per second through commit_gb300.trk2dictionary.voxelise (host arrays in and out) against
+    the CPU restatement of the reference's voxeliser (one thread) on a sample."""
+    import torch
+    from commit_gb300 import trk2dictionary as V
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    import trk2dict as T
+    rng = np.random.default_rng(20)
+    dim, pix = (145, 174, 145), (1.25, 1.25, 1.25)
+    nf = args.t2d_fibers
+    n_pts = rng.integers(1, 300, size=nf)
+    off = np.concatenate([[0], np.cumsum(n_pts)]).astype(np.int64)
+    ext = np.array(dim) * np.array(pix)
+    start = rng.uniform(0.2, 0.8, (nf, 3)) * ext
+    steps = rng.normal(size=(int(off[-1]), 3))
+    d = np.cumsum(0.3 * steps, axis=0)                       # smooth random directions
+    d -= np.repeat(d[off[:-1]], n_pts, axis=0)
+    d += np.repeat(rng.normal(size=(nf, 3)), n_pts, axis=0)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    seg = 0.7 * d
+    pos = np.cumsum(seg, axis=0)
+    pos -= np.repeat(pos[off[:-1]], n_pts, axis=0)
+    pts = (pos + np.repeat(start, n_pts, axis=0)).astype(np.float32)
+    dirs = synth_dirs(500)
+    H = V.hash_table(dirs)
+    for _ in range(max(1, args.warmup)):
+        V.voxelise(pts[:off[min(nf, 1000)]], off[:min(nf, 1000) + 1], dim, pix, H)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        r = V.voxelise(pts, off, dim, pix, H)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    gpu_s = statistics.median(times)
+    ns = min(nf, 5000)
+    t0 = time.perf_counter()
+    rc = T.voxelise(pts[:off[ns]], off[:ns + 1], dim, pix, H)
+    cpu_s = time.perf_counter() - t0
+    rg = V.voxelise(pts[:off[ns]], off[:ns + 1], dim, pix, H)
+    same = all(np.array_equal(rg[c][k], rc[c][k]) for c in ('IC', 'TRK') for k in rc[c])
+    out = {'metric': 'streamline voxelisation (trk2dictionary IC/EC/ISO) streamlines/s', 'value': nf / gpu_s,
+           'unit': 'streamlines/s', 'higher_is_better': True, 'n_gpus': 1, 'data': 'synthetic',
+           'config': {'workload': f'{nf} random smooth streamlines, 1-300 points of 0.7 mm, grid 145x174x145 '
+                                  f'at 1.25 mm, 500 directions, intersections on',
+                      'points': int(off[-1]), 'segments': int(r['IC']['f'].size), 'kept': int(r['TRK']['kept'].sum())},
+           'seconds': gpu_s, 'e2e': {'value': nf / gpu_s, 'unit': 'streamlines/s',
+                                     'note': 'host arrays in and out, all copies inside the timed call'},
+           'cpu_baseline': {'value': ns / cpu_s, 'unit': 'streamlines/s', 'cores': 1, 'kind': 'port',
+                            'sample': f'first {ns} streamlines, {cpu_s:.2f} s'},
+           'sample_bitwise_equal_to_cpu': bool(same)}
+    print(json.dumps(out))
+    return 0
+
+
+def synth_dirs(n: int) -> np.ndarray:
+    from commit_gb300 import synth
+    return synth.fibonacci_sphere(n, hemisphere=True)
+
+
 def main():
     args = parse()
     if args.impl == 'reference':
         return run_reference(args)
     if args.demo:
         return run_demo(args)
+    if args.trk2dict:
+        return run_trk2dict(args)
     if args.batch:
         return run_batch(args)
     return run_ours(args)
