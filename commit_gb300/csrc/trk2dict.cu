@@ -58,6 +58,22 @@ struct Sink {
     float flen, flentot;
 };
 
+// (int)round(atan2(y, x) in degrees) as the reference evaluates it in FP64.  The FP64
+// atan2 is the most expensive step of a piece on this part (FP64 is 1/58 of the FP32 rate),
+// so it is evaluated in FP32 first (accurate to a few 1e-5 degree here) and again in FP64
+// only when the FP32 value lies within 1e-3 degree of a rounding boundary, or an input is
+// below FP32's normal range; the result is the FP64 one in every case.
+__device__ __forceinline__ int round_deg(double y, double x) {
+    const double ay = fabs(y), ax = fabs(x);
+    const bool small = (ay != 0.0 && ay < 1e-30) || (ax != 0.0 && ax < 1e-30);
+    if (!small) {
+        const float v = atan2f((float)y, (float)x) * 57.2957795130823208768f;
+        const float fr = v - floorf(v);
+        if (fabsf(fr - 0.5f) > 1e-3f) return (int)floorf(v + 0.5f);
+    }
+    return (int)round(atan2(y, x) / 3.14159265358979323846 * 180.0);
+}
+
 __device__ void add_piece(const T2DCfg &c, D3 P1, D3 P2, int k, double w, const int16_t *__restrict__ hash,
                           const uint8_t *__restrict__ mask, Sink &S) {
     D3 d;
@@ -78,10 +94,8 @@ __device__ void add_piece(const T2DCfg &c, D3 P1, D3 P2, int k, double w, const 
     const int vz = (int)floor(0.5 * (P1.z + P2.z) / (double)c.pz);
     if (vx >= c.dimx || vx < 0 || vy >= c.dimy || vy < 0 || vz >= c.dimz || vz < 0) return;
     if (mask && mask[vz + (int64_t)c.dimz * (vy + (int64_t)c.dimy * vx)] == 0) return;
-    const double lon = atan2(d.y, d.x);
-    const double colat = atan2(sqrt(d.x * d.x + d.y * d.y), d.z);
-    const int ox = (int)round(colat / 3.14159265358979323846 * 180.0);
-    const int oy = (int)round(lon / 3.14159265358979323846 * 180.0);
+    const int oy = round_deg(d.y, d.x);
+    const int ox = round_deg(sqrt(d.x * d.x + d.y * d.y), d.z);
     // the reference indexes hash[ox*181 + oy] unchecked; an index outside the table (which
     // it would read out of bounds) is clamped to the table
     int hi = ox * 181 + oy;
@@ -121,9 +135,11 @@ __global__ void k_walk(const T2DCfg c, const float *__restrict__ pts, const int6
                        const uint8_t *__restrict__ blur_apply, const int16_t *__restrict__ hash,
                        const uint8_t *__restrict__ mask, const int64_t *__restrict__ poff, uint64_t *__restrict__ keys,
                        double *__restrict__ lens, int64_t *__restrict__ cnt, float *__restrict__ flen,
-                       float *__restrict__ flentot) {
-    const int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (f >= nfib) return;
+                       float *__restrict__ flentot, const uint32_t *__restrict__ order) {
+    // streamlines in order of decreasing point count, so a warp's walks have similar lengths
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (tid >= nfib) return;
+    const int64_t f = order ? (int64_t)order[tid] : tid;
     Sink S;
     S.key = keys ? keys + poff[f] : nullptr;
     S.len = keys ? lens + poff[f] : nullptr;
@@ -214,6 +230,15 @@ __global__ void k_walk(const T2DCfg c, const float *__restrict__ pts, const int6
         flen[f] = S.flen;
         flentot[f] = S.flentot;
     }
+}
+
+__global__ void k_npts(const int64_t *__restrict__ off, int64_t nfib, uint32_t *__restrict__ npts,
+                       uint32_t *__restrict__ ids) {
+    const int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (f >= nfib) return;
+    const int64_t n = off[f + 1] - off[f];
+    npts[f] = (uint32_t)(n > 0xffffffffll ? 0xffffffffll : n);
+    ids[f] = (uint32_t)f;
 }
 
 // merged segments of streamline f: runs of equal keys summed in FP32 in generation order.
@@ -339,10 +364,8 @@ __global__ void k_ec(int pass, const ECCfg c, const double *__restrict__ tdi, co
                         d.y = -d.y;
                         d.z = -d.z;
                     }
-                    const double colat = atan2(sqrt(d.x * d.x + d.y * d.y), d.z);
-                    const double lon = atan2(d.y, d.x);
-                    const int ox = (int)round(colat / 3.14159265358979323846 * 180.0);
-                    const int oy = (int)round(lon / 3.14159265358979323846 * 180.0);
+                    const int ox = round_deg(sqrt(d.x * d.x + d.y * d.y), d.z);
+                    const int oy = round_deg(d.y, d.x);
                     int hi = ox * 181 + oy;
                     hi = hi < 0 ? 0 : (hi > 181 * 181 - 1 ? 181 * 181 - 1 : hi);
                     if (pass) {
@@ -467,6 +490,7 @@ int cgb_trk2dict(const cgb_t2d_params *prm, const float *pts, const int64_t *off
     double *lens = nullptr, *lens2 = nullptr;
     float *vval = nullptr, *vval2 = nullptr;
     int64_t *vcnt = nullptr, *voff = nullptr;
+    uint32_t *npts = nullptr, *order = nullptr;  // [2*nfib]: counts / ids, sorted keys / sorted ids
     int rc = CGB_OK;
     auto body = [&]() -> int {
         CGB_TRY(dmalloc(&cnt, nf1 + 1, st));
@@ -476,9 +500,24 @@ int cgb_trk2dict(const cgb_t2d_params *prm, const float *pts, const int64_t *off
         CGB_CUDA(cudaMemsetAsync(cnt, 0, (nf1 + 1) * sizeof(int64_t), st));
         const int tb = 128;
         const int gb = (int)((nfib + tb - 1) / tb);
+        if (nfib > 0 && nfib < ((int64_t)1 << 31)) {
+            CGB_TRY(dmalloc(&npts, 2 * nf1, st));
+            CGB_TRY(dmalloc(&order, 2 * nf1, st));
+            k_npts<<<gb, tb, 0, st>>>(offsets, nfib, npts, npts + nf1);
+            CGB_CUDA(cudaGetLastError());
+            size_t bytes = 0;
+            CGB_CUDA(cub::DeviceRadixSort::SortPairsDescending(nullptr, bytes, npts, order + nf1, npts + nf1, order,
+                                                                (int)nfib, 0, 32, st));
+            void *t = nullptr;
+            CGB_TRY(dmalloc((char **)&t, bytes, st));
+            const cudaError_t e = cub::DeviceRadixSort::SortPairsDescending(t, bytes, npts, order + nf1, npts + nf1,
+                                                                             order, (int)nfib, 0, 32, st);
+            cudaFreeAsync(t, st);
+            CGB_CUDA(e);
+        }
         if (nfib > 0) {
             k_walk<<<gb, tb, 0, st>>>(c, pts, offsets, nfib, blur_apply, hash, mask, nullptr, nullptr, nullptr, cnt,
-                                      flen, flentot);
+                                      flen, flentot, order);
             CGB_CUDA(cudaGetLastError());
         }
         CGB_TRY(exclusive_scan(cnt, poff, nfib + 1, st));
@@ -490,7 +529,7 @@ int cgb_trk2dict(const cgb_t2d_params *prm, const float *pts, const int64_t *off
         CGB_TRY(dmalloc(&lens2, npieces, st));
         if (nfib > 0) {
             k_walk<<<gb, tb, 0, st>>>(c, pts, offsets, nfib, blur_apply, hash, mask, poff, keys, lens, nullptr, nullptr,
-                                      nullptr);
+                                      nullptr, order);
             CGB_CUDA(cudaGetLastError());
         }
         CGB_TRY(seg_sort(keys, keys2, lens, lens2, npieces, nfib, poff, st));
@@ -582,8 +621,8 @@ int cgb_trk2dict(const cgb_t2d_params *prm, const float *pts, const int64_t *off
         return CGB_OK;
     };
     rc = body();
-    void *tmp[] = {cnt,   poff,  mcnt, soff,  kid,   kept64, flen, flentot, keys,
-                   keys2, vkey,  vkey2, lens, lens2, vval, vval2,  vcnt, voff};
+    void *tmp[] = {cnt,  poff, mcnt, soff, kid,  kept64, flen, flentot, keys, keys2,
+                   vkey, vkey2, lens, lens2, vval, vval2, vcnt, voff, npts, order};
     for (void *q : tmp)
         if (q) cudaFreeAsync(q, st);
     if (rc == CGB_OK) {
