@@ -203,6 +203,33 @@ def sample_slab(D, K, frac: float):
     return {'IC': IC, 'EC': EC, 'ISO': ISO}, (s1 - s0) / n, (lo, hi)
 
 
+def cpu_reference_fista(D, K, frac, iters):
+    """Per-iteration time of the reference's FISTA (numpy restatement of solvers.py driving
+    the reference's compiled operator, all host cores) on the central voxel slab of the
+    workload, scaled to the whole workload by segment share; nnls on all compartments."""
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    import oracle as O
+    import build_ref
+    Ds, share, (lo, hi) = sample_slab(D, K, frac)
+    threads = min(os.cpu_count() or 1, 255)
+    kind = 'port'
+    try:
+        if build_ref.generate() and build_ref.compile_operator() and O.ref_available():
+            kind = 'reference'
+    except Exception:
+        kind = 'port'
+    A = O.RefOperator(Ds, K, O.set_threads(Ds, threads)) if kind == 'reference' else \
+        O.PortOperator(Ds, K, None, nthreads=threads)
+    y = A.dot(np.random.default_rng(3).uniform(0.0, 1.0, A.nCOLS))
+    rp = O.reg_params(Ds, K)
+    t0 = time.perf_counter()
+    O.solve(y, A, A.T, tol_fun=0.0, tol_x=0.0, max_iter=iters, verbose=0, regularisation=O.init_regularisation(rp))
+    dt = (time.perf_counter() - t0) / iters
+    return {'value': 1000.0 * dt / share, 'unit': 'ms/iteration', 'cores': threads, 'kind': kind,
+            'sample': f'central voxel slab [{lo},{hi}) = {share * 100:.2f}% of the IC segments, {iters} iterations '
+                      f'in {dt * iters:.2f} s (initialisation included), time scaled by segment share'}
+
+
 def cpu_reference(D, K, frac, steps, warmup):
     """Time the reference CPU operator (oracle/_ref if compiled for this host, else the
     C restatement) on a voxel-slab sample; returns a cpu_baseline dict (pairs/s scaled
@@ -445,6 +472,8 @@ def run_fista(args, spec, D, K, dev):
            'plain': {'iterations': int(d_plain['iterations']), 'seconds': float(tr_p[-1, 0]),
                      'ms_per_iteration': 1000.0 * float(tr_p[-1, 0]) / len(tr_p), 'final_rel': float(tr_p[-1, 1])},
            'mixed': mixed, 'reference_solve_s': t_ref}
+    if not args.no_cpu:
+        out['cpu_baseline'] = cpu_reference_fista(D, K, args.sample_frac, 5)
     print(json.dumps(out))
     return 0
 
