@@ -54,7 +54,7 @@ __device__ __forceinline__ uint64_t seg_key(unsigned o, unsigned z, unsigned y, 
 struct Sink {
     uint64_t *key;       // null: count only
     double *len;
-    int64_t n;
+    int64_t n, cap;      // pieces produced; room at key / len
     float flen, flentot;
 };
 
@@ -100,7 +100,7 @@ __device__ void add_piece(const T2DCfg &c, D3 P1, D3 P2, int k, double w, const 
     // it would read out of bounds) is clamped to the table
     int hi = ox * 181 + oy;
     hi = hi < 0 ? 0 : (hi > 181 * 181 - 1 ? 181 * 181 - 1 : hi);
-    if (S.key) {
+    if (S.key && S.n < S.cap) {
         S.key[S.n] = seg_key((uint16_t)hash[hi], (unsigned)vz, (unsigned)vy, (unsigned)vx);
         S.len[S.n] = w * len;
     }
@@ -143,6 +143,7 @@ __global__ void k_walk(const T2DCfg c, const float *__restrict__ pts, const int6
     Sink S;
     S.key = keys ? keys + poff[f] : nullptr;
     S.len = keys ? lens + poff[f] : nullptr;
+    S.cap = keys ? poff[f + 1] - poff[f] : 0;
     S.n = 0;
     S.flen = 0.f;
     S.flentot = 0.f;
@@ -225,11 +226,47 @@ __global__ void k_walk(const T2DCfg c, const float *__restrict__ pts, const int6
             }
         }
     }
-    if (!keys) {
+    if (cnt) {
         cnt[f] = S.n;
         flen[f] = S.flen;
         flentot[f] = S.flentot;
     }
+}
+
+// Room for the pieces of streamline f in the one-walk path: per step at most one piece per
+// voxel face crossed plus the piece that ends the step, estimated from the raw points with
+// three spare pieces per step, for every replica in use.  The walk writes min(count, room)
+// pieces and reports the count, so a streamline whose projected steps outgrow the estimate
+// is detected and the exact two-walk path is taken instead.
+__global__ void k_room(const T2DCfg c, const float *__restrict__ pts, const int64_t *__restrict__ off, int64_t nfib,
+                       const uint8_t *__restrict__ blur_apply, int64_t *__restrict__ room) {
+    const int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (f >= nfib) return;
+    const int64_t b = off[f];
+    const int N = (int)(off[f + 1] - b);
+    if (N <= 2) {
+        room[f] = 0;
+        return;
+    }
+    const float *p = pts + 3 * b;
+    float r = 0.f;
+    for (int i = 1; i < N; ++i) {
+        const float dx = fabsf(p[3 * i] - p[3 * i - 3]), dy = fabsf(p[3 * i + 1] - p[3 * i - 2]),
+                    dz = fabsf(p[3 * i + 2] - p[3 * i - 1]);
+        r += c.do_intersect ? dx / c.px + dy / c.py + dz / c.pz + 4.f : 1.f;
+    }
+    const int reps = (blur_apply && blur_apply[f]) ? c.n_rep : 1;
+    room[f] = (int64_t)ceilf(r) * reps + 16;
+}
+
+// end of each streamline's pieces (begin + count) and whether any count exceeded its room
+__global__ void k_ends(const int64_t *__restrict__ poff, const int64_t *__restrict__ cnt, int64_t nfib,
+                       int64_t *__restrict__ pend, int *__restrict__ overflow) {
+    const int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (f >= nfib) return;
+    const int64_t room = poff[f + 1] - poff[f];
+    pend[f] = poff[f] + (cnt[f] < room ? cnt[f] : room);
+    if (cnt[f] > room) *overflow = 1;
 }
 
 __global__ void k_npts(const int64_t *__restrict__ off, int64_t nfib, uint32_t *__restrict__ npts,
@@ -244,6 +281,7 @@ __global__ void k_npts(const int64_t *__restrict__ off, int64_t nfib, uint32_t *
 // merged segments of streamline f: runs of equal keys summed in FP32 in generation order.
 // Pass 0 counts them (0 for a streamline that is not kept); pass 1 writes them.
 __global__ void k_merge(int pass, int64_t nfib, const T2DCfg c, const int64_t *__restrict__ poff,
+                        const int64_t *__restrict__ pend,
                         const uint64_t *__restrict__ keys, const double *__restrict__ lens,
                         const float *__restrict__ flen, const int64_t *__restrict__ soff,
                         const int64_t *__restrict__ kid, int64_t *__restrict__ mcnt, uint8_t *__restrict__ kept,
@@ -252,7 +290,7 @@ __global__ void k_merge(int pass, int64_t nfib, const T2DCfg c, const int64_t *_
                         float *__restrict__ ic_len, uint64_t *__restrict__ vkey, float *__restrict__ vval) {
     const int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (f >= nfib) return;
-    const int64_t b = poff[f], e = poff[f + 1];
+    const int64_t b = poff[f], e = pend[f];
     const bool keep = e > b && flen[f] > c.min_fiber_len && flen[f] < c.max_fiber_len;
     if (pass == 0) {
         kept[f] = keep ? 1 : 0;
@@ -415,15 +453,16 @@ int exclusive_scan(const int64_t *in, int64_t *out, int64_t n, cudaStream_t st) 
 
 template <class V>
 int seg_sort(const uint64_t *kin, uint64_t *kout, const V *vin, V *vout, int64_t n, int64_t nseg, const int64_t *segoff,
-             cudaStream_t st) {
+             cudaStream_t st, const int64_t *segend = nullptr) {
     if (n == 0) return CGB_OK;
+    if (!segend) segend = segoff + 1;
     size_t bytes = 0;
     CGB_CUDA(cub::DeviceSegmentedSort::StableSortPairs(nullptr, bytes, kin, kout, vin, vout, n, nseg, segoff,
-                                                       segoff + 1, st));
+                                                       segend, st));
     void *t = nullptr;
     CGB_TRY(dmalloc((char **)&t, bytes, st));
     const cudaError_t e = cub::DeviceSegmentedSort::StableSortPairs(t, bytes, kin, kout, vin, vout, n, nseg, segoff,
-                                                                    segoff + 1, st);
+                                                                    segend, st);
     cudaFreeAsync(t, st);
     CGB_CUDA(e);
     return CGB_OK;
@@ -491,6 +530,8 @@ int cgb_trk2dict(const cgb_t2d_params *prm, const float *pts, const int64_t *off
     float *vval = nullptr, *vval2 = nullptr;
     int64_t *vcnt = nullptr, *voff = nullptr;
     uint32_t *npts = nullptr, *order = nullptr;  // [2*nfib]: counts / ids, sorted keys / sorted ids
+    int64_t *pend = nullptr;                      // end of each streamline's pieces
+    int *oflow = nullptr;
     int rc = CGB_OK;
     auto body = [&]() -> int {
         CGB_TRY(dmalloc(&cnt, nf1 + 1, st));
@@ -515,24 +556,54 @@ int cgb_trk2dict(const cgb_t2d_params *prm, const float *pts, const int64_t *off
             cudaFreeAsync(t, st);
             CGB_CUDA(e);
         }
+        // one walk into estimated room per streamline; the exact two-walk path (count, then
+        // emit) only if some streamline outgrew its room
+        CGB_TRY(dmalloc(&pend, nf1, st));
+        CGB_TRY(dmalloc(&oflow, 1, st));
+        CGB_CUDA(cudaMemsetAsync(oflow, 0, sizeof(int), st));
+        int64_t npieces = 0;
+        int over = 1;
         if (nfib > 0) {
+            k_room<<<gb, tb, 0, st>>>(c, pts, offsets, nfib, blur_apply, cnt);
+            CGB_CUDA(cudaGetLastError());
+            CGB_TRY(exclusive_scan(cnt, poff, nfib + 1, st));
+            CGB_TRY(read_i64(poff + nfib, &npieces, st));
+            const int64_t kMaxRoom = (int64_t)1 << 31;  // items of one segmented sort
+            if (npieces < kMaxRoom) {
+                CGB_TRY(dmalloc(&keys, npieces, st));
+                CGB_TRY(dmalloc(&lens, npieces, st));
+                k_walk<<<gb, tb, 0, st>>>(c, pts, offsets, nfib, blur_apply, hash, mask, poff, keys, lens, cnt, flen,
+                                          flentot, order);
+                CGB_CUDA(cudaGetLastError());
+                k_ends<<<gb, tb, 0, st>>>(poff, cnt, nfib, pend, oflow);
+                CGB_CUDA(cudaGetLastError());
+                CGB_CUDA(cudaMemcpyAsync(&over, oflow, sizeof(int), cudaMemcpyDeviceToHost, st));
+                CGB_CUDA(cudaStreamSynchronize(st));
+            }
+        } else {
+            over = 0;
+            CGB_CUDA(cudaMemsetAsync(poff, 0, sizeof(int64_t), st));
+        }
+        if (over) {
+            if (keys) cudaFreeAsync(keys, st);
+            if (lens) cudaFreeAsync(lens, st);
+            keys = nullptr;
+            lens = nullptr;
             k_walk<<<gb, tb, 0, st>>>(c, pts, offsets, nfib, blur_apply, hash, mask, nullptr, nullptr, nullptr, cnt,
                                       flen, flentot, order);
             CGB_CUDA(cudaGetLastError());
-        }
-        CGB_TRY(exclusive_scan(cnt, poff, nfib + 1, st));
-        int64_t npieces = 0;
-        CGB_TRY(read_i64(poff + nfib, &npieces, st));
-        CGB_TRY(dmalloc(&keys, npieces, st));
-        CGB_TRY(dmalloc(&lens, npieces, st));
-        CGB_TRY(dmalloc(&keys2, npieces, st));
-        CGB_TRY(dmalloc(&lens2, npieces, st));
-        if (nfib > 0) {
+            CGB_TRY(exclusive_scan(cnt, poff, nfib + 1, st));
+            CGB_TRY(read_i64(poff + nfib, &npieces, st));
+            CGB_TRY(dmalloc(&keys, npieces, st));
+            CGB_TRY(dmalloc(&lens, npieces, st));
             k_walk<<<gb, tb, 0, st>>>(c, pts, offsets, nfib, blur_apply, hash, mask, poff, keys, lens, nullptr, nullptr,
                                       nullptr, order);
             CGB_CUDA(cudaGetLastError());
+            CGB_CUDA(cudaMemcpyAsync(pend, poff + 1, nfib * sizeof(int64_t), cudaMemcpyDeviceToDevice, st));
         }
-        CGB_TRY(seg_sort(keys, keys2, lens, lens2, npieces, nfib, poff, st));
+        CGB_TRY(dmalloc(&keys2, npieces, st));
+        CGB_TRY(dmalloc(&lens2, npieces, st));
+        CGB_TRY(seg_sort(keys, keys2, lens, lens2, npieces, nfib, poff, st, pend));
         // merge: counts, kept flags, offsets, kept ids
         CGB_TRY(dmalloc(&mcnt, nf1 + 1, st));
         CGB_TRY(dmalloc(&soff, nf1 + 1, st));
@@ -542,7 +613,7 @@ int cgb_trk2dict(const cgb_t2d_params *prm, const float *pts, const int64_t *off
         CGB_CUDA(cudaMemsetAsync(mcnt, 0, (nf1 + 1) * sizeof(int64_t), st));
         CGB_CUDA(cudaMemsetAsync(kept64, 0, (nf1 + 1) * sizeof(int64_t), st));
         if (nfib > 0) {
-            k_merge<<<gb, tb, 0, st>>>(0, nfib, c, poff, keys2, lens2, flen, nullptr, nullptr, mcnt, out->trk_kept,
+            k_merge<<<gb, tb, 0, st>>>(0, nfib, c, poff, pend, keys2, lens2, flen, nullptr, nullptr, mcnt, out->trk_kept,
                                        kept64, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
             CGB_CUDA(cudaGetLastError());
         }
@@ -567,7 +638,8 @@ int cgb_trk2dict(const cgb_t2d_params *prm, const float *pts, const int64_t *off
         CGB_TRY(dmalloc(&vval, nseg, st));
         CGB_TRY(dmalloc(&vval2, nseg, st));
         if (nfib > 0) {
-            k_merge<<<gb, tb, 0, st>>>(1, nfib, c, poff, keys2, lens2, flen, soff, kid, nullptr, nullptr, nullptr, out->ic_f,
+            k_merge<<<gb, tb, 0, st>>>(1, nfib, c, poff, pend, keys2, lens2, flen, soff, kid, nullptr, nullptr, nullptr,
+                                       out->ic_f,
                                        out->ic_v, out->ic_o, out->ic_len, vkey, vval);
             CGB_CUDA(cudaGetLastError());
         }
@@ -622,7 +694,7 @@ int cgb_trk2dict(const cgb_t2d_params *prm, const float *pts, const int64_t *off
     };
     rc = body();
     void *tmp[] = {cnt,  poff, mcnt, soff, kid,  kept64, flen, flentot, keys, keys2,
-                   vkey, vkey2, lens, lens2, vval, vval2, vcnt, voff, npts, order};
+                   vkey, vkey2, lens, lens2, vval, vval2, vcnt, voff, npts, order, pend, oflow};
     for (void *q : tmp)
         if (q) cudaFreeAsync(q, st);
     if (rc == CGB_OK) {
