@@ -102,6 +102,7 @@ def lib() -> ctypes.CDLL:
     L.cgb_op_occupancy.argtypes = [P, c_i32, c_i32, ctypes.POINTER(c_i32), ctypes.POINTER(ctypes.c_float),
                                    ctypes.POINTER(ctypes.c_float)]
     L.cgb_op_batch_width.argtypes = [P, c_i32, ctypes.POINTER(c_i32)]
+    L.cgb_op_batch_shape.argtypes = [P, c_i32, ctypes.POINTER(c_i32)]
     L.cgb_op_apply_batch.argtypes = [P, c_i32, c_i32, ctypes.POINTER(c_vp), ctypes.POINTER(c_vp), P]
     L.cgb_op_voxel_maps.argtypes = [P, P, P, P, P, P, P, P, P, P, P, P, P]
     L.cgb_trk2dict.argtypes = [ctypes.POINTER(CgbT2DParams), P, P, c_i64, P, P, P, P, P, ctypes.POINTER(CgbT2DResult), P]

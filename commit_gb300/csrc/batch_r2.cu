@@ -10,8 +10,8 @@ using LT = __nv_bfloat16;
 CompsM<LT> comps_bf16(const cgb_op *op) {
     CompsM<LT> C;
     C.n = 0;
-    C.nSp = op->nSp;
-    const uint32_t ndirs = (uint32_t)op->ndirs, nSp = (uint32_t)op->nSp;
+    C.nSp = op->nSp_r;
+    const uint32_t ndirs = (uint32_t)op->ndirs, nSp = (uint32_t)op->nSp_r;
     const LT *ic = (const LT *)op->lut_r_ic(CGB_ARITH_BF16);
     const LT *ec = (const LT *)op->lut_r_ec(CGB_ARITH_BF16);
     const LT *iso = (const LT *)op->lut_r_iso(CGB_ARITH_BF16);
@@ -78,13 +78,13 @@ struct AdjR {
 int forward_R2(cgb_op *op, const RhsPtrs &V, const float *yobs, const float *sqw, double *partials,
                 cudaStream_t st, int *grid) {
     FwdR L{op, &V, yobs, sqw, partials, st, grid};
-    return dispatch_pair_shape(pick_pair_shape(op->nS), L);
+    return dispatch_pair_shape(op->batch_lpv == 2 ? wide_pair_shape(op->nS) : pick_pair_shape(op->nS), L);
 }
 
 int adjoint_R2(cgb_op *op, const RhsPtrs &V, int in_mode, const float *yobs, const float *sqw,
                 double *partials, cudaStream_t st, int *grid) {
     AdjR L{op, &V, in_mode, yobs, sqw, partials, st, grid};
-    return dispatch_pair_shape(pick_pair_shape(op->nS), L);
+    return dispatch_pair_shape(op->batch_lpv == 2 ? wide_pair_shape(op->nS) : pick_pair_shape(op->nS), L);
 }
 
 }  // namespace cgb

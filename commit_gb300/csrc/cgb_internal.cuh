@@ -89,6 +89,8 @@ struct cgb_op {
     int nSp;
     void *lutIC_r, *lutEC_r, *lutISO_r;  // reduced-precision LUT copies (padded pair layout)
     int lut_r_kind;                 // CGB_ARITH_BF16 / CGB_ARITH_FP16 / 0
+    int nSp_r;                      // row stride of the BF16 / FP16 copies: room for the 16- and 32-lane shapes
+    int batch_lpv;                  // voxel shape of the multi-vector kernels: 0 not tuned, 1 default, 2 a warp per voxel
     __half *seg_l16;                // FP16 lengths scaled by 2^k (reduced path)
     float len16_inv_scale;          // 2^-k
     double *d_x64;                  // [ncols] staging for FP32 applies

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "cgb_internal.cuh"
+#include "operator_pair.cuh"
 
 namespace cgb {
 namespace {
@@ -1139,8 +1140,12 @@ struct BatchSolver {
     bool reuse = false;
     int tune() {
         const bool want_r = op->batch_rhs == 0 && P >= 4;
+        const bool want_shape = op->batch_lpv == 0;
         const bool want_reuse = prm->momentum_reuse == 2 && op->batch_reuse == 0;
-        if (op->nV == 0 || (!want_r && !want_reuse)) return CGB_OK;
+        if (op->nV == 0 || (!want_r && !want_shape && !want_reuse)) {
+            if (op->batch_lpv == 0) op->batch_lpv = 1;
+            return CGB_OK;
+        }
         std::vector<int> J;
         for (int p = 0; p < P && p < 4; ++p) J.push_back(p);
         std::vector<double *> xh(P);
@@ -1157,39 +1162,53 @@ struct BatchSolver {
             CGB_CUDA(cudaEventElapsedTime(ms, e[0], e[1]));
             return CGB_OK;
         };
+        // candidates: vectors per pass x voxel shape (default, or a warp per voxel when that
+        // is a different shape); each timed on one iteration's passes, with and without reuse
         const int widths[2] = {4, 2};
         const int nw = want_r ? 2 : 1;
-        float cost[2][2] = {{0.f, 0.f}, {0.f, 0.f}};  // [width][reuse]
+        const bool wide_differs = detail::wide_pair_shape(op->nS).lpv != detail::pick_pair_shape(op->nS).lpv;
+        const int ns = want_shape && wide_differs ? 2 : 1;
+        float cost[2][2][2] = {};  // [shape][width][reuse]
         for (int rep = 0; rep < 2; ++rep) {
-            for (int k = 0; k < nw; ++k) {
-                R = want_r ? widths[k] : (op->batch_rhs == 2 ? 2 : 4);
-                float t0 = 0.f, t1 = 0.f, t2 = 0.f, t3 = 0.f;
-                CGB_TRY(timed([&] { return forward(J, xh.data(), y32, 0, nullptr); }, &t0));
-                CGB_TRY(timed([&] { return gradient(J, false, nullptr, nullptr, nullptr, nullptr); }, &t1));
-                if (!ax32.empty()) {
-                    CGB_TRY(timed([&] { return forward(J, xh.data(), y32, 0, zero.data()); }, &t2));
-                    CGB_TRY(timed([&] { return gradient(J, true, zero.data(), zero.data(), one.data(), nil.data()); },
-                                  &t3));
-                }
-                if (rep == 1) {
-                    cost[k][0] = t0 + t1;
-                    cost[k][1] = t2 + t3;
+            for (int h = 0; h < ns; ++h) {
+                op->batch_lpv = want_shape ? h + 1 : op->batch_lpv;
+                for (int k = 0; k < nw; ++k) {
+                    R = want_r ? widths[k] : (op->batch_rhs == 2 ? 2 : 4);
+                    float t0 = 0.f, t1 = 0.f, t2 = 0.f, t3 = 0.f;
+                    CGB_TRY(timed([&] { return forward(J, xh.data(), y32, 0, nullptr); }, &t0));
+                    CGB_TRY(timed([&] { return gradient(J, false, nullptr, nullptr, nullptr, nullptr); }, &t1));
+                    if (!ax32.empty()) {
+                        CGB_TRY(timed([&] { return forward(J, xh.data(), y32, 0, zero.data()); }, &t2));
+                        CGB_TRY(timed(
+                            [&] { return gradient(J, true, zero.data(), zero.data(), one.data(), nil.data()); }, &t3));
+                    }
+                    if (rep == 1) {
+                        cost[h][k][0] = t0 + t1;
+                        cost[h][k][1] = t2 + t3;
+                    }
                 }
             }
         }
         for (auto &ev : e) cudaEventDestroy(ev);
-        int kb = 0;
-        if (want_r) {
-            // reuse: -1 to be chosen, else fixed (by the caller or an earlier tuning)
-            const int ru = want_reuse ? -1 : (prm->momentum_reuse == 2 ? op->batch_reuse == 2 : prm->momentum_reuse != 0);
-            auto best_of = [&](int k) {
-                if (ru >= 0) return cost[k][ru];
-                return cost[k][0] < cost[k][1] ? cost[k][0] : cost[k][1];
-            };
-            kb = best_of(1) < best_of(0) ? 1 : 0;
-            op->batch_rhs = widths[kb];
-        }
-        if (want_reuse) op->batch_reuse = cost[kb][1] < cost[kb][0] ? 2 : 1;
+        // reuse: -1 to be chosen, else fixed (by the caller or an earlier tuning)
+        const int ru = want_reuse ? -1 : (prm->momentum_reuse == 2 ? op->batch_reuse == 2 : prm->momentum_reuse != 0);
+        float best = 1e30f;
+        int bh = 0, bk = 0, bu = 0;
+        for (int h = 0; h < ns; ++h)
+            for (int k = 0; k < nw; ++k)
+                for (int u = 0; u < 2; ++u) {
+                    if (ru >= 0 && u != ru) continue;
+                    if (u == 1 && ax32.empty()) continue;
+                    if (cost[h][k][u] < best) {
+                        best = cost[h][k][u];
+                        bh = h;
+                        bk = k;
+                        bu = u;
+                    }
+                }
+        if (want_shape) op->batch_lpv = bh + 1;
+        if (want_r) op->batch_rhs = widths[bk];
+        if (want_reuse) op->batch_reuse = bu ? 2 : 1;
         R = op->batch_rhs == 2 ? 2 : 4;
         return CGB_OK;
     }
@@ -1411,6 +1430,16 @@ int cgb_op_batch_width(cgb_op *op, int set, int *width) {
         op->batch_rhs = set;
     }
     if (width) *width = op->batch_rhs;
+    return CGB_OK;
+}
+
+int cgb_op_batch_shape(cgb_op *op, int set, int *shape) {
+    if (!op) return fail(CGB_ERR_INVALID, "null handle");
+    if (set >= 0) {
+        if (set > 2) return fail(CGB_ERR_INVALID, "shape must be 0 (tune), 1 (default) or 2 (a warp per voxel)");
+        op->batch_lpv = set;
+    }
+    if (shape) *shape = op->batch_lpv;
     return CGB_OK;
 }
 

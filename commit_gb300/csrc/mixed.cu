@@ -2,7 +2,10 @@
 // of the mixed kernels (operator_mixed_*.cu) and the per-fibre FP64 sum of FP32 terms.
 #include <math.h>
 
+#include <type_traits>
+
 #include "cgb_internal.cuh"
+#include "operator_pair.cuh"
 
 namespace cgb {
 
@@ -20,6 +23,19 @@ int adjoint_mix_f32(cgb_op *, const float *, int, const double *, const float *,
                     const float *, float, float, double *, double *, cudaStream_t, int *);
 
 namespace {
+
+// rows of `w` entries at stride `sin` -> rows at stride `sout` (sout >= sin), zero beyond w
+template <class T>
+__global__ void k_to_reduced(const float *__restrict__ in, T *__restrict__ out, size_t rows, int sin, int sout) {
+    const size_t n = rows * (size_t)sout;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t r = i / sout;
+        const int k = (int)(i - r * sout);
+        const float v = k < sin ? in[r * sin + k] : 0.f;
+        if constexpr (sizeof(T) == 2 && std::is_same<T, __nv_bfloat16>::value) out[i] = __float2bfloat16_rn(v);
+        else out[i] = __float2half_rn(v);
+    }
+}
 
 __global__ void k_to_bf16(const float *in, __nv_bfloat16 *out, size_t n) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -179,19 +195,23 @@ int ensure_reduced(cgb_op *op, int arith) {
         if (op->lutEC_r) cudaFree(op->lutEC_r);
         if (op->lutISO_r) cudaFree(op->lutISO_r);
         op->lutIC_r = op->lutEC_r = op->lutISO_r = nullptr;
-        const size_t nic = (size_t)op->nIC * op->ndirs * op->nSp, nec = (size_t)op->nEC * op->ndirs * op->nSp,
-                     niso = (size_t)op->nISO * op->nSp;
+        // rows at a stride with room for the 32-lane shape of the multi-vector kernels
+        const int wide = 2 * detail::wide_pair_shape(op->nS).lpv * detail::wide_pair_shape(op->nS).np;
+        op->nSp_r = wide > op->nSp ? wide : op->nSp;
+        const size_t ric = (size_t)op->nIC * op->ndirs, rec = (size_t)op->nEC * op->ndirs, riso = (size_t)op->nISO;
+        const size_t nic = ric * op->nSp_r, nec = rec * op->nSp_r, niso = riso * op->nSp_r;
         CGB_CUDA(cudaMalloc(&op->lutIC_r, (nic ? nic : 1) * 2));
         CGB_CUDA(cudaMalloc(&op->lutEC_r, (nec ? nec : 1) * 2));
         CGB_CUDA(cudaMalloc(&op->lutISO_r, (niso ? niso : 1) * 2));
         if (arith == CGB_ARITH_BF16) {
-            if (nic) k_to_bf16<<<grid_n(nic), 256>>>(op->lutIC_p, (__nv_bfloat16 *)op->lutIC_r, nic);
-            if (nec) k_to_bf16<<<grid_n(nec), 256>>>(op->lutEC_p, (__nv_bfloat16 *)op->lutEC_r, nec);
-            if (niso) k_to_bf16<<<grid_n(niso), 256>>>(op->lutISO_p, (__nv_bfloat16 *)op->lutISO_r, niso);
+            if (nic) k_to_reduced<<<grid_n(nic), 256>>>(op->lutIC_p, (__nv_bfloat16 *)op->lutIC_r, ric, op->nSp, op->nSp_r);
+            if (nec) k_to_reduced<<<grid_n(nec), 256>>>(op->lutEC_p, (__nv_bfloat16 *)op->lutEC_r, rec, op->nSp, op->nSp_r);
+            if (niso)
+                k_to_reduced<<<grid_n(niso), 256>>>(op->lutISO_p, (__nv_bfloat16 *)op->lutISO_r, riso, op->nSp, op->nSp_r);
         } else {
-            if (nic) k_to_fp16<<<grid_n(nic), 256>>>(op->lutIC_p, (__half *)op->lutIC_r, nic);
-            if (nec) k_to_fp16<<<grid_n(nec), 256>>>(op->lutEC_p, (__half *)op->lutEC_r, nec);
-            if (niso) k_to_fp16<<<grid_n(niso), 256>>>(op->lutISO_p, (__half *)op->lutISO_r, niso);
+            if (nic) k_to_reduced<<<grid_n(nic), 256>>>(op->lutIC_p, (__half *)op->lutIC_r, ric, op->nSp, op->nSp_r);
+            if (nec) k_to_reduced<<<grid_n(nec), 256>>>(op->lutEC_p, (__half *)op->lutEC_r, rec, op->nSp, op->nSp_r);
+            if (niso) k_to_reduced<<<grid_n(niso), 256>>>(op->lutISO_p, (__half *)op->lutISO_r, riso, op->nSp, op->nSp_r);
         }
         CGB_CUDA(cudaGetLastError());
         op->lut_r_kind = arith;

@@ -10,8 +10,8 @@ using LT = __half;
 CompsM<LT> comps(const cgb_op *op) {
     CompsM<LT> C;
     C.n = 0;
-    C.nSp = op->nSp;
-    const uint32_t ndirs = (uint32_t)op->ndirs, nSp = (uint32_t)op->nSp;
+    C.nSp = op->nSp_r;
+    const uint32_t ndirs = (uint32_t)op->ndirs, nSp = (uint32_t)op->nSp_r;
     const LT *ic = (const LT *)op->lut_r_ic(CGB_ARITH_FP16);
     const LT *ec = (const LT *)op->lut_r_ec(CGB_ARITH_FP16);
     const LT *iso = (const LT *)op->lut_r_iso(CGB_ARITH_FP16);

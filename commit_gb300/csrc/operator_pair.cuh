@@ -493,6 +493,15 @@ inline PairShape pick_pair_shape(int nS) {
     return best;
 }
 
+// the 32-lane shape for nS (a warp per voxel, half the samples per lane of the 16-lane
+// shape): the smallest NP with 64 * NP >= nS that has kernels
+inline PairShape wide_pair_shape(int nS) {
+    PairShape best = {32, 8};
+    for (const PairShape &s : kPairShapes)
+        if (s.lpv == 32 && 2 * s.lpv * s.np >= nS && s.np < best.np) best = s;
+    return best;
+}
+
 template <class Fn>
 int dispatch_pair_shape(PairShape s, Fn &fn) {
 #define CGB_PSHAPE(L, N) \

@@ -210,6 +210,13 @@ class LinearOperator:
         check(lib().cgb_op_batch_width(self._h.ptr, -1 if set_to is None else int(set_to), ctypes.byref(w)))
         return int(w.value)
 
+    def batch_shape(self, set_to: int | None = None) -> int:
+        """Voxel shape of the multi-vector kernels (1 default lanes per voxel, 2 a warp per
+        voxel, 0 chosen by timing on the next batched solve)."""
+        w = ctypes.c_int32()
+        check(lib().cgb_op_batch_shape(self._h.ptr, -1 if set_to is None else int(set_to), ctypes.byref(w)))
+        return int(w.value)
+
     def dot_batch(self, vs):
         """A @ v (or A' @ v) for a list of CUDA vectors in multi-right-hand-side passes
         (BF16 LUT, FP32 accumulation; 2 or 4 vectors per pass).  Forward: float64 columns

@@ -273,6 +273,11 @@ int cgb_op_occupancy(cgb_op *op, int slot, int set, int *choice, float *ms_a, fl
  * receives the current value (0 while untuned). */
 int cgb_op_batch_width(cgb_op *op, int set, int *width);
 
+/* Voxel shape of the multi-right-hand-side kernels: 1 the single-vector kernels' lanes per
+ * voxel, 2 a warp per voxel (half the samples per lane, fewer registers per vector), 0 =
+ * chosen by timing on the next batched solve; set < 0 only reads. */
+int cgb_op_batch_shape(cgb_op *op, int set, int *shape);
+
 /* ------------------------------------------------------------------ voxelwise maps */
 /*
  * The maps of Evaluation.save_results (commit/core.pyx:1614-1750) for a fitted x (device

@@ -177,3 +177,30 @@ def test_batched_path_with_adjoint_slabs_is_bitwise_unchanged():
     for (x1, d1), (x4, d4) in zip(out[1], out[4]):
         assert d1['iterations'] == d4['iterations']
         assert np.array_equal(x1, x4)
+
+
+@pytest.mark.parametrize('shape', [1, 2])
+def test_batch_voxel_shapes_agree(shape):
+    """Both voxel shapes of the multi-vector kernels (the single-vector kernels' lanes per
+    voxel, a warp per voxel) give the same products to FP32 summation-order accuracy."""
+    from commit_gb300 import solvers
+    from commit_gb300.operator import LinearOperator
+    D, K, P, y = _demo('demo_5k', n_b0=18, shells=[(1000.0, 90), (2000.0, 90), (3000.0, 90)], n_fibers=2000)
+    A = LinearOperator(D, K, None)
+    A.batch_width(4)
+    A.batch_shape(shape)
+    rng = np.random.default_rng(8)
+    xs = [torch.from_numpy(rng.uniform(0, 1, P.nCOLS)).cuda() for _ in range(4)]
+    for x, yb in zip(xs, A.dot_batch(xs)):
+        assert G.rel(yb.cpu().numpy(), P.dot(x.cpu().numpy())) <= 1.5e-2
+    ws = [torch.from_numpy(rng.normal(size=P.nROWS).astype(np.float32)).cuda() for _ in range(4)]
+    for w, xb in zip(ws, A.T.dot_batch(ws)):
+        xsingle = A.T.dot(w, arith='bf16')
+        assert G.rel(xb.cpu().numpy(), xsingle.double().cpu().numpy()) <= 1e-5
+    regs = _path_regs(A, D, K, y, [1e-4, 1e-2])
+    out = solvers.solve_batch(y, A, regs, tol_fun=1e-5, tol_x=1e-7, max_iter=60, momentum_reuse=False)
+    for (xb, db), rp in zip(out, regs):
+        xs1, ds1 = solvers.solve(y, A, A.T, tol_fun=1e-5, tol_x=1e-7, max_iter=60, verbose=0, regularisation=rp,
+                                 arith='bf16', momentum_reuse=False)
+        assert G.rel(xb, xs1) <= 2e-3
+    assert A.batch_shape() == shape
