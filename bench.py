@@ -544,7 +544,8 @@ def run_batch(args):
                       'iterations_per_solve': M, 'tolerances': 'off (fixed iteration count)'},
            'batched': {'seconds': t_batch, 'solves_per_s': nsolves / t_batch,
                        'ms_per_solve_iteration': 1000.0 * t_batch / (nsolves * M),
-                       'widths': [t['A'].batch_width() for t in tracts], 'streams': args.batch_streams},
+                       'widths': [t['A'].batch_width() for t in tracts],
+                       'voxel_shapes': [t['A'].batch_shape() for t in tracts], 'streams': args.batch_streams},
            'sequential_plain': {'seconds': t_seq, 'solves_per_s': nsolves / t_seq,
                                 'ms_per_solve_iteration': 1000.0 * t_seq / (nsolves * M)},
            'speedup': t_seq / t_batch,
