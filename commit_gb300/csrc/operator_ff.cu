@@ -35,7 +35,7 @@ struct FwdPair {
     }
     template <int L, int N>
     int run() {
-        return occ_launch(op, kOccFwdFF, st, [&] { return launch<L, N, 1>(); }, [&] { return launch<L, N, 3>(); });
+        return occ_launch(op, kOccFwdFF, st, [&] { return launch<L, N, 3>(); }, [&] { return launch<L, N, 4>(); });
     }
 };
 

@@ -73,8 +73,8 @@ struct AdjMix {
     }
     template <int L, int N>
     int run() {
-        return occ_launch(op, kOccAdjMix + (CGB_ARITH_BF16 - CGB_ARITH_BF16), st, [&] { return launch<L, N, 1>(); },
-                          [&] { return launch<L, N, 3>(); });
+        return occ_launch(op, kOccAdjMix + (CGB_ARITH_BF16 - CGB_ARITH_BF16), st, [&] { return launch<L, N, 3>(); },
+                          [&] { return launch<L, N, 4>(); });
     }
 };
 

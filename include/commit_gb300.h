@@ -260,8 +260,9 @@ int cgb_op_apply_batch(cgb_op *op, int adjoint, int nvec, const void *const *in,
 /*
  * Occupancy autotuning of the voxel kernels.  Slots: 0 float-float A, 1 float-float A' pass
  * 1, 2 / 3 / 4 reduced-precision A' pass 1 (BF16 / FP16 / F32), 5 two-vector BF16 A'.
- * Each tuned kernel has two builds (1: registers unconstrained, 2: capped for more resident
- * warps); the first call on a handle times both on its own arguments and keeps the faster.
+ * Each tuned kernel has two builds with different register caps (2: the tighter cap, more
+ * resident warps); the first call on a handle times both on its own arguments and keeps the
+ * faster.
  * set >= 0 stores a choice (0 = tune again on the next call, 1 or 2 = fixed), set < 0 only
  * reads; choice / ms_a / ms_b (may be NULL) receive the choice and the two measured times.
  * Both builds compute the same operations in the same order: results are identical.
