@@ -132,8 +132,8 @@ __device__ __forceinline__ void forward_row_mix(const CompsM<LT> &C, const Group
 }
 
 // y = A x (float rows); optional ax_out; optional FP64 partials of |sqw*(Ax - yobs)|^2
-template <class LT, int LPV, int NP>
-__global__ void __launch_bounds__(kBlock) k_forward_mix(const int nV, const int nS, const __grid_constant__ CompsM<LT> C,
+template <class LT, int LPV, int NP, int MINB = 1>
+__global__ void __launch_bounds__(kBlock, MINB) k_forward_mix(const int nV, const int nS, const __grid_constant__ CompsM<LT> C,
                                                         const double *__restrict__ x, float *__restrict__ yout,
                                                         float *__restrict__ axout, const float *__restrict__ yobs,
                                                         const float *__restrict__ sqw, double *__restrict__ partials) {

@@ -36,9 +36,9 @@ struct FwdMix {
     double *partials;
     cudaStream_t st;
     int *grid_out;
-    template <int L, int N>
-    int run() {
-        auto kern = k_forward_mix<LT, L, N>;
+    template <int L, int N, int MINB>
+    int launch() {
+        auto kern = k_forward_mix<LT, L, N, MINB>;
         int g = 0;
         CGB_TRY(grid_for_kernel(kern, 0, op->nsm, op->nV, kBlock / L, &g));
         if (g > reduction_blocks(op)) g = reduction_blocks(op);
@@ -46,6 +46,11 @@ struct FwdMix {
         CGB_CUDA(cudaGetLastError());
         if (grid_out) *grid_out = g;
         return CGB_OK;
+    }
+    template <int L, int N>
+    int run() {
+        return occ_launch(op, kOccFwdMix + (CGB_ARITH_F32 - CGB_ARITH_BF16), st, [&] { return launch<L, N, 5>(); },
+                          [&] { return launch<L, N, 6>(); });
     }
 };
 
