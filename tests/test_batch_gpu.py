@@ -204,3 +204,21 @@ def test_batch_voxel_shapes_agree(shape):
                                  arith='bf16', momentum_reuse=False)
         assert G.rel(xb, xs1) <= 2e-3
     assert A.batch_shape() == shape
+
+
+def test_batch_single_and_three_problems():
+    """One problem (single-vector kernels) and three (a 4-vector pass with an idle slot)
+    match sequential BF16 solves."""
+    from commit_gb300 import solvers
+    from commit_gb300.operator import LinearOperator
+    D, K, P, y = _demo()
+    A = LinearOperator(D, K, None)
+    A.batch_width(4)
+    for fr in ([1e-3], [1e-4, 1e-3, 1e-2]):
+        regs = _path_regs(A, D, K, y, fr)
+        out = solvers.solve_batch(y, A, regs, tol_fun=1e-5, tol_x=1e-7, max_iter=50, momentum_reuse=False)
+        for (xb, db), rp in zip(out, regs):
+            xs1, ds1 = solvers.solve(y, A, A.T, tol_fun=1e-5, tol_x=1e-7, max_iter=50, verbose=0, regularisation=rp,
+                                     arith='bf16', momentum_reuse=False)
+            assert G.rel(xb, xs1) <= 2e-3
+            assert abs(db['iterations'] - ds1['iterations']) <= 3

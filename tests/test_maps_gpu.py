@@ -45,3 +45,16 @@ def test_voxel_maps_volumes_and_normalisation():
     vol = m['compartment_IC_vol']
     assert vol.shape == D['MASK'].shape
     assert np.array_equal(vol[D['MASK_ix'], D['MASK_iy'], D['MASK_iz']], m['compartment_IC'])
+
+
+def test_voxel_maps_reject_bad_sizes():
+    from commit_gb300 import evaluation
+    from commit_gb300.operator import LinearOperator
+    c = G.load_case('szb')
+    A = LinearOperator(c['D'], c['K'], None)
+    with pytest.raises(RuntimeError):
+        evaluation.voxel_maps(A, np.zeros(A.nCOLS - 1))
+    with pytest.raises(RuntimeError):
+        evaluation.voxel_maps(A, np.zeros(A.nCOLS), y=np.zeros(A.nROWS + 1))
+    m = evaluation.voxel_maps(A, np.zeros(A.nCOLS), y=c['y_obs'])
+    assert not m['compartment_IC'].any() and m['fit_RMSE'].max() > 0

@@ -69,3 +69,26 @@ def test_voxelised_dictionary_loads_into_the_operator(tmp_path):
 def load_case(name):
     from test_t2d_oracle import load
     return load(os.path.join(HERE, 'golden', f't2d_{name}.npz'))
+
+
+def test_voxeliser_edge_cases():
+    """No streamlines; streamlines of 0, 1, 2 points (no segments, not kept); a streamline
+    entirely outside the grid; identical to the oracle in every case."""
+    from commit_gb300 import trk2dictionary as V
+    dim, pix = (8, 8, 8), (1.0, 1.0, 1.0)
+    H = V.hash_table(np.eye(3))
+    r = V.voxelise(np.zeros((0, 3), np.float32), np.array([0]), dim, pix, H)
+    assert r['IC']['f'].size == 0 and r['TRK']['kept'].size == 0 and not r['TDI'].any()
+    pts = np.array([[1.5, 1.5, 1.5],                                   # 1 point
+                    [2.2, 2.1, 2.0], [2.9, 2.5, 2.4],                   # 2 points
+                    [20.0, 20.0, 20.0], [21.0, 20.5, 20.0], [22.0, 21.0, 20.0],   # outside
+                    [0.5, 0.5, 0.5], [1.7, 0.9, 0.6], [2.9, 1.4, 0.8], [3.6, 2.2, 1.5]],  # inside
+                   np.float32)
+    off = np.array([0, 0, 1, 3, 6, 10])                                 # first streamline empty
+    a = V.voxelise(pts, off, dim, pix, H)
+    b = T.voxelise(pts, off, dim, pix, H)
+    for comp in ('IC', 'TRK'):
+        for k in b[comp]:
+            assert np.array_equal(a[comp][k], b[comp][k]), (comp, k)
+    assert list(a['TRK']['kept']) == [0, 0, 0, 0, 1]
+    assert set(np.unique(a['IC']['f'])) == {0}
