@@ -48,7 +48,7 @@ struct AdjPair {
     double *xout, *partials;
     cudaStream_t st;
     int *grid_out;
-    template <int L, int N, int MINB>
+    template <int L, int N, int MINB, bool FUSED>
     int launch() {
         OpDev P = op->dev();
         if (op->vr1 > 0) {
@@ -56,7 +56,7 @@ struct AdjPair {
             P.nV = op->vr1;
         }
         const Comps C = make_comps(op);
-        auto kern = k_adjoint_p<L, N, MINB>;
+        auto kern = k_adjoint_p<L, N, MINB, FUSED>;
         int g = 0;  // sized for all voxels, so every range launch has the same grid
         CGB_TRY(grid_for_kernel(kern, 0, op->nsm, op->nV, kBlock / L, &g));
         if (g > reduction_blocks(op)) g = reduction_blocks(op);
@@ -67,7 +67,12 @@ struct AdjPair {
     }
     template <int L, int N>
     int run() {
-        return occ_launch(op, kOccAdjFF, st, [&] { return launch<L, N, 1>(); }, [&] { return launch<L, N, 2>(); });
+        // the fused-forward build (in_mode 1) holds the forward row as well
+        if (in_mode == 1)
+            return occ_launch(op, kOccAdjFFFused, st, [&] { return launch<L, N, 1, true>(); },
+                              [&] { return launch<L, N, 2, true>(); });
+        return occ_launch(op, kOccAdjFF, st, [&] { return launch<L, N, 2, false>(); },
+                          [&] { return launch<L, N, 3, false>(); });
     }
 };
 

@@ -349,7 +349,7 @@ __device__ __forceinline__ double batch_dots_p(const Group<LPV> &G, const float 
 // A' pass 1 over all compartments.  Per batch, one dot product per run of equal
 // orientation; every item of the run takes that total: IC items write l*<L,z> to the
 // per-segment scratch stream, EC / ISO items write their column of xout.
-template <int LPV, int NP, int MINB = 1>
+template <int LPV, int NP, int MINB = 1, bool FUSED = true>
 __global__ void __launch_bounds__(kBlock, MINB) k_adjoint_p(const OpDev P, const __grid_constant__ Comps C,
                                                       const double *__restrict__ yin,
                                                       int in_mode, const double *__restrict__ x,
@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_adjoint_p(const OpDev P, const
     double nrm = 0.0;
     for (int v = P.v0 + blockIdx.x * gpb + (int)threadIdx.x / LPV; v < P.nV; v += ngroups) {
         double a[2 * NP];
-        if (in_mode == 1) {
+        if (FUSED && in_mode == 1) {
             DD2 acc[NP];
             forward_row_p<LPV, NP>(C, G, v, x, acc);
 #pragma unroll

@@ -177,7 +177,8 @@ class LinearOperator:
         return res
 
     OCC_SLOTS = {'ff_forward': 0, 'ff_adjoint': 1, 'bf16_adjoint': 2, 'fp16_adjoint': 3, 'f32_adjoint': 4,
-                 'bf16x2_adjoint': 5, 'bf16_forward': 6, 'fp16_forward': 7, 'f32_forward': 8}
+                 'bf16x2_adjoint': 5, 'bf16_forward': 6, 'fp16_forward': 7, 'f32_forward': 8,
+                 'ff_fused_gradient': 9}
 
     def occupancy(self, set_to: dict | None = None) -> dict:
         """Occupancy autotuning state per tuned kernel: {name: (choice, ms_build1, ms_build2)}
