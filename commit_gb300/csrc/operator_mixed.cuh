@@ -203,7 +203,7 @@ __device__ __forceinline__ float batch_dots_mix(const Group<LPV> &G, const LT *_
 
 // A' pass 1.  in_mode 0: z = yin; 1: z = sqw*r, r = sqw*(A x - yobs) (FP64 norm partials);
 // 2: as 1 with A x = ca*ax_a + cb*ax_b.  IC terms -> scr (FP32), EC/ISO -> xout (FP64).
-template <class LT, int LPV, int NP, int MINB = 1>
+template <class LT, int LPV, int NP, int MINB = 1, bool FUSED = true>
 __global__ void __launch_bounds__(kBlock, MINB) k_adjoint_mix(const int v0, const int nV, const int nS, const int64_t n,
                                                         const __grid_constant__ CompsM<LT> C,
                                                         const float *__restrict__ yin, int in_mode,
@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_adjoint_mix(const int v0, cons
     double nrm = 0.0;
     for (int v = v0 + blockIdx.x * gpb + (int)threadIdx.x / LPV; v < nV; v += ngroups) {
         f2 acc[NP];
-        if (in_mode == 1) forward_row_mix<LT, LPV, NP>(C, G, v, x, acc);
+        if (FUSED && in_mode == 1) forward_row_mix<LT, LPV, NP>(C, G, v, x, acc);
         f2 z[NP];
         float vn = 0.f;
 #pragma unroll

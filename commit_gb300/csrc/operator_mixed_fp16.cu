@@ -64,9 +64,9 @@ struct AdjMix {
     double *xout, *partials;
     cudaStream_t st;
     int *grid_out;
-    template <int L, int N, int MINB>
+    template <int L, int N, int MINB, bool FUSED>
     int launch() {
-        auto kern = k_adjoint_mix<LT, L, N, MINB>;
+        auto kern = k_adjoint_mix<LT, L, N, MINB, FUSED>;
         int g = 0;
         CGB_TRY(grid_for_kernel(kern, 0, op->nsm, op->nV, kBlock / L, &g));
         if (g > reduction_blocks(op)) g = reduction_blocks(op);
@@ -78,8 +78,12 @@ struct AdjMix {
     }
     template <int L, int N>
     int run() {
-        return occ_launch(op, kOccAdjMix + (CGB_ARITH_FP16 - CGB_ARITH_BF16), st, [&] { return launch<L, N, 3>(); },
-                          [&] { return launch<L, N, 4>(); });
+        // the fused-forward build (in_mode 1) holds the forward row as well
+        if (in_mode == 1)
+            return occ_launch(op, kOccAdjMixFused + (CGB_ARITH_FP16 - CGB_ARITH_BF16), st,
+                              [&] { return launch<L, N, 3, true>(); }, [&] { return launch<L, N, 4, true>(); });
+        return occ_launch(op, kOccAdjMix + (CGB_ARITH_FP16 - CGB_ARITH_BF16), st, [&] { return launch<L, N, 4, false>(); },
+                          [&] { return launch<L, N, 5, false>(); });
     }
 };
 
