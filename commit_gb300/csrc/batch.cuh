@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(kBlock) k_forward_R(const int nV, const int nS
 
 // A' pass 1 for R vectors.  in_mode 0: z_r = yin_r; 1: z_r from the fused forward
 // (r = sqw*(A x_r - yobs), FP64 norm partials per vector); 2: A x_r = ca_r*axa_r + cb_r*axb_r.
-template <class LT, int LPV, int NP, int R, int MINB = 1>
+template <class LT, int LPV, int NP, int R, int MINB = 1, bool FUSED = true>
 __global__ void __launch_bounds__(kBlock, MINB) k_adjoint_R(const int v0, const int nV, const int nS, const int64_t n,
                                                       const __grid_constant__ CompsM<LT> C,
                                                       const __grid_constant__ RhsPtrs V, int in_mode,
@@ -157,14 +157,14 @@ __global__ void __launch_bounds__(kBlock, MINB) k_adjoint_R(const int v0, const 
         f2 z[R][NP];
         {
             f2 acc[R][NP];
-            if (in_mode == 1) forward_row_R<LT, LPV, NP, R>(C, G, v, V, acc);
+            if (FUSED && in_mode == 1) forward_row_R<LT, LPV, NP, R>(C, G, v, V, acc);
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 float vn = 0.f;
 #pragma unroll
                 for (int k = 0; k < NP; ++k) {
                     float a[2] = {0.f, 0.f}, zz[2] = {0.f, 0.f};
-                    if (in_mode == 1) f2_unpack(acc[r][k], a[0], a[1]);
+                    if (FUSED && in_mode == 1) f2_unpack(acc[r][k], a[0], a[1]);
 #pragma unroll
                     for (int u = 0; u < 2; ++u) {
                         const int s = 2 * (G.sub + k * LPV) + u;

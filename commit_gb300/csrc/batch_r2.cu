@@ -55,9 +55,9 @@ struct AdjR {
     double *partials;
     cudaStream_t st;
     int *grid_out;
-    template <int L, int N, int MINB>
+    template <int L, int N, int MINB, bool FUSED>
     int launch() {
-        auto kern = k_adjoint_R<LT, L, N, 2, MINB>;
+        auto kern = k_adjoint_R<LT, L, N, 2, MINB, FUSED>;
         int g = 0;
         CGB_TRY(grid_for_kernel(kern, 0, op->nsm, op->nV, kBlock / L, &g));
         if (g > reduction_blocks(op)) g = reduction_blocks(op);
@@ -69,7 +69,11 @@ struct AdjR {
     }
     template <int L, int N>
     int run() {
-        return occ_launch(op, kOccAdjR2, st, [&] { return launch<L, N, 1>(); }, [&] { return launch<L, N, 3>(); });
+        if (in_mode == 1)
+            return occ_launch(op, kOccAdjR2Fused, st, [&] { return launch<L, N, 1, true>(); },
+                              [&] { return launch<L, N, 3, true>(); });
+        return occ_launch(op, kOccAdjR2, st, [&] { return launch<L, N, 2, false>(); },
+                          [&] { return launch<L, N, 3, false>(); });
     }
 };
 

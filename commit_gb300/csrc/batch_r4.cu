@@ -55,9 +55,9 @@ struct AdjR {
     double *partials;
     cudaStream_t st;
     int *grid_out;
-    template <int L, int N>
-    int run() {
-        auto kern = k_adjoint_R<LT, L, N, 4>;
+    template <int L, int N, int MINB, bool FUSED>
+    int launch() {
+        auto kern = k_adjoint_R<LT, L, N, 4, MINB, FUSED>;
         int g = 0;
         CGB_TRY(grid_for_kernel(kern, 0, op->nsm, op->nV, kBlock / L, &g));
         if (g > reduction_blocks(op)) g = reduction_blocks(op);
@@ -66,6 +66,12 @@ struct AdjR {
         CGB_CUDA(cudaGetLastError());
         if (grid_out) *grid_out = g;
         return CGB_OK;
+    }
+    template <int L, int N>
+    int run() {
+        if (in_mode == 1) return launch<L, N, 1, true>();
+        return occ_launch(op, kOccAdjR4, st, [&] { return launch<L, N, 1, false>(); },
+                          [&] { return launch<L, N, 2, false>(); });
     }
 };
 

@@ -228,7 +228,7 @@ int convert_f32_to_f64(const float *in, double *out, int64_t n, cudaStream_t st)
 // fewer registers give more resident warps at the price of a few spills; the pairs were
 // picked from measurements: float-float A 3 / 4, float-float A' 2 / 3 (1 / 2 for the build
 // with the fused forward), reduced A 5 / 6, reduced A' 4 / 5 (3 / 4 fused), two-vector A'
-// 1 / 3).  On the first call for a handle, outside stream capture, both builds run twice
+// 2 / 3 (1 / 3 fused), four-vector A' 1 / 2).  On the first call for a handle, outside stream capture, both builds run twice
 // on the call's own arguments (every output is overwritten by the real launch that
 // follows) and the faster build of the second round is kept on the handle.  Both builds
 // do the same arithmetic in the same order, so results do not depend on the choice.
@@ -240,6 +240,8 @@ enum OccSlot {
     kOccFwdMix = 6,  // + arith - BF16
     kOccAdjFFFused = 9,
     kOccAdjMixFused = 10,  // + arith - BF16
+    kOccAdjR2Fused = 13,
+    kOccAdjR4 = 14,
     kOccSlots = 16
 };
 

@@ -179,7 +179,7 @@ class LinearOperator:
     OCC_SLOTS = {'ff_forward': 0, 'ff_adjoint': 1, 'bf16_adjoint': 2, 'fp16_adjoint': 3, 'f32_adjoint': 4,
                  'bf16x2_adjoint': 5, 'bf16_forward': 6, 'fp16_forward': 7, 'f32_forward': 8,
                  'ff_fused_gradient': 9, 'bf16_fused_gradient': 10, 'fp16_fused_gradient': 11,
-                 'f32_fused_gradient': 12}
+                 'f32_fused_gradient': 12, 'bf16x2_fused_gradient': 13, 'bf16x4_adjoint': 14}
 
     def occupancy(self, set_to: dict | None = None) -> dict:
         """Occupancy autotuning state per tuned kernel: {name: (choice, ms_build1, ms_build2)}

@@ -261,7 +261,7 @@ int cgb_op_apply_batch(cgb_op *op, int adjoint, int nvec, const void *const *in,
  * Occupancy autotuning of the voxel kernels.  Slots: 0 float-float A, 1 float-float A' pass
  * 1, 2 / 3 / 4 reduced-precision A' pass 1 (BF16 / FP16 / F32), 5 two-vector BF16 A',
  * 6 / 7 / 8 reduced-precision A (BF16 / FP16 / F32), 9 float-float fused A x + A' pass 1,
- * 10 / 11 / 12 reduced-precision fused A x + A' pass 1.
+ * 10 / 11 / 12 reduced-precision fused A x + A' pass 1, 13 two-vector fused, 14 four-vector A'.
  * Each tuned kernel has two builds with different register caps (2: the tighter cap, more
  * resident warps); the first call on a handle times both on its own arguments and keeps the
  * faster.
