@@ -111,3 +111,15 @@ def test_regspec_reproduces_reference_flags():
     rp2 = dict(rp, regIC='lasso', lambdaIC=0.5, nnIC=0)
     s2 = RegSpec(rp2)
     assert not s2.nn_ic and s2.lam_ic == 0.5
+
+
+def test_product_package_never_uses_the_oracle():
+    """The oracle is test infrastructure: nothing in the package imports, loads or runs it."""
+    import glob
+    import os
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    for path in glob.glob(os.path.join(root, 'commit_gb300', '*.py')):
+        src = open(path).read()
+        for bad in ('import oracle', 'from oracle', "'oracle'", '"oracle"', 'trk2dict_oracle', 'commit_oracle',
+                    'libcommit_ref', 'oracle/'):
+            assert bad not in src, (path, bad)
