@@ -313,11 +313,7 @@ static int create_impl(int device, int nS, int ndirs, int nF, int64_t n, int nE,
     op->nrows = (int64_t)nV * nS;
     op->ncols = (int64_t)nF * nIC + (int64_t)nE * nEC + (int64_t)nISOv * nISO;
     op->arith = arith;
-    {
-        // float-float kernel family: packed pairs (default) or scalar samples
-        const char *v = getenv("CGB_FF_KERNEL");
-        op->ff_variant = (v && strcmp(v, "scalar") == 0) ? 0 : 1;
-    }
+    op->ff_variant = 1;  // float-float kernel family: packed pairs (cgb_op_ff_kernels selects the other)
     CGB_CUDA(cudaDeviceGetAttribute(&op->nsm, cudaDevAttrMultiProcessorCount, device));
     // lanes per voxel: whole warps for long sample vectors, sub-warps for short ones
     if (nS >= 96) op->lpv = 32;
@@ -528,6 +524,14 @@ int cgb_op_set_lut(cgb_op *op, const float *lutIC, const float *lutEC, const flo
                               cudaMemcpyDefault));
     }
     op->lut_r_kind = 0;  // reduced-precision copies are rebuilt on their next use
+    return CGB_OK;
+}
+
+int cgb_op_ff_kernels(cgb_op *op, int variant, int *out) {
+    if (!op) return fail(CGB_ERR_INVALID, "null handle");
+    if (variant > 1) return fail(CGB_ERR_INVALID, "variant must be 0 (scalar samples) or 1 (packed pairs)");
+    if (variant >= 0) op->ff_variant = variant;
+    if (out) *out = op->ff_variant;
     return CGB_OK;
 }
 

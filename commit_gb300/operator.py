@@ -192,6 +192,13 @@ class LinearOperator:
             out[name] = (int(c.value), float(a.value), float(b.value))
         return out
 
+    def ff_kernels(self, variant: int | None = None) -> int:
+        """Float-float kernel family: 1 packed sample pairs (default), 0 one sample per lane;
+        None only reads."""
+        out = ctypes.c_int32()
+        check(lib().cgb_op_ff_kernels(self._h.ptr, -1 if variant is None else int(variant), ctypes.byref(out)))
+        return int(out.value)
+
     def host_mode(self, mode: int | None = None) -> int:
         """Host-buffer products: 0 automatic (direct row access for page-locked rows),
         1 staged copies, 2 direct; None only reads."""

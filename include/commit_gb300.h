@@ -103,6 +103,12 @@ int cgb_op_lut_grad(cgb_op *op, const double *x, const double *g, double *g_ic, 
                     void *stream);
 
 /*
+ * Float-float kernel family: 1 (default) packed f32x2 pairs of samples on padded LUT rows,
+ * 0 one sample per lane; a negative value only reads.  Same arithmetic to ~1e-15.
+ */
+int cgb_op_ff_kernels(cgb_op *op, int variant, int *out);
+
+/*
  * Adjoint slabs: A' runs its voxel pass and fibre pass slab by slab (voxel ranges whose
  * per-segment terms fit in L2, so the fibre pass gathers them from L2).  nslab 0 chooses
  * the count from the problem size (the default at creation), 1 turns slabs off, 2..64

@@ -257,3 +257,15 @@ def test_page_locked_host_rows_direct_and_staged(mode):
     gd = A.T.dot(torch.from_numpy(wh.copy()).cuda()).cpu().numpy()
     assert np.array_equal(yh, yd)
     assert np.array_equal(gh, gd)
+
+
+@pytest.mark.parametrize('name', ['szb', 'multi_rf', 'eval_gaps', 'ball_stick'])
+def test_scalar_float_float_kernels_match_golden(name):
+    """The one-sample-per-lane float-float kernels (the other kernel family) against the
+    reference's golden products."""
+    from commit_gb300.operator import LinearOperator
+    c = G.load_case(name)
+    A = LinearOperator(c['D'], c['K'], None, nolut=c['nolut'])
+    assert A.ff_kernels(0) == 0
+    assert G.rel(A.dot(c['x_in']), c['Ax']) <= 1e-10
+    assert G.rel(A.T.dot(c['y_in']), c['Aty']) <= 1e-10
