@@ -36,7 +36,7 @@ METRIC = 'A·x+Aᵀx operator pairs/s (1M-streamline workload)'
 # --steps 1 --warmup 1 --no-e2e --no-cpu`, one pass, full workload; summarised in
 # profiles/operator_ff_hcp1m.md).  Keyed by (workload, streamlines, arith); the A' entry
 # is the 7 slab voxel passes plus the 7 slab fibre passes of one product.
-MEASURED_TRAFFIC = {('hcp_1m', 1000000, 'ff'): {'forward': 2636454144, 'adjoint': 11855195392}}
+MEASURED_TRAFFIC = {('hcp_1m', 1000000, 'ff'): {'forward': 2679165952, 'adjoint': 11855011840}}
 
 
 def parse():
