@@ -304,13 +304,15 @@ def _fista(y, A, spec: RegSpec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, a
 
 
 def solve_mixed(y, A, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, verbose=0, x0=None, regularisation=None,
-                confidence_array=None, arith='bf16', refine_arith=None, refine_max_iter=None,
+                confidence_array=None, arith='fp16', refine_arith=None, refine_max_iter=None,
                 refine_tol_fun=None, refine_tol_x=None, x_ref=None):
     """Reduced-precision FISTA followed by an FP64 refinement solve.
 
     Phase 1 runs FISTA with the operator in ``arith`` ('bf16', 'fp16' or 'f32': LUT in
     that format, FP16 lengths, FP32 accumulation; FISTA vectors, the Lipschitz estimate
-    and every objective / stopping reduction in FP64).  Phase 2 restarts the plain FP64
+    and every objective / stopping reduction in FP64).  The default is FP16: as fast as BF16
+    on GB300 (65 vs 69 operator pairs/s at 1M streamlines) with a tenth of its error
+    (solution within 4e-4 instead of 4e-3 of the FP64 one on the demo case).  Phase 2 restarts the plain FP64
     solver (float-float by default) from the phase-1 solution, which removes the bias of
     the reduced-precision operator.  Returns (x, details) with details['mixed'] and
     details['refine'] holding each phase's opt_details.
