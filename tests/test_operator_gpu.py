@@ -269,3 +269,34 @@ def test_scalar_float_float_kernels_match_golden(name):
     assert A.ff_kernels(0) == 0
     assert G.rel(A.dot(c['x_in']), c['Ax']) <= 1e-10
     assert G.rel(A.T.dot(c['y_in']), c['Aty']) <= 1e-10
+
+
+def test_handles_release_their_device_memory():
+    """Creating, using (float-float, reduced precision, slabs, batched, solver) and
+    destroying handles returns the device memory: no growth over repeated cycles."""
+    import gc
+    import torch
+    from commit_gb300 import solvers, synth
+    from commit_gb300.operator import LinearOperator
+    D, K = synth.make_dictionary(synth.scaled_spec('demo_5k', n_fibers=3000))
+    x = torch.from_numpy(synth.make_x(synth.n_cols(D, K), 1)).cuda()
+
+    def cycle():
+        A = LinearOperator(D, K, None)
+        A.set_slabs(3)
+        y = A.dot(x)
+        A.T.dot(y)
+        A.T.dot(y.float(), arith='bf16')
+        A.dot_batch([x, x])
+        solvers.solve(y, A, A.T, tol_fun=0, tol_x=0, max_iter=5, verbose=0)
+        solvers.solve_batch(y, A, [None, None, None], tol_fun=0, tol_x=0, max_iter=5)
+        del A
+        gc.collect()
+        torch.cuda.synchronize()
+
+    cycle()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(5):
+        cycle()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free0 - free1 < 64 << 20, (free0, free1)
