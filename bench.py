@@ -333,7 +333,11 @@ def run_ours(args):
     if args.fista:
         return run_fista(args, spec, D, K, dev)
     reduced = args.arith in ('bf16', 'fp16', 'f32')
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
     A = LinearOperator(D, K, None, arith='ff' if reduced else args.arith, device=dev.index)
+    torch.cuda.synchronize()
+    tcreate = time.perf_counter() - t0  # host arrays -> device re-layout (sorts, CSR, slabs)
     if args.slabs >= 0:
         A.set_slabs(args.slabs)
     At = A.T
@@ -385,7 +389,8 @@ def run_ours(args):
                         'traffic': traffic_for(args, spec, dom), 'algorithmic_bytes_per_launch': nbytes,
                         'forward_ms': fwd_ms, 'adjoint_ms': adj_ms,
                         'fma_per_product': nfma, 'achieved_gfma_s': nfma / (dom_ms / 1000.0) / 1e9},
-           'clocks': clk, 'gpu_launches': args.steps * launches_per_pair(A, reduced), 'setup_s': {'generate': tgen},
+           'clocks': clk, 'gpu_launches': args.steps * launches_per_pair(A, reduced),
+           'setup_s': {'generate': tgen, 'create_operator': tcreate},
            'occupancy_tuning': A.occupancy(), 'adjoint_slabs': A.set_slabs(None)}
     # end to end through the public API on pinned host buffers
     if not args.no_e2e and not reduced:
