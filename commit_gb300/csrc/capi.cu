@@ -193,7 +193,7 @@ int cgb_op_apply_host(cgb_op *op, int adjoint, const double *in, int64_t in_len,
 
 extern "C" int cgb_op_occupancy(cgb_op *op, int slot, int set, int *choice, float *ms_a, float *ms_b) {
     if (!op) return fail(CGB_ERR_INVALID, "null handle");
-    if (slot < 0 || slot >= kOccSlots) return fail(CGB_ERR_INVALID, "slot out of range");
+    if (slot < 0 || slot >= kOccSlots) return fail(CGB_ERR_INVALID, "slot out of range");  // kOccSlots = 24
     if (set >= 0) {
         if (set > 2) return fail(CGB_ERR_INVALID, "choice must be 0 (retune), 1 or 2");
         op->occ_choice[slot] = set;

@@ -90,6 +90,7 @@ struct cgb_op {
     void *lutIC_r, *lutEC_r, *lutISO_r;  // reduced-precision LUT copies (padded pair layout)
     int lut_r_kind;                 // CGB_ARITH_BF16 / CGB_ARITH_FP16 / 0
     int nSp_r;                      // row stride of the BF16 / FP16 copies: room for the 16- and 32-lane shapes
+    int ff_shape[2];                // float-float A / A' voxel shape: 0 not tuned, 1 default, 2 a warp per voxel
     int batch_lpv;                  // voxel shape of the multi-vector kernels: 0 not tuned, 1 default, 2 a warp per voxel
     __half *seg_l16;                // FP16 lengths scaled by 2^k (reduced path)
     float len16_inv_scale;          // 2^-k
@@ -97,8 +98,8 @@ struct cgb_op {
     void *gstate;                   // LUT-gradient streams (lutgrad.cu), built on first use
     int batch_rhs;                  // vectors per multi-right-hand-side pass (0: not tuned)
     int batch_reuse;                // batched FISTA momentum reuse chosen by timing (0: not tuned, 1 off, 2 on)
-    int occ_choice[16];             // occupancy build per tuned kernel (0: not tuned, 1 or 2), see occ_launch
-    float occ_ms[16][2];            // the two builds' times measured by the tuning
+    int occ_choice[24];             // occupancy build per tuned kernel (0: not tuned, 1 or 2), see occ_launch
+    float occ_ms[24][2];            // the two builds' times measured by the tuning
     uint32_t *vox_ptr, *seg_f, *eval, *fib_ptr, *fib_perm, *ec_ptr, *ec_col, *iso_ptr, *iso_col;
     uint16_t *seg_o, *ec_o;
     float *seg_l;
@@ -242,7 +243,10 @@ enum OccSlot {
     kOccAdjMixFused = 10,  // + arith - BF16
     kOccAdjR2Fused = 13,
     kOccAdjR4 = 14,
-    kOccSlots = 16
+    kOccFwdFFWide = 16,
+    kOccAdjFFWide = 17,
+    kOccAdjFFWideFused = 18,
+    kOccSlots = 24
 };
 
 template <class FA, class FB>

@@ -366,8 +366,9 @@ static int create_impl(int device, int nS, int ndirs, int nF, int64_t n, int nE,
     CGB_TRY(dalloc(op, &op->lutISO, lutISO_n)); CGB_TRY(upload(op->lutISO, lutISO, nolut ? 0 : lutISO_n));
     // zero-padded copies with row stride nSp for the paired float-float kernels
     {
-        const detail::PairShape ps = detail::pick_pair_shape(nS);
-        op->nSp = 2 * ps.lpv * ps.np;
+        // rows padded for both voxel shapes of the pair kernels (the tuner may pick either)
+        const detail::PairShape ps = detail::pick_pair_shape(nS), pw = detail::wide_pair_shape(nS);
+        op->nSp = 2 * ps.lpv * ps.np > 2 * pw.lpv * pw.np ? 2 * ps.lpv * ps.np : 2 * pw.lpv * pw.np;
         const size_t sp = (size_t)op->nSp;
         CGB_TRY(dalloc(op, &op->lutIC_p, (size_t)nIC * op->ndirs * sp));
         CGB_TRY(dalloc(op, &op->lutEC_p, (size_t)nEC * op->ndirs * sp));
@@ -524,6 +525,17 @@ int cgb_op_set_lut(cgb_op *op, const float *lutIC, const float *lutEC, const flo
                               cudaMemcpyDefault));
     }
     op->lut_r_kind = 0;  // reduced-precision copies are rebuilt on their next use
+    return CGB_OK;
+}
+
+int cgb_op_ff_shape(cgb_op *op, int set, int *fwd, int *adj) {
+    if (!op) return fail(CGB_ERR_INVALID, "null handle");
+    if (set >= 0) {
+        if (set > 2) return fail(CGB_ERR_INVALID, "shape must be 0 (tune), 1 (default) or 2 (a warp per voxel)");
+        op->ff_shape[0] = op->ff_shape[1] = set;
+    }
+    if (fwd) *fwd = op->ff_shape[0];
+    if (adj) *adj = op->ff_shape[1];
     return CGB_OK;
 }
 

@@ -35,7 +35,8 @@ struct FwdPair {
     }
     template <int L, int N>
     int run() {
-        return occ_launch(op, kOccFwdFF, st, [&] { return launch<L, N, 3>(); }, [&] { return launch<L, N, 4>(); });
+        const int slot = L == 32 && L != pick_pair_shape(op->nS).lpv ? kOccFwdFFWide : kOccFwdFF;
+        return occ_launch(op, slot, st, [&] { return launch<L, N, 3>(); }, [&] { return launch<L, N, 4>(); });
     }
 };
 
@@ -67,28 +68,52 @@ struct AdjPair {
     }
     template <int L, int N>
     int run() {
+        const bool wide = L == 32 && L != pick_pair_shape(op->nS).lpv;
         // the fused-forward build (in_mode 1) holds the forward row as well
         if (in_mode == 1)
-            return occ_launch(op, kOccAdjFFFused, st, [&] { return launch<L, N, 1, true>(); },
-                              [&] { return launch<L, N, 2, true>(); });
-        return occ_launch(op, kOccAdjFF, st, [&] { return launch<L, N, 2, false>(); },
+            return occ_launch(op, wide ? kOccAdjFFWideFused : kOccAdjFFFused, st,
+                              [&] { return launch<L, N, 1, true>(); }, [&] { return launch<L, N, 2, true>(); });
+        return occ_launch(op, wide ? kOccAdjFFWide : kOccAdjFF, st, [&] { return launch<L, N, 2, false>(); },
                           [&] { return launch<L, N, 3, false>(); });
     }
 };
 
 }  // namespace
 
+// Voxel shape of the pair kernels: the single-vector default (fewest padded samples) or a
+// warp per voxel (half the samples per lane, fewer registers).  On the first call outside
+// stream capture both are run with their occupancy builds tuned, and the faster shape is
+// kept on the handle (ff_shape[0] for A, [1] for A').
+template <class Fn>
+static int shaped(cgb_op *op, int which, int slot_default, int slot_wide, cudaStream_t st, Fn &L) {
+    const PairShape d = pick_pair_shape(op->nS), w = wide_pair_shape(op->nS);
+    int &choice = op->ff_shape[which];
+    if (choice == 0 && w.lpv != d.lpv) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        CGB_CUDA(cudaStreamIsCapturing(st, &cs));
+        if (cs == cudaStreamCaptureStatusNone) {
+            CGB_TRY(dispatch_pair_shape(d, L));
+            CGB_TRY(dispatch_pair_shape(w, L));
+            const float td = fminf(op->occ_ms[slot_default][0], op->occ_ms[slot_default][1]);
+            const float tw = fminf(op->occ_ms[slot_wide][0], op->occ_ms[slot_wide][1]);
+            choice = tw < td ? 2 : 1;
+        }
+    }
+    return dispatch_pair_shape(choice == 2 && w.lpv != d.lpv ? w : d, L);
+}
+
 int forward_ff(cgb_op *op, const double *x, double *y, double *ax, const double *yobs, const double *sqw,
                double *partials, cudaStream_t st, int *grid) {
     FwdPair L{op, x, y, ax, yobs, sqw, partials, st, grid};
-    return dispatch_pair_shape(pick_pair_shape(op->nS), L);
+    return shaped(op, 0, kOccFwdFF, kOccFwdFFWide, st, L);
 }
 
 int adjoint_ff(cgb_op *op, const double *yin, int in_mode, const double *x, const double *yobs, const double *sqw,
                const double *ax_a, const double *ax_b, double ca, double cb, double *xout, double *partials,
                cudaStream_t st, int *grid) {
     AdjPair L{op, yin, in_mode, x, yobs, sqw, ax_a, ax_b, ca, cb, xout, partials, st, grid};
-    return dispatch_pair_shape(pick_pair_shape(op->nS), L);
+    if (in_mode == 1) return dispatch_pair_shape(op->ff_shape[1] == 2 ? wide_pair_shape(op->nS) : pick_pair_shape(op->nS), L);
+    return shaped(op, 1, kOccAdjFF, kOccAdjFFWide, st, L);
 }
 
 }  // namespace cgb

@@ -179,7 +179,8 @@ class LinearOperator:
     OCC_SLOTS = {'ff_forward': 0, 'ff_adjoint': 1, 'bf16_adjoint': 2, 'fp16_adjoint': 3, 'f32_adjoint': 4,
                  'bf16x2_adjoint': 5, 'bf16_forward': 6, 'fp16_forward': 7, 'f32_forward': 8,
                  'ff_fused_gradient': 9, 'bf16_fused_gradient': 10, 'fp16_fused_gradient': 11,
-                 'f32_fused_gradient': 12, 'bf16x2_fused_gradient': 13, 'bf16x4_adjoint': 14}
+                 'f32_fused_gradient': 12, 'bf16x2_fused_gradient': 13, 'bf16x4_adjoint': 14,
+                 'ff_forward_wide': 16, 'ff_adjoint_wide': 17, 'ff_fused_gradient_wide': 18}
 
     def occupancy(self, set_to: dict | None = None) -> dict:
         """Occupancy autotuning state per tuned kernel: {name: (choice, ms_build1, ms_build2)}
@@ -191,6 +192,14 @@ class LinearOperator:
             check(lib().cgb_op_occupancy(self._h.ptr, slot, st, ctypes.byref(c), ctypes.byref(a), ctypes.byref(b)))
             out[name] = (int(c.value), float(a.value), float(b.value))
         return out
+
+    def ff_shape(self, set_to: int | None = None) -> tuple:
+        """Voxel shape of the float-float pair kernels (A, A'): 1 default, 2 a warp per voxel,
+        0 timed on the next call; ``set_to`` sets both."""
+        f, a = ctypes.c_int32(), ctypes.c_int32()
+        check(lib().cgb_op_ff_shape(self._h.ptr, -1 if set_to is None else int(set_to), ctypes.byref(f),
+                                    ctypes.byref(a)))
+        return int(f.value), int(a.value)
 
     def ff_kernels(self, variant: int | None = None) -> int:
         """Float-float kernel family: 1 packed sample pairs (default), 0 one sample per lane;

@@ -103,6 +103,13 @@ int cgb_op_lut_grad(cgb_op *op, const double *x, const double *g, double *g_ic, 
                     void *stream);
 
 /*
+ * Voxel shape of the float-float pair kernels: 1 the default (fewest padded samples), 2 a
+ * warp per voxel, 0 = timed on the next call (the default at creation); set < 0 only reads.
+ * *fwd / *adj (may be NULL) receive the shapes of A and A'.  Results agree to ~1e-16.
+ */
+int cgb_op_ff_shape(cgb_op *op, int set, int *fwd, int *adj);
+
+/*
  * Float-float kernel family: 1 (default) packed f32x2 pairs of samples on padded LUT rows,
  * 0 one sample per lane; a negative value only reads.  Same arithmetic to ~1e-15.
  */
@@ -267,7 +274,8 @@ int cgb_op_apply_batch(cgb_op *op, int adjoint, int nvec, const void *const *in,
  * Occupancy autotuning of the voxel kernels.  Slots: 0 float-float A, 1 float-float A' pass
  * 1, 2 / 3 / 4 reduced-precision A' pass 1 (BF16 / FP16 / F32), 5 two-vector BF16 A',
  * 6 / 7 / 8 reduced-precision A (BF16 / FP16 / F32), 9 float-float fused A x + A' pass 1,
- * 10 / 11 / 12 reduced-precision fused A x + A' pass 1, 13 two-vector fused, 14 four-vector A'.
+ * 10 / 11 / 12 reduced-precision fused A x + A' pass 1, 13 two-vector fused, 14 four-vector A',
+ * 16 / 17 / 18 float-float A / A' / fused A' in the warp-per-voxel shape.
  * Each tuned kernel has two builds with different register caps (2: the tighter cap, more
  * resident warps); the first call on a handle times both on its own arguments and keeps the
  * faster.

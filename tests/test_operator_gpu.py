@@ -300,3 +300,27 @@ def test_handles_release_their_device_memory():
         cycle()
     free1 = torch.cuda.mem_get_info()[0]
     assert free0 - free1 < 64 << 20, (free0, free1)
+
+
+@pytest.mark.parametrize('name', ['szb', 'multi_rf', 'eval_gaps', 'ball_stick', 'scalar_map'])
+def test_float_float_voxel_shapes_match_golden(name):
+    """Both voxel shapes of the float-float pair kernels (default lanes per voxel, a warp
+    per voxel) reproduce the reference's products, and the FISTA fits."""
+    from commit_gb300 import solvers
+    from commit_gb300.operator import LinearOperator
+    c = G.load_case(name)
+    out = {}
+    for shape in (1, 2):
+        A = LinearOperator(c['D'], c['K'], None, nolut=c['nolut'])
+        A.ff_shape(shape)
+        out[shape] = (A.dot(c['x_in']), A.T.dot(c['y_in']))
+        assert G.rel(out[shape][0], c['Ax']) <= 1e-10
+        assert G.rel(out[shape][1], c['Aty']) <= 1e-10
+        f = c['fits']['nnls']
+        x, det = solvers.solve(c['y_obs'], A, A.T, tol_fun=1e-5, tol_x=1e-7, max_iter=f['details']['iterations'],
+                               verbose=0, regularisation=solvers.init_regularisation(G.fresh_reg(f['reg'])),
+                               confidence_array=f['conf'])
+        assert det['iterations'] == f['details']['iterations']
+        assert G.rel(x, f['x']) <= 1e-8
+    assert G.rel(out[1][0], out[2][0]) <= 1e-13
+    assert G.rel(out[1][1], out[2][1]) <= 1e-13
