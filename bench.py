@@ -66,7 +66,7 @@ def parse():
     p.add_argument('--batch-scale', type=float, default=1.0, help='scale of the tractogram sizes (smaller runs)')
     p.add_argument('--batch-iters', type=int, default=20, help='FISTA iterations per solve (tolerances off)')
     p.add_argument('--batch-streams', type=int, default=4, help='tractograms solved concurrently (streams)')
-    p.add_argument('--sample-frac', type=float, default=1.0 / 16.0, help='CPU sample: fraction of the segments')
+    p.add_argument('--sample-frac', type=float, default=0.25, help='CPU sample: fraction of the segments')
     p.add_argument('--no-e2e', action='store_true')
     p.add_argument('--no-cpu', action='store_true')
     return p.parse_args()
@@ -417,7 +417,7 @@ def run_ours(args):
                                     'by the kernels over NVLink-C2C' if A.host_mode(None) != 1 else
                                     'staged copies pipelined against the kernels')}
     if rank == 0 and ws == 1 and not args.no_cpu:
-        out['cpu_baseline'] = cpu_reference(D, K, args.sample_frac, 3, 1)
+        out['cpu_baseline'] = cpu_reference(D, K, args.sample_frac, 5, 1)
     if rank == 0:
         print(json.dumps(out))
     if ws > 1:
