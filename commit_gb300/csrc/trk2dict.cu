@@ -4,9 +4,13 @@
 //
 // The reference walks each streamline on one CPU thread and merges its pieces in a
 // std::map keyed by (orientation, z, y, x).  Here:
-//   1. k_walk (count)  one thread per streamline runs the forward model and counts the
-//                      pieces (voxel, orientation, weighted length) it produces;
-//   2. k_walk (emit)   the same walk writes them, keyed, at the streamline's offset;
+//   1. k_room          an estimate of each streamline's pieces (voxel faces crossed per
+//                      step plus spares) gives it room in one piece buffer;
+//   2. k_walk          one thread per streamline (longest first) runs the forward model
+//                      and writes its keyed pieces (voxel, orientation, weighted length)
+//                      into that room, reporting the count; a streamline that outgrew its
+//                      room sends the whole call down the exact path (count walk, then
+//                      emit walk at exact offsets);
 //   3. a segmented stable sort by key per streamline (CUB) puts equal keys together in
 //      generation order, so
 //   4. k_merge sums each key's pieces in that order in FP32, exactly as the map's
