@@ -30,13 +30,17 @@ sys.path.insert(0, ROOT)
 
 METRIC = 'A·x+Aᵀx operator pairs/s (1M-streamline workload)'
 
-# DRAM bytes (read + write) per product from one ncu capture of the same workload
+# DRAM bytes (read + write) per product, recorded from one ncu capture of this workload
 # (`ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum
 # --clock-control none -k regex:"k_(forward_p|adjoint_p|fibre_sum)" --csv python bench.py
-# --steps 1 --warmup 1 --no-e2e --no-cpu`, one pass, full workload; summarised in
-# profiles/operator_ff_hcp1m.md).  Keyed by (workload, streamlines, arith); the A' entry
-# is the 7 slab voxel passes plus the 7 slab fibre passes of one product.
+# --steps 1 --warmup 1 --no-e2e --no-cpu`, one pass, full workload).  A constant: the bench
+# line labels it as such.  Keyed by (workload, streamlines, arith); the A' entry is the slab
+# voxel passes plus the slab fibre passes of one product.
 MEASURED_TRAFFIC = {('hcp_1m', 1000000, 'ff'): {'forward': 2679165952, 'adjoint': 11855011840}}
+
+
+# relative-error bounds of the reduced-precision LUT formats (the FP64 path's bar is 1e-10)
+REDUCED_BOUNDS = {'bf16': 1.5e-2, 'fp16': 4e-3, 'f32': 2e-5}
 
 
 def parse():
@@ -69,6 +73,10 @@ def parse():
     p.add_argument('--sample-frac', type=float, default=0.25, help='CPU sample: fraction of the segments')
     p.add_argument('--no-e2e', action='store_true')
     p.add_argument('--no-cpu', action='store_true')
+    p.add_argument('--no-f64', action='store_true', help='skip the native-FP64 arithmetic pairs')
+    p.add_argument('--tensor-cores', type=int, default=-1,
+                   help='reduced-precision BF16 path: 0 tensor cores when the shape allows, 1 CUDA cores, '
+                        '2 tensor cores required (default: the handle\'s own setting)')
     return p.parse_args()
 
 
@@ -173,34 +181,10 @@ def algorithmic(D, K, reduced=False) -> tuple:
 
 
 def sample_slab(D, K, frac: float):
-    """Central slab of voxels holding about `frac` of the IC segments (voxel-sorted)."""
-    vox = D['IC']['vox']
-    nV = D['IC']['nVOX']
-    counts = np.bincount(vox, minlength=nV)
-    c = np.cumsum(counts)
-    n = int(c[-1])
-    mid = int(np.searchsorted(c, n // 2))
-    lo, hi = mid, mid
-    target = max(1, int(frac * n))
-    while (int(c[hi - 1]) if hi > 0 else 0) - (int(c[lo - 1]) if lo > 0 else 0) < target and (lo > 0 or hi < nV):
-        lo = max(0, lo - max(1, (hi - lo) // 2 + 16))
-        hi = min(nV, hi + max(1, (hi - lo) // 2 + 16))
-    s0 = int(c[lo - 1]) if lo > 0 else 0
-    s1 = int(c[hi - 1]) if hi > 0 else 0
-    IC = {k: np.ascontiguousarray(D['IC'][k][s0:s1]) for k in ('str', 'vox', 'dir', 'len')}
-    IC['vox'] = (IC['vox'] - lo).astype(np.uint32)
-    IC['n'] = s1 - s0
-    IC['nSTR'] = D['IC']['nSTR']
-    IC['nVOX'] = hi - lo
-    IC['eval'] = np.ones(IC['nSTR'] * K['wmr'].shape[0], np.uint32)
-    ev = D['EC']['vox']
-    e0, e1 = np.searchsorted(ev, lo), np.searchsorted(ev, hi)
-    EC = {'vox': (ev[e0:e1] - lo).astype(np.uint32), 'dir': np.ascontiguousarray(D['EC']['dir'][e0:e1]),
-          'n': int(e1 - e0)}
-    iv = D['ISO']['vox']
-    i0, i1 = np.searchsorted(iv, lo), np.searchsorted(iv, hi)
-    ISO = {'vox': (iv[i0:i1] - lo).astype(np.uint32), 'n': int(i1 - i0)}
-    return {'IC': IC, 'EC': EC, 'ISO': ISO}, (s1 - s0) / n, (lo, hi)
+    """Central slab of voxels holding about `frac` of the IC segments (synth.voxel_slab)."""
+    from commit_gb300 import synth
+    S = synth.voxel_slab(D, K, frac)
+    return S['D'], S['share'], S['voxels']
 
 
 def cpu_reference_fista(D, K, frac, iters):
@@ -230,15 +214,19 @@ def cpu_reference_fista(D, K, frac, iters):
                       f'in {dt * iters:.2f} s (initialisation included), time scaled by segment share'}
 
 
-def cpu_reference(D, K, frac, steps, warmup):
+def cpu_reference(D, K, frac, steps, warmup, x_full=None):
     """Time the reference CPU operator (oracle/_ref if compiled for this host, else the
     C restatement) on a voxel-slab sample; returns a cpu_baseline dict (pairs/s scaled
-    to the full workload by segment count)."""
+    to the full workload by segment count).  With x_full (the benchmark's own column
+    vector) the sample's x is its slab columns, and the last pair's outputs are returned
+    under 'outputs' for checking the GPU's results on the slab."""
     sys.path.insert(0, os.path.join(ROOT, 'oracle'))
     import oracle as O
     import build_ref
+    from commit_gb300 import synth
     cores = os.cpu_count() or 1
-    Ds, share, (lo, hi) = sample_slab(D, K, frac)
+    S = synth.voxel_slab(D, K, frac)
+    Ds, share, (lo, hi) = S['D'], S['share'], S['voxels']
     kind = 'port'
     try:
         if build_ref.generate() and build_ref.compile_operator() and O.ref_available():
@@ -250,21 +238,50 @@ def cpu_reference(D, K, frac, steps, warmup):
         A = O.RefOperator(Ds, K, O.set_threads(Ds, threads))
     else:
         A = O.PortOperator(Ds, K, None, nthreads=threads)
-    x = np.random.default_rng(11).uniform(0.0, 1.0, size=A.nCOLS)
+    if x_full is None:
+        x = np.random.default_rng(11).uniform(0.0, 1.0, size=A.nCOLS)
+    else:
+        x = np.ascontiguousarray(x_full[S['cols']])
     for _ in range(max(1, warmup)):
         y = A.dot(x)
-        A.T.dot(y)
+        g = A.T.dot(y)
     t0 = time.perf_counter()
     for _ in range(steps):
         y = A.dot(x)
-        A.T.dot(y)
+        g = A.T.dot(y)
     dt = time.perf_counter() - t0
     rate_sample = steps / dt
-    return {'value': rate_sample * share, 'unit': 'pairs/s', 'cores': threads, 'kind': kind,
-            'sample': (f'central voxel slab [{lo},{hi}) = {share * 100:.2f}% of the IC segments '
-                       f'({Ds["IC"]["n"]} segments, {Ds["EC"]["n"]} EC, {Ds["ISO"]["n"]} ISO); {steps} pairs in '
-                       f'{dt:.2f} s on {threads} threads, rate scaled by segment share'),
-            'sample_pairs_per_s': rate_sample}
+    out = {'value': rate_sample * share, 'unit': 'pairs/s', 'cores': threads, 'kind': kind,
+           'sample': (f'central voxel slab [{lo},{hi}) = {share * 100:.2f}% of the IC segments '
+                      f'({Ds["IC"]["n"]} segments, {Ds["EC"]["n"]} EC, {Ds["ISO"]["n"]} ISO); {steps} pairs in '
+                      f'{dt:.2f} s on {threads} threads, rate scaled by segment share'),
+           'sample_pairs_per_s': rate_sample}
+    if x_full is not None:
+        out['outputs'] = {'y': y, 'g': g, 'cols': S['cols'], 'voxels': (lo, hi)}
+    return out
+
+
+def check_against_reference(A, y_gpu, cb, nS, arith='ff') -> dict:
+    """Relative 2-norm errors of the GPU's timed A x on the reference sample's rows, and of
+    the GPU's A' (of the reference's y placed in those rows, zero elsewhere) on its columns."""
+    import torch
+    o = cb.pop('outputs')
+    lo, hi = o['voxels']
+    r0, r1 = lo * nS, hi * nS
+    yg = y_gpu[r0:r1].double().cpu().numpy()
+    fwd = float(np.linalg.norm(yg - o['y']) / np.linalg.norm(o['y']))
+    ym = torch.zeros(A.nROWS, dtype=torch.float64, device=y_gpu.device)
+    ym[r0:r1] = torch.from_numpy(o['y']).to(y_gpu.device)
+    if arith in REDUCED_BOUNDS:
+        g = A.T.dot(ym.float(), arith=arith).double().cpu().numpy()
+    else:
+        g = A.T.dot(ym).cpu().numpy()
+    gm = np.zeros(A.nCOLS)
+    gm[o['cols']] = o['g']
+    adj = float(np.linalg.norm(g - gm) / np.linalg.norm(gm))
+    return {'forward_rel': fwd, 'adjoint_rel': adj, 'bar': REDUCED_BOUNDS.get(arith, 1e-10),
+            'what': 'timed A x on the reference sample rows; A\' of the reference y on the sample columns',
+            'rows': [int(r0), int(r1)]}
 
 
 def build_workload(args, device):
@@ -288,11 +305,18 @@ def workload_config(spec, D, K, args):
             'arith': args.arith, 'l2': 'inputs larger than L2 (y is nV*nS f64), no flush'}
 
 
-def launches_per_pair(A, reduced: bool) -> int:
-    """Kernels of one A + A' pair: the forward, then per adjoint slab a voxel pass and a fibre
-    pass (one of each without slabs); the FP32-vector path adds two conversions."""
+def launches_per_pair(A, reduced: bool, tc: bool = False) -> int:
+    """Kernels of one A + A' pair.  FP64 path: the max-|x| pass of the range guard and the
+    forward, then per adjoint slab a voxel pass and a fibre pass.  Reduced precision: the
+    FP32 -> FP64 column conversion and the forward, the adjoint (slab passes, or the
+    tensor-core voxel pass and its fibre pass) and the FP64 -> FP32 conversion; the
+    tensor-core forward adds its x*eval pass."""
     ns = max(1, A.set_slabs(None))
-    return 1 + 2 * ns + (2 if reduced else 0)
+    if tc:
+        return 3 + 3
+    if reduced:
+        return 2 + 2 * ns + 1
+    return 2 + 2 * ns
 
 
 def traffic_for(args, spec, dom: str):
@@ -340,6 +364,8 @@ def run_ours(args):
     tcreate = time.perf_counter() - t0  # host arrays -> device re-layout (sorts, CSR, slabs)
     if args.slabs >= 0:
         A.set_slabs(args.slabs)
+    if args.tensor_cores >= 0:
+        A.tensor_cores(args.tensor_cores)
     At = A.T
     nbytes, nfma, nrows, ncols = algorithmic(D, K, reduced)
     vdt = torch.float32 if reduced else torch.float64
@@ -386,12 +412,39 @@ def run_ours(args):
            'data': 'synthetic', 'config': workload_config(spec, D, K, args),
            'roofline': {'bound': 'hbm', 'kernel': dom, 'achieved': achieved, 'peak': peaks['hbm_gbs'],
                         'unit': 'GB/s', 'frac': achieved / peaks['hbm_gbs'], 'peak_src': peaks['src'],
-                        'traffic': traffic_for(args, spec, dom), 'algorithmic_bytes_per_launch': nbytes,
+                        'traffic': traffic_for(args, spec, dom),
+                        'traffic_src': 'recorded constant: dram__bytes_read.sum + dram__bytes_write.sum of one ncu '
+                                       'capture of this workload and arithmetic, per product',
+                        'algorithmic_bytes_per_launch': nbytes,
                         'forward_ms': fwd_ms, 'adjoint_ms': adj_ms,
                         'fma_per_product': nfma, 'achieved_gfma_s': nfma / (dom_ms / 1000.0) / 1e9},
-           'clocks': clk, 'gpu_launches': args.steps * launches_per_pair(A, reduced),
+           'clocks': clk,
+           'gpu_launches': args.steps * launches_per_pair(A, reduced, reduced and args.arith == 'bf16' and A.tensor_cores()),
            'setup_s': {'generate': tgen, 'create_operator': tcreate},
-           'occupancy_tuning': A.occupancy(), 'adjoint_slabs': A.set_slabs(None)}
+           'occupancy_tuning': A.occupancy(), 'adjoint_slabs': A.set_slabs(None),
+           'tensor_cores': bool(reduced and args.arith == 'bf16' and A.tensor_cores())}
+    # the reference's own FP64 arithmetic (native FP64 FMAs) on the same vectors, a few pairs
+    if args.arith == 'ff' and not args.no_f64:
+        nf = 3
+        for _ in range(2):
+            A.dot(x, out=y, arith='f64')
+            At.dot(y, out=g, arith='f64')
+        torch.cuda.synchronize()
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        f_ms, a_ms = 0.0, 0.0
+        for _ in range(nf):
+            e[0].record(st)
+            A.dot(x, out=y, arith='f64')
+            e[1].record(st)
+            At.dot(y, out=g, arith='f64')
+            e[2].record(st)
+            torch.cuda.synchronize()
+            f_ms += e[0].elapsed_time(e[1]) / nf
+            a_ms += e[1].elapsed_time(e[2]) / nf
+        out['f64_arith'] = {'pairs_per_s': 1000.0 / (f_ms + a_ms), 'forward_ms': f_ms, 'adjoint_ms': a_ms,
+                            'pairs': nf, 'note': 'native FP64 FMAs (the reference arithmetic), same workload'}
+        # leave y as the float-float A x of the timed steps for the parity check below
+        A.dot(x, out=y)
     # end to end through the public API on pinned host buffers
     if not args.no_e2e and not reduced:
         xh = torch.empty(ncols, dtype=torch.float64, pin_memory=True).numpy()
@@ -416,8 +469,26 @@ def run_ours(args):
                                     'x copied to and from the device, the row vector read / written in place '
                                     'by the kernels over NVLink-C2C' if A.host_mode(None) != 1 else
                                     'staged copies pipelined against the kernels')}
+        # the shape of COMMIT's own call site (operator.pyx:114-184): pageable numpy vectors in,
+        # a fresh numpy output per call
+        xp = x.cpu().numpy().copy()
+        for _ in range(max(1, args.warmup)):
+            At.dot(A.dot(xp))
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            yp = A.dot(xp)
+            At.dot(yp)
+        dt = time.perf_counter() - t0
+        if ws > 1:
+            dt = max_over_ranks(dt, dev)
+        out['e2e_pageable'] = {'value': replica_value(args.steps, dt, ws), 'unit': 'pairs/s',
+                               'h2d_bytes_per_step': (ncols + nrows) * 8, 'd2h_bytes_per_step': (nrows + ncols) * 8,
+                               'host_path': 'pageable numpy vectors through LinearOperator.dot, fresh output '
+                                            'arrays per call (the reference call site)'}
     if rank == 0 and ws == 1 and not args.no_cpu:
-        out['cpu_baseline'] = cpu_reference(D, K, args.sample_frac, 5, 1)
+        cb = cpu_reference(D, K, args.sample_frac, 5, 1, x_full=x.double().cpu().numpy())
+        out['parity_vs_reference'] = check_against_reference(A, y, cb, K['wmr'].shape[2], args.arith)
+        out['cpu_baseline'] = cb
     if rank == 0:
         print(json.dumps(out))
     if ws > 1:

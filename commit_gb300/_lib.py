@@ -98,6 +98,8 @@ def lib() -> ctypes.CDLL:
     L.cgb_fista_batch_run.argtypes = [P, P, P, ctypes.POINTER(CgbReg), c_i32, ctypes.POINTER(CgbFistaParams),
                                       ctypes.POINTER(c_vp), ctypes.POINTER(CgbFistaResult), P]
     L.cgb_op_host_mode.argtypes = [P, c_i32, ctypes.POINTER(c_i32)]
+    L.cgb_op_tensor_cores.argtypes = [P, c_i32, ctypes.POINTER(c_i32)]
+    L.cgb_op_device_status.argtypes = [P]
     L.cgb_op_ff_shape.argtypes = [P, c_i32, ctypes.POINTER(c_i32), ctypes.POINTER(c_i32)]
     L.cgb_op_ff_kernels.argtypes = [P, c_i32, ctypes.POINTER(c_i32)]
     L.cgb_op_set_slabs.argtypes = [P, c_i32, ctypes.POINTER(c_i32)]

@@ -93,6 +93,8 @@ static int apply_host_pipelined(cgb_op *op, int adjoint, const double *in, int64
     auto vb = [&](int k) { return slabs ? op->slab_v[k] : (int)((int64_t)op->nV * k / kPipe); };
     if (!adjoint) {
         CGB_CUDA(cudaMemcpyAsync(op->d_in, in, in_len * sizeof(double), cudaMemcpyHostToDevice, sc));
+        CGB_TRY(measure_input(op, op->d_in, in_len, sc));
+        XScale guard(op);
         for (int k = 0; k < K; ++k) {
             const int v0 = vb(k), v1 = vb(k + 1);
             if (v1 > v0) {
@@ -134,6 +136,7 @@ int cgb_op_apply(cgb_op *op, int adjoint, const void *in, int64_t in_len, void *
     if (!op) return fail(CGB_ERR_INVALID, "null handle");
     CGB_TRY(check_lengths(op, adjoint, in_len, out_len));
     if ((in_len > 0 && !in) || (out_len > 0 && !out)) return fail(CGB_ERR_INVALID, "null vector");
+    NvtxRange nv(adjoint ? "cgb_op_apply A'" : "cgb_op_apply A");
     DevGuard g(op->device);
     cudaStream_t st = (cudaStream_t)stream;
     if (out_len == 0) return CGB_OK;
@@ -165,6 +168,7 @@ int cgb_op_apply_host(cgb_op *op, int adjoint, const double *in, int64_t in_len,
     if (!op) return fail(CGB_ERR_INVALID, "null handle");
     CGB_TRY(check_lengths(op, adjoint, in_len, out_len));
     if ((in_len > 0 && !in) || (out_len > 0 && !out)) return fail(CGB_ERR_INVALID, "null vector");
+    NvtxRange nv(adjoint ? "cgb_op_apply_host A'" : "cgb_op_apply_host A");
     DevGuard g(op->device);
     if (out_len == 0) return CGB_OK;
     // staging buffers sized for the larger of the two vector lengths, kept on the handle

@@ -7,6 +7,8 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <string>
 
 #include "../../include/commit_gb300.h"
@@ -29,6 +31,16 @@ int cuda_fail(cudaError_t e, const char *what);
         int rc__ = (call);                    \
         if (rc__ != CGB_OK) return rc__;      \
     } while (0)
+
+// ------------------------------------------------------------------ tracing
+// NVTX range over a scope (an entry point, a FISTA iteration); a no-op unless a profiler
+// (Nsight Systems / Compute) is attached
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // ------------------------------------------------------------------ sizes
 constexpr int kMaxChunks = 16;       // samples per lane: nS <= 32 * kMaxChunks
@@ -57,6 +69,11 @@ struct OpDev {
     const uint16_t *ec_o;           // [nE]
     const uint32_t *iso_ptr;        // [nV+1]
     const uint32_t *iso_col;        // [nISOv]
+    // float-float range guard (operator_kernels.cuh ff_exp_hi): magnitude bits of max|x| of
+    // the forward input (null: not measured, no scaling) and the exponents of the largest
+    // LUT value times the largest length (forward) and of the largest LUT value (adjoint)
+    const unsigned long long *xmax;
+    int lut_exp_fwd, lut_exp_adj;
 };
 
 // vectors of a multi-right-hand-side pass (batch.cuh)
@@ -107,6 +124,9 @@ struct cgb_op {
     float *scratch32;               // [nIC*n] per-segment adjoint terms (FP32 path), on demand
     double *partials;               // block partial sums
     double *dscal;                  // device scalars
+    unsigned long long *d_xmax;     // max |x| (magnitude bits) of the current forward input
+    int xmax_on;                    // 1 while d_xmax holds the input of the launches being issued
+    int lut_exp_fwd, lut_exp_adj;   // exponents of max|LUT| * max(length, 1) and of max|LUT|
     double *h_scal;                 // pinned host scalars
     double *d_in, *d_out;           // staging for cgb_op_apply_host
     int64_t d_in_len, d_out_len;
@@ -121,6 +141,23 @@ struct cgb_op {
     cudaStream_t slab_st[3];        // slab schedule streams (created on first use)
     cudaEvent_t slab_ev[68];
     cudaEvent_t pipe_ev[8];
+    // tensor-core BF16 forward (tc_forward.cu), laid out on first use
+    int tc_mode;                    // 0 automatic, 1 CUDA cores only, 2 tensor cores
+    int tc_ready;                   // entries and LUT images built
+    int tc_np, tc_nkb, tc_ntiles;   // padded samples, K-blocks of 64 LUT rows, tiles of 128 voxels
+    int tc_kb_ec;                   // first K-block of the EC / ISO rows
+    float tc_lscale;                // 2^-k of the FP16 lengths
+    uint32_t *tc_ptr, *tc_co;       // entry offsets per (tile, K-block, voxel); column | row << 26
+    __half *tc_l;                   // entry lengths (FP16, scaled by 2^k)
+    __nv_bfloat16 *tc_bimg;         // LUT K-block images (swizzled BF16)
+    float *tc_xe;                   // x * eval as FP32, per forward
+    int *tc_err;                    // device status word of the bounded waits
+    int tc_kbs, tc_rounds;          // adjoint: sample K-blocks of 64, rounds of 256 LUT rows
+    int64_t tc_nent;                // entries
+    uint32_t *tc_fptr, *tc_fperm;   // adjoint: IC entry positions grouped by column, CSR offsets
+    __nv_bfloat16 *tc_abimg;        // adjoint LUT images
+    float *tc_terms;                // adjoint IC terms in entry order
+    float *tc_ax;                   // A x rows for the gradient (FISTA), on demand
     size_t bytes;
     int nsm;
     cgb::OpDev dev() const;
@@ -159,6 +196,15 @@ int launch_forward_R(cgb_op *op, int R, const RhsPtrs &V, const float *yobs, con
 int launch_adjoint_R(cgb_op *op, int R, const RhsPtrs &V, int in_mode, const float *yobs, const float *sqw,
                      double *partials, cudaStream_t st, int *grid);
 int fibre_sum32_from(cgb_op *op, const float *scr, double *xout, cudaStream_t st);
+// tensor-core BF16 forward (tc_forward.cu)
+bool tc_forward_enabled(const cgb_op *op);
+bool tc_supported(const cgb_op *op);
+int ensure_tc(cgb_op *op);
+// tensor-core BF16 A' (tc_adjoint.cu): mode 0 z = yin; 2 z = sqw*r, r = sqw*(ca*axa + cb*axb - yobs)
+int adjoint_tc(cgb_op *op, int mode, const float *yin, const float *axa, const float *axb, float ca, float cb,
+               const float *yobs, const float *sqw, double *xout, double *partials, cudaStream_t st, int *grid);
+int forward_tc(cgb_op *op, const double *x, float *y, float *ax, const float *yobs, const float *sqw,
+               double *partials, cudaStream_t st, int *grid);
 // float-float packed kernels over the voxel range [v0, v1) (host-buffer pipeline); A' pass 1
 // only (the fibre pass follows once all ranges are done)
 int fibre_sum(cgb_op *op, double *xout, cudaStream_t st);
@@ -223,6 +269,18 @@ struct VoxelRange {
     }
 };
 int convert_f32_to_f64(const float *in, double *out, int64_t n, cudaStream_t st);
+
+// Float-float range guard of the forward input: enqueues max|x| into op->d_xmax; while an
+// XScale lives, the FP64-path voxel kernels scale x by the exact power of two that keeps
+// their FP32 words in range (no scaling, bitwise unchanged results, for ordinary ranges).
+int measure_input(cgb_op *op, const double *x, int64_t n, cudaStream_t st);
+struct XScale {
+    cgb_op *op;
+    explicit XScale(cgb_op *o, bool on = true) : op(o) { op->xmax_on = on ? 1 : 0; }
+    ~XScale() { op->xmax_on = 0; }
+};
+// exponents of the LUT bounds used by the range guard, from the device LUTs and lengths
+int update_lut_exponents(cgb_op *op);
 
 // ------------------------------------------------------------------ occupancy autotuning
 // A tuned kernel has two builds with different __launch_bounds__ min-blocks (register caps:

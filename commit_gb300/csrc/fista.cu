@@ -658,6 +658,7 @@ struct Solver {
         double curr_obj = 0, reg_term_x = 0, abs_obj = 0, rel_obj = 0, abs_x = 0, rel_x = 0;
         int crit = 4;
         while (true) {
+            NvtxRange nvi("fista iteration");
             auto eval_x = [&](double s) -> int {
                 CGB_TRY(prox(x, ws.xhat, ws.grad, s, s));
                 CGB_TRY(stats(x, ws.xhat, ws.grad, ws.prev));
@@ -1384,6 +1385,7 @@ int cgb_fista_run(cgb_op *op, const double *y, const double *sqrt_w, const cgb_r
         return fail(CGB_ERR_INVALID, "group regulariser needs a level schedule");
     if (params->graph && (params->momentum_reuse || (params->trace && params->x_ref) || params->verbose == 4))
         return fail(CGB_ERR_UNSUPPORTED, "graph mode runs without momentum reuse, trace or verbose output");
+    NvtxRange nv("cgb_fista_run");
     DevGuard g(op->device);
     Solver S;
     S.op = op;
@@ -1401,6 +1403,7 @@ int cgb_fista_batch_run(cgb_op *op, const double *y, const double *sqrt_w, const
     if (!op || !y || !regs || !params || !x || !results) return fail(CGB_ERR_INVALID, "null argument");
     if (nprob < 1) return fail(CGB_ERR_INVALID, "nprob must be >= 1");
     if (params->arith != CGB_ARITH_BF16) return fail(CGB_ERR_UNSUPPORTED, "batched FISTA runs in BF16-LUT arithmetic");
+    NvtxRange nv("cgb_fista_batch_run");
     for (int p = 0; p < nprob; ++p) {
         const cgb_reg *reg = regs + p;
         if (!x[p]) return fail(CGB_ERR_INVALID, "null x");

@@ -182,6 +182,8 @@ cgb::OpDev cgb_op::dev() const {
     d.eval = eval; d.fib_ptr = fib_ptr; d.fib_perm = fib_perm;
     d.ec_ptr = ec_ptr; d.ec_col = ec_col; d.ec_o = ec_o;
     d.iso_ptr = iso_ptr; d.iso_col = iso_col;
+    d.xmax = xmax_on ? d_xmax : nullptr;
+    d.lut_exp_fwd = lut_exp_fwd; d.lut_exp_adj = lut_exp_adj;
     return d;
 }
 
@@ -257,7 +259,9 @@ static void free_op(cgb_op *op) {
     void *ptrs[] = {op->lutIC, op->lutEC, op->lutISO, op->lutIC_p, op->lutEC_p, op->lutISO_p, op->lutIC_r, op->lutEC_r, op->lutISO_r, op->seg_l16, op->vox_ptr,
                     op->seg_f, op->eval, op->fib_ptr, op->fib_perm, op->ec_ptr, op->ec_col, op->iso_ptr,
                     op->iso_col, op->seg_o, op->ec_o, op->seg_l, op->scratch, op->scratch32, op->partials,
-                    op->dscal, op->d_in, op->d_out, op->d_x64, op->fib_slab};
+                    op->dscal, op->d_in, op->d_out, op->d_x64, op->fib_slab, op->d_xmax,
+                    op->tc_ptr, op->tc_co, op->tc_l, op->tc_bimg, op->tc_xe, op->tc_err,
+                    op->tc_fptr, op->tc_fperm, op->tc_abimg, op->tc_terms, op->tc_ax};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (op->h_scal) cudaFreeHost(op->h_scal);
@@ -448,7 +452,9 @@ static int create_impl(int device, int nS, int ndirs, int nF, int64_t n, int nE,
     CGB_TRY(dalloc(op, &op->scratch, (size_t)n * (nIC > 0 ? nIC : 1)));
     CGB_TRY(dalloc(op, &op->partials, (size_t)partial_blocks(op) * kRedSlots));
     CGB_TRY(dalloc(op, &op->dscal, 64));
+    CGB_TRY(dalloc(op, &op->d_xmax, 1));
     CGB_CUDA(cudaMallocHost((void **)&op->h_scal, 64 * sizeof(double)));
+    if (!nolut) CGB_TRY(update_lut_exponents(op));
     CGB_CUDA(cudaDeviceSynchronize());
     CGB_CUDA(cudaGetLastError());
     return CGB_OK;
@@ -470,9 +476,11 @@ int cgb_op_create(int device, int nS, int ndirs, int nF, int64_t n, int nE, int 
     int ndev = 0;
     CGB_CUDA(cudaGetDeviceCount(&ndev));
     if (device < 0 || device >= ndev) return fail(CGB_ERR_INVALID, "no such CUDA device");
+    NvtxRange nv("cgb_op_create (device re-layout)");
     DeviceGuard g(device);
     cgb_op *op = new cgb_op();
     memset((void *)op, 0, sizeof(cgb_op));
+    op->tc_mode = 1;  // tensor-core forward off until asked for (cgb_op_tensor_cores)
     int rc = create_impl(device, nS, ndirs, nF, n, nE, nV, nISOv, ICf, ICeval, ICv, ICo, ICl, ECv, ECo, ISOv, lutIC,
                          lutEC, lutISO, nIC, nEC, nISO, nolut, arith, op);
     if (rc != CGB_OK) {
@@ -525,7 +533,7 @@ int cgb_op_set_lut(cgb_op *op, const float *lutIC, const float *lutEC, const flo
                               cudaMemcpyDefault));
     }
     op->lut_r_kind = 0;  // reduced-precision copies are rebuilt on their next use
-    return CGB_OK;
+    return update_lut_exponents(op);
 }
 
 int cgb_op_ff_shape(cgb_op *op, int set, int *fwd, int *adj) {

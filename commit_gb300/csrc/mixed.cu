@@ -244,6 +244,7 @@ int ensure_reduced(cgb_op *op, int arith) {
 
 static int fwd_mix(cgb_op *op, int arith, const double *x, float *y, float *ax, const float *yobs, const float *sqw,
                    double *partials, cudaStream_t st, int *grid) {
+    if (arith == CGB_ARITH_BF16 && tc_forward_enabled(op)) return forward_tc(op, x, y, ax, yobs, sqw, partials, st, grid);
     if (arith == CGB_ARITH_BF16) return forward_mix_bf16(op, x, y, ax, yobs, sqw, partials, st, grid);
     if (arith == CGB_ARITH_FP16) return forward_mix_fp16(op, x, y, ax, yobs, sqw, partials, st, grid);
     return forward_mix_f32(op, x, y, ax, yobs, sqw, partials, st, grid);
@@ -301,6 +302,18 @@ int launch_gradient_mix(cgb_op *op, const double *x, const float *y, const float
         if (op->ncols > 0) CGB_CUDA(cudaMemsetAsync(grad, 0, op->ncols * sizeof(double), st));
         return CGB_OK;
     }
+    if (arith == CGB_ARITH_BF16 && tc_forward_enabled(op)) {
+        // tensor cores: A x into a row buffer first when it is not given, then A' of the residual
+        if (!ax_a) {
+            if (!op->tc_ax) {
+                CGB_CUDA(cudaMalloc((void **)&op->tc_ax, (size_t)op->nrows * sizeof(float)));
+                op->bytes += (size_t)op->nrows * sizeof(float);
+            }
+            CGB_TRY(forward_tc(op, x, nullptr, op->tc_ax, nullptr, nullptr, nullptr, st, nullptr));
+            return adjoint_tc(op, 2, nullptr, op->tc_ax, nullptr, 1.f, 0.f, y, sqw, grad, partials, st, grid);
+        }
+        return adjoint_tc(op, 2, nullptr, ax_a, ax_b, ca, cb, y, sqw, grad, partials, st, grid);
+    }
     return adj_mix_slabs(op, arith, nullptr, ax_a ? 2 : 1, x, y, sqw, ax_a, ax_b, ca, cb, grad, partials, st, grid);
 }
 
@@ -310,6 +323,8 @@ int launch_adjoint_mix(cgb_op *op, const float *yin, double *xout, cudaStream_t 
         if (op->ncols > 0) CGB_CUDA(cudaMemsetAsync(xout, 0, op->ncols * sizeof(double), st));
         return CGB_OK;
     }
+    if (arith == CGB_ARITH_BF16 && tc_forward_enabled(op))
+        return adjoint_tc(op, 0, yin, nullptr, nullptr, 0.f, 0.f, nullptr, nullptr, xout, nullptr, st, nullptr);
 return adj_mix_slabs(op, arith, yin, 0, nullptr, nullptr, nullptr, nullptr, nullptr, 0.f, 0.f, xout, nullptr, st,
                          nullptr);
 }

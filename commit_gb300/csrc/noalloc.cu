@@ -12,7 +12,17 @@
 // The kernels are variants of the operator's A' (operator_kernels.cuh) that read the
 // reference's own array layout (segments, EC and ISO elements sorted by voxel, as
 // load_dictionary leaves them) and find each voxel's range by binary search, so no
-// re-laid-out copy of the dictionary is needed.
+// re-laid-out copy of the dictionary is needed.  Like the operator's float-float A', each
+// voxel row of y outside FP32's comfortable exponent range is scaled by an exact power of
+// two (ff_exp_hi), using the LUT's largest magnitude measured on every call.
+//
+// Module loading.  Under CUDA's lazy module loading (the default since CUDA 12.2) the
+// static array is allocated, and a kernel's code loaded, when the module or kernel is
+// first used -- which would make the first call, and the first call for each kernel
+// shape, allocate device memory.  The first call on a device therefore does all of that
+// at once: it looks up the array's address and loads every kernel of this file
+// (cudaFuncGetAttributes).  Later calls load and allocate nothing.  A call whose sizes are
+// all zero (y may be any non-null pointer) does only this set-up.
 #include <mutex>
 
 #include "operator_launch.cuh"
@@ -44,8 +54,28 @@ __device__ __forceinline__ int64_t lower_bound_dev(const uint32_t *a, int64_t n,
     return lo;
 }
 
+// largest finite |LUT| of the three compartments, as float bits, into *out (zeroed)
+__global__ void k_lut_absmax(const NoAllocArgs A, unsigned *__restrict__ out) {
+    const float *L[3] = {A.lutIC, A.lutEC, A.lutISO};
+    const int64_t n[3] = {(int64_t)A.nIC * A.ndirs * A.nS, (int64_t)A.nEC * A.ndirs * A.nS, (int64_t)A.nISO * A.nS};
+    unsigned m = 0;
+    for (int c = 0; c < 3; ++c)
+        for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; L[c] && i < n[c];
+             i += (int64_t)gridDim.x * blockDim.x) {
+            const unsigned b = __float_as_uint(L[c][i]) & 0x7fffffffu;
+            if (b < 0x7f800000u && b > m) m = b;
+        }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        const unsigned t = __shfl_xor_sync(0xffffffffu, m, o);
+        m = t > m ? t : m;
+    }
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
 template <int LPV, int NCH>
-__global__ void __launch_bounds__(kBlock) k_adjoint_noalloc(const NoAllocArgs A, double *__restrict__ terms) {
+__global__ void __launch_bounds__(kBlock) k_adjoint_noalloc(const NoAllocArgs A, double *__restrict__ terms,
+                                                            const unsigned *__restrict__ lutmax) {
     using AR = ArFF;
     constexpr int B = LPV < 8 ? LPV : 8;
     constexpr int SPAN = LPV / B;
@@ -57,12 +87,27 @@ __global__ void __launch_bounds__(kBlock) k_adjoint_noalloc(const NoAllocArgs A,
     const bool writer = (G.sub % SPAN) == 0;
     const int64_t ec_base = (int64_t)A.nF * A.nIC;
     const int64_t iso_base = ec_base + (int64_t)A.nE * A.nEC;
+    // exponent of the LUT's largest magnitude (0 when it was not measured)
+    const unsigned lb = lutmax ? *lutmax : 0u;
+    const int lut_exp = lb ? (int)((lb >> 23) & 0xffu) - 127 : 0;
     for (int v = blockIdx.x * gpb + (int)threadIdx.x / LPV; v < A.nV; v += ngroups) {
         typename AR::Coef z[NCH];
+        unsigned zmax = 0;
 #pragma unroll
         for (int k = 0; k < NCH; ++k) {
             const int s = G.sub + k * LPV;
-            z[k] = AR::coef(s < nS ? A.y[(size_t)v * nS + s] : 0.0);
+            const double yv = s < nS ? A.y[(size_t)v * nS + s] : 0.0;
+            const unsigned h = abs_hi(yv);
+            zmax = h > zmax ? h : zmax;
+            z[k] = AR::coef(yv);
+        }
+        const int ez = ff_exp_hi(group_max_u<LPV>(zmax, G.mask), lut_exp);
+        if (ez) {
+#pragma unroll
+            for (int k = 0; k < NCH; ++k) {
+                const int s = G.sub + k * LPV;
+                z[k] = AR::coef((s < nS ? A.y[(size_t)v * nS + s] : 0.0) * pow2(-ez));
+            }
         }
         if (A.nIC > 0) {
             const int64_t beg = lower_bound_dev(A.ICv, A.n, (uint32_t)v);
@@ -82,7 +127,9 @@ __global__ void __launch_bounds__(kBlock) k_adjoint_noalloc(const NoAllocArgs A,
                         auto rowf = [&](int q) { return __shfl_sync(G.mask, row, t0 + q, LPV); };
                         const AR::Acc tot = batch_dots<LPV, NCH, AR>(G, A.lutIC, rowf, cnt, nS, z);
                         const float lq = __shfl_sync(G.mask, l, t0 + q_me, LPV);
-                        if (writer && q_me < cnt) terms[(size_t)i * A.n + b + t0 + q_me] = (double)lq * AR::val(tot);
+                        double tv = AR::val(tot);
+                        if (ez) tv *= pow2(ez);
+                        if (writer && q_me < cnt) terms[(size_t)i * A.n + b + t0 + q_me] = (double)lq * tv;
                     }
                 }
             }
@@ -104,8 +151,9 @@ __global__ void __launch_bounds__(kBlock) k_adjoint_noalloc(const NoAllocArgs A,
                         auto rowf = [&](int q) { return __shfl_sync(G.mask, row, t0 + q, LPV); };
                         const AR::Acc tot = batch_dots<LPV, NCH, AR>(G, A.lutEC, rowf, cnt, nS, z);
                         const int okq = __shfl_sync(G.mask, (int)o_ok, t0 + q_me, LPV);
-                        if (writer && q_me < cnt)
-                            A.x[ec_base + (size_t)i * A.nE + b + t0 + q_me] = okq ? AR::val(tot) : 0.0;
+                        double tv = AR::val(tot);
+                        if (ez) tv *= pow2(ez);
+                        if (writer && q_me < cnt) A.x[ec_base + (size_t)i * A.nE + b + t0 + q_me] = okq ? tv : 0.0;
                     }
                 }
             }
@@ -119,7 +167,8 @@ __global__ void __launch_bounds__(kBlock) k_adjoint_noalloc(const NoAllocArgs A,
                     auto rowf = [&](int q) { return (uint32_t)((t0 + q) * nS); };
                     const AR::Acc tot = batch_dots<LPV, NCH, AR>(G, A.lutISO, rowf, cnt, nS, z);
                     if (writer && q_me < cnt) {
-                        const double d = AR::val(tot);
+                        double d = AR::val(tot);
+                        if (ez) d *= pow2(ez);
                         for (int64_t e = beg; e < end; ++e) A.x[iso_base + (size_t)(t0 + q_me) * A.nISOv + e] = d;
                     }
                 }
@@ -149,6 +198,7 @@ __global__ void k_fibre_sum_noalloc(const NoAllocArgs A, const double *__restric
 struct NoAllocLaunch {
     NoAllocArgs args;
     double *terms;
+    const unsigned *lutmax;
     int nsm;
     cudaStream_t st;
     template <int L, int N>
@@ -156,13 +206,26 @@ struct NoAllocLaunch {
         auto kern = k_adjoint_noalloc<L, N>;
         int g = 0;
         CGB_TRY(grid_for_kernel(kern, 0, nsm, args.nV, kBlock / L, &g));
-        kern<<<g, kBlock, 0, st>>>(args, terms);
+        kern<<<g, kBlock, 0, st>>>(args, terms, lutmax);
         CGB_CUDA(cudaGetLastError());
         return CGB_OK;
     }
 };
 
-// Per-device address of the static scratch, looked up once with that device current.
+// loads the code of one kernel shape (cudaFuncGetAttributes), so no later call does
+struct NoAllocLoad {
+    template <int L, int N>
+    int run() {
+        cudaFuncAttributes a;
+        CGB_CUDA(cudaFuncGetAttributes(&a, k_adjoint_noalloc<L, N>));
+        return CGB_OK;
+    }
+};
+
+// Per-device set-up, done once with that device current: the static scratch's device
+// address and the loading of every kernel of this file.  The cached address is that of
+// the module loaded in the device's primary context: cudaDeviceReset invalidates it, so a
+// process that resets a device must not call this entry point on it afterwards.
 std::mutex g_noalloc_mutex;
 double *g_noalloc_addr[64] = {nullptr};
 
@@ -172,6 +235,11 @@ int noalloc_terms(int dev, double **out) {
     if (!g_noalloc_addr[dev]) {
         void *p = nullptr;
         CGB_CUDA(cudaGetSymbolAddress(&p, g_noalloc_terms));
+        NoAllocLoad ld;
+        for (const Shape &s : kShapes) CGB_TRY(dispatch_shape(s, ld));
+        cudaFuncAttributes a;
+        CGB_CUDA(cudaFuncGetAttributes(&a, k_fibre_sum_noalloc));
+        CGB_CUDA(cudaFuncGetAttributes(&a, k_lut_absmax));
         g_noalloc_addr[dev] = (double *)p;
     }
     *out = g_noalloc_addr[dev];
@@ -201,7 +269,8 @@ extern "C" int cgb_op_adjoint_noalloc(int nS, int ndirs, int nF, int64_t n, int 
                                              " exceeds its static scratch of " + std::to_string(kNoAllocMaxTerms) +
                                              " terms; use cgb_op_create/cgb_op_apply");
     const int64_t ncols = (int64_t)nF * nIC + (int64_t)nE * nEC + (int64_t)nISOv * nISO;
-    if (!y || (ncols > 0 && !x) || (n > 0 && nIC > 0 && (!ICf || !ICv || !ICo || !ICl || !fib_perm)) ||
+    // ICf is not read: the fibre index (fib_ptr, fib_perm) replaces it
+    if (!y || (ncols > 0 && !x) || (n > 0 && nIC > 0 && (!ICv || !ICo || !ICl || !fib_perm)) ||
         (nIC > 0 && (!ICeval || !fib_ptr || !lutIC)) || (nE > 0 && nEC > 0 && (!ECv || !ECo || !lutEC)) ||
         (nISOv > 0 && nISO > 0 && (!ISOv || !lutISO)))
         return fail(CGB_ERR_INVALID, "null array");
@@ -215,15 +284,22 @@ extern "C" int cgb_op_adjoint_noalloc(int nS, int ndirs, int nF, int64_t n, int 
     // the terms of segments outside every voxel and the columns of elements outside every
     // voxel are never written by the passes below: start both from zero
     if (ncols > 0) CGB_CUDA(cudaMemsetAsync(x, 0, ncols * sizeof(double), st));
-    if (n > 0 && nIC > 0) CGB_CUDA(cudaMemsetAsync(terms, 0, n * nIC * sizeof(double), st));
+    // the LUT's largest magnitude goes to the slot after the terms (when there is one)
+    const int64_t nterms = n * (nIC > 0 ? nIC : 0);
+    unsigned *lutmax = nterms < kNoAllocMaxTerms ? reinterpret_cast<unsigned *>(terms + nterms) : nullptr;
     if (nV == 0 || ncols == 0) return CGB_OK;
+    CGB_CUDA(cudaMemsetAsync(terms, 0, (nterms + (lutmax ? 1 : 0)) * sizeof(double), st));
     NoAllocArgs a;
     a.nS = nS; a.ndirs = ndirs; a.nF = nF; a.nE = nE; a.nV = nV; a.nISOv = nISOv;
     a.nIC = nIC; a.nEC = nE > 0 ? nEC : 0; a.nISO = nISOv > 0 ? nISO : 0; a.n = n;
     a.y = y; a.x = x; a.ICf = ICf; a.ICeval = ICeval; a.ICv = ICv; a.ECv = ECv; a.ISOv = ISOv;
     a.fib_ptr = fib_ptr; a.fib_perm = fib_perm; a.ICo = ICo; a.ECo = ECo; a.ICl = ICl;
     a.lutIC = lutIC; a.lutEC = lutEC; a.lutISO = lutISO;
-    NoAllocLaunch L{a, terms, nsm, st};
+    if (lutmax) {
+        k_lut_absmax<<<nsm, 256, 0, st>>>(a, lutmax);
+        CGB_CUDA(cudaGetLastError());
+    }
+    NoAllocLaunch L{a, terms, lutmax, nsm, st};
     CGB_TRY(dispatch_shape(pick_shape(nS), L));
     if (nIC > 0 && nF > 0) {
         const int64_t total = (int64_t)nF * nIC;

@@ -2,6 +2,9 @@
 // LUT-free kernels (setup_operator.py:713-915) and the per-fibre second pass of A'.
 #include "operator_kernels.cuh"
 
+#include <math.h>
+#include <string.h>
+
 namespace cgb {
 
 int forward_f64(cgb_op *op, const double *x, double *y, double *ax, const double *yobs, const double *sqw,
@@ -124,9 +127,77 @@ __global__ void k_fibre_sum_slab(const OpDev P, const double *__restrict__ scrat
     }
 }
 
+// largest finite magnitude (as bits: non-negative floats order like their bit patterns)
+__global__ void k_absmax_f64(const double *__restrict__ a, int64_t n, unsigned long long *__restrict__ out) {
+    unsigned long long m = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned long long b = (unsigned long long)__double_as_longlong(a[i]) & 0x7fffffffffffffffull;
+        if (b < 0x7ff0000000000000ull && b > m) m = b;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        const unsigned long long t = __shfl_xor_sync(0xffffffffu, m, o);
+        m = t > m ? t : m;
+    }
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
+__global__ void k_absmax_f32(const float *__restrict__ a, int64_t n, unsigned *__restrict__ out) {
+    unsigned m = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned b = __float_as_uint(a[i]) & 0x7fffffffu;
+        if (b < 0x7f800000u && b > m) m = b;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        const unsigned t = __shfl_xor_sync(0xffffffffu, m, o);
+        m = t > m ? t : m;
+    }
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
 }  // namespace detail
 
 using namespace detail;
+
+int measure_input(cgb_op *op, const double *x, int64_t n, cudaStream_t st) {
+    CGB_CUDA(cudaMemsetAsync(op->d_xmax, 0, sizeof(unsigned long long), st));
+    if (n <= 0) return CGB_OK;
+    int g = (int)((n + 255) / 256);
+    if (g > op->nsm * 8) g = op->nsm * 8;
+    k_absmax_f64<<<g, 256, 0, st>>>(x, n, op->d_xmax);
+    CGB_CUDA(cudaGetLastError());
+    return CGB_OK;
+}
+
+int update_lut_exponents(cgb_op *op) {
+    // [0] max |LUT| over IC, EC and ISO, [1] max |IC length| (bits of non-negative floats)
+    unsigned *m = reinterpret_cast<unsigned *>(op->d_xmax);
+    CGB_CUDA(cudaMemset(m, 0, 2 * sizeof(unsigned)));
+    const struct {
+        const float *p;
+        int64_t n;
+        int slot;
+    } parts[4] = {{op->lutIC, (int64_t)op->nIC * op->ndirs * op->nS, 0},
+                  {op->lutEC, (int64_t)op->nEC * op->ndirs * op->nS, 0},
+                  {op->lutISO, (int64_t)op->nISO * op->nS, 0},
+                  {op->seg_l, op->nIC > 0 ? op->n : 0, 1}};
+    for (const auto &q : parts) {
+        if (!q.p || q.n <= 0) continue;
+        int g = (int)((q.n + 255) / 256);
+        if (g > op->nsm * 8) g = op->nsm * 8;
+        k_absmax_f32<<<g, 256>>>(q.p, q.n, m + q.slot);
+        CGB_CUDA(cudaGetLastError());
+    }
+    unsigned h[2] = {0, 0};
+    CGB_CUDA(cudaMemcpy(h, m, sizeof(h), cudaMemcpyDeviceToHost));
+    float lut, len;
+    memcpy(&lut, &h[0], 4);
+    memcpy(&len, &h[1], 4);
+    op->lut_exp_adj = lut > 0.f ? ilogbf(lut) : 0;
+    op->lut_exp_fwd = op->lut_exp_adj + (len > 1.f ? ilogbf(len) : 0);
+    return CGB_OK;
+}
 
 int fibre_sum_slab(cgb_op *op, double *xout, int s, cudaStream_t st) {
     if (op->nIC > 0 && op->nF > 0) {
@@ -165,6 +236,8 @@ static int run_forward(cgb_op *op, const double *x, double *y, double *ax, const
         if (grid_out) *grid_out = g;
         return CGB_OK;
     }
+    CGB_TRY(measure_input(op, x, op->ncols, st));
+    XScale guard(op);
     if (arith == CGB_ARITH_F64) return forward_f64(op, x, y, ax, yobs, sqw, partials, st, grid_out);
     if (op->ff_variant == 0) return forward_ffs(op, x, y, ax, yobs, sqw, partials, st, grid_out);
     return forward_ff(op, x, y, ax, yobs, sqw, partials, st, grid_out);
@@ -178,6 +251,10 @@ static int run_adjoint(cgb_op *op, const double *yin, int in_mode, const double 
         if (op->ncols > 0) CGB_CUDA(cudaMemsetAsync(xout, 0, op->ncols * sizeof(double), st));
         return CGB_OK;
     }
+    // the fused gradient pass recomputes A x: measure x for the range guard
+    const bool mx = in_mode == 1 && !op->nolut;
+    if (mx) CGB_TRY(measure_input(op, x, op->ncols, st));
+    XScale guard(op, mx);
     if (op->nolut) {
         const OpDev P = op->dev();
         int g = (op->nV + kBlock - 1) / kBlock;

@@ -121,11 +121,53 @@ __device__ __forceinline__ void block_sum_store(double v, double *dst) {
     }
 }
 
+// ------------------------------------------------------------------ float-float range guard
+// The float-float words are FP32: products and sums keep their ~48-bit significand only
+// while they stay well inside FP32's exponent range, and FP64 operands can lie far outside
+// it (the reference accumulates in FP64, setup_operator.py:92-96).  An operand is therefore
+// scaled by an exact power of two 2^-e when the bound on its products with the LUT,
+// 2^(exponent of its largest magnitude + lut_exp), leaves [2^-kFFRange, 2^kFFRange], and
+// the results are scaled back by 2^e in FP64.  Inside that range e = 0: nothing is scaled
+// and results are bitwise those of the unguarded kernels.  `hi` is the high word of the
+// largest magnitude (exponent in bits 20..30); zero, infinities and NaN give e = 0.
+constexpr int kFFRange = 60;
+__device__ __forceinline__ int ff_exp_hi(unsigned hi, int lut_exp) {
+    const int be = (int)(hi >> 20) & 0x7ff;
+    if (hi == 0 || be == 0x7ff) return 0;
+    const int e = (be == 0 ? -1022 : be - 1023) + lut_exp;
+    if (e >= -kFFRange && e <= kFFRange) return 0;
+    return e < -1000 ? -1000 : (e > 1000 ? 1000 : e);
+}
+
+// 2^e as a double for |e| <= 1000 (exponent field only)
+__device__ __forceinline__ double pow2(int e) { return __hiloint2double((e + 1023) << 20, 0); }
+
+// scaling exponent of the forward input x of this launch (0 when not measured)
+__device__ __forceinline__ int ff_exp_x(const OpDev &P) {
+    return P.xmax ? ff_exp_hi((unsigned)(*P.xmax >> 32), P.lut_exp_fwd) : 0;
+}
+
+// high word of |v| for finite v, 0 for infinities and NaN (they propagate unscaled)
+__device__ __forceinline__ unsigned abs_hi(double v) {
+    const unsigned h = (unsigned)__double2hiint(v) & 0x7fffffffu;
+    return h < 0x7ff00000u ? h : 0u;
+}
+
+template <int LPV>
+__device__ __forceinline__ unsigned group_max_u(unsigned m, unsigned mask) {
+#pragma unroll
+    for (int d = LPV / 2; d >= 1; d >>= 1) {
+        const unsigned t = __shfl_xor_sync(mask, m, d, LPV);
+        m = t > m ? t : m;
+    }
+    return m;
+}
+
 // ------------------------------------------------------------------ forward accumulation
 // Accumulates row v of A*x into acc[NCH] (lane owns samples sub + k*LPV).
 template <int LPV, int NCH, class AR>
 __device__ __forceinline__ void forward_row(const OpDev &P, const Group<LPV> &G, int v, const double *__restrict__ x,
-                                            typename AR::Acc (&acc)[NCH]) {
+                                            typename AR::Acc (&acc)[NCH], int ex) {
     const int nS = P.nS;
 #pragma unroll
     for (int k = 0; k < NCH; ++k) AR::zero(acc[k]);
@@ -147,7 +189,9 @@ __device__ __forceinline__ void forward_row(const OpDev &P, const Group<LPV> &G,
                 double c = 0.0;
                 if (valid) {
                     const size_t col = (size_t)i * P.nF + f;
-                    c = (double)l * (x[col] * (double)P.eval[col]);
+                    double xv = x[col];
+                    if (ex) xv = xv * pow2(-ex);
+                    c = (double)l * (xv * (double)P.eval[col]);
                 }
                 const typename AR::Coef cf = AR::coef(c);
                 const uint32_t row = ((uint32_t)i * P.ndirs + o) * (uint32_t)nS;
@@ -179,7 +223,8 @@ __device__ __forceinline__ void forward_row(const OpDev &P, const Group<LPV> &G,
             }
             const int cnt = min((int)(end - b), LPV);
             for (int i = 0; i < P.nEC; ++i) {
-                const double c = valid ? x[P.ec_base + (size_t)i * P.nE + col] : 0.0;
+                double c = valid ? x[P.ec_base + (size_t)i * P.nE + col] : 0.0;
+                if (ex) c = c * pow2(-ex);
                 const typename AR::Coef cf = AR::coef(c);
                 const uint32_t row = ((uint32_t)i * P.ndirs + o) * (uint32_t)nS;
                 for (int t = 0; t < cnt; ++t) {
@@ -206,7 +251,8 @@ __device__ __forceinline__ void forward_row(const OpDev &P, const Group<LPV> &G,
             const uint32_t col = valid ? P.iso_col[j] : 0;
             const int cnt = min((int)(end - b), LPV);
             for (int i = 0; i < P.nISO; ++i) {
-                const double c = valid ? x[P.iso_base + (size_t)i * P.nISOv + col] : 0.0;
+                double c = valid ? x[P.iso_base + (size_t)i * P.nISOv + col] : 0.0;
+                if (ex) c = c * pow2(-ex);
                 const typename AR::Coef cf = AR::coef(c);
                 for (int t = 0; t < cnt; ++t) {
                     const typename AR::Coef ct = AR::shfl(G.mask, cf, t, LPV);
@@ -234,15 +280,17 @@ __global__ void __launch_bounds__(kBlock) k_forward(const OpDev P, const double 
     const int gpb = kBlock / LPV;
     const int ngroups = gridDim.x * gpb;
     double nrm = 0.0;
+    const int ex = ff_exp_x(P);
     for (int v = blockIdx.x * gpb + (int)threadIdx.x / LPV; v < P.nV; v += ngroups) {
         typename AR::Acc acc[NCH];
-        forward_row<LPV, NCH, AR>(P, G, v, x, acc);
+        forward_row<LPV, NCH, AR>(P, G, v, x, acc, ex);
 #pragma unroll
         for (int k = 0; k < NCH; ++k) {
             const int s = G.sub + k * LPV;
             if (s < P.nS) {
                 const size_t idx = (size_t)v * P.nS + s;
-                const double a = AR::val(acc[k]);
+                double a = AR::val(acc[k]);
+                if (ex) a = a * pow2(ex);
                 if (yout) yout[idx] = a;
                 if (axout) axout[idx] = a;
                 if (partials) {
@@ -315,42 +363,44 @@ __global__ void __launch_bounds__(kBlock) k_adjoint(const OpDev P, const double 
     const int q_me = G.sub / SPAN;
     const bool writer = (G.sub % SPAN) == 0;
     double nrm = 0.0;
+    const int ex = in_mode == 1 ? ff_exp_x(P) : 0;
     for (int v = blockIdx.x * gpb + (int)threadIdx.x / LPV; v < P.nV; v += ngroups) {
         typename AR::Coef z[NCH];
-        if (in_mode == 0) {
+        double a[NCH];
+        if (in_mode == 1) {
+            typename AR::Acc acc[NCH];
+            forward_row<LPV, NCH, AR>(P, G, v, x, acc, ex);
 #pragma unroll
             for (int k = 0; k < NCH; ++k) {
-                const int s = G.sub + k * LPV;
-                z[k] = AR::coef(s < nS ? yin[(size_t)v * nS + s] : 0.0);
+                a[k] = AR::val(acc[k]);
+                if (ex) a[k] = a[k] * pow2(ex);
             }
-        } else {
-            double a[NCH];
-            if (in_mode == 1) {
-                typename AR::Acc acc[NCH];
-                forward_row<LPV, NCH, AR>(P, G, v, x, acc);
+        }
+        // input row z (y, or the weighted residual); `first` adds the residual norm
+        auto zval = [&](int k, bool first) -> double {
+            const int s = G.sub + k * LPV;
+            if (s >= nS) return 0.0;
+            const size_t idx = (size_t)v * nS + s;
+            if (in_mode == 0) return yin[idx];
+            const double av = in_mode == 1 ? a[k] : ca * ax_a[idx] + cb * ax_b[idx];
+            double r = av - yobs[idx];
+            if (sqw) r *= sqw[idx];
+            if (first) nrm = fma(r, r, nrm);
+            return sqw ? sqw[idx] * r : r;
+        };
+        unsigned zmax = 0;
 #pragma unroll
-                for (int k = 0; k < NCH; ++k) a[k] = AR::val(acc[k]);
-            } else {
+        for (int k = 0; k < NCH; ++k) {
+            const double zz = zval(k, true);
+            const unsigned h = abs_hi(zz);
+            zmax = h > zmax ? h : zmax;
+            z[k] = AR::coef(zz);
+        }
+        // range guard: a row outside float-float's range is split again, scaled (exact)
+        const int ez = ff_exp_hi(group_max_u<LPV>(zmax, G.mask), P.lut_exp_adj);
+        if (ez) {
 #pragma unroll
-                for (int k = 0; k < NCH; ++k) {
-                    const int s = G.sub + k * LPV;
-                    const size_t idx = (size_t)v * nS + s;
-                    a[k] = s < nS ? ca * ax_a[idx] + cb * ax_b[idx] : 0.0;
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < NCH; ++k) {
-                const int s = G.sub + k * LPV;
-                double zz = 0.0;
-                if (s < nS) {
-                    const size_t idx = (size_t)v * nS + s;
-                    double r = a[k] - yobs[idx];
-                    if (sqw) r *= sqw[idx];
-                    nrm = fma(r, r, nrm);
-                    zz = sqw ? sqw[idx] * r : r;
-                }
-                z[k] = AR::coef(zz);
-            }
+            for (int k = 0; k < NCH; ++k) z[k] = AR::coef(zval(k, false) * pow2(-ez));
         }
         // IC segments -> per-segment terms l * <LUT, z> in voxel order
         if (P.nIC > 0) {
@@ -368,7 +418,9 @@ __global__ void __launch_bounds__(kBlock) k_adjoint(const OpDev P, const double 
                         auto rowf = [&](int q) { return __shfl_sync(G.mask, row, t0 + q, LPV); };
                         const typename AR::Acc tot = batch_dots<LPV, NCH, AR>(G, P.lutIC, rowf, cnt, nS, z);
                         const float lq = __shfl_sync(G.mask, l, t0 + q_me, LPV);
-                        if (writer && q_me < cnt) scratch[(size_t)i * P.n + b + t0 + q_me] = (double)lq * AR::val(tot);
+                        double tv = AR::val(tot);
+                        if (ez) tv = tv * pow2(ez);
+                        if (writer && q_me < cnt) scratch[(size_t)i * P.n + b + t0 + q_me] = (double)lq * tv;
                     }
                 }
             }
@@ -388,7 +440,9 @@ __global__ void __launch_bounds__(kBlock) k_adjoint(const OpDev P, const double 
                         auto rowf = [&](int q) { return __shfl_sync(G.mask, row, t0 + q, LPV); };
                         const typename AR::Acc tot = batch_dots<LPV, NCH, AR>(G, P.lutEC, rowf, cnt, nS, z);
                         const uint32_t cq = __shfl_sync(G.mask, col, t0 + q_me, LPV);
-                        if (writer && q_me < cnt) xout[P.ec_base + (size_t)i * P.nE + cq] = AR::val(tot);
+                        double tv = AR::val(tot);
+                        if (ez) tv = tv * pow2(ez);
+                        if (writer && q_me < cnt) xout[P.ec_base + (size_t)i * P.nE + cq] = tv;
                     }
                 }
             }
@@ -402,7 +456,8 @@ __global__ void __launch_bounds__(kBlock) k_adjoint(const OpDev P, const double 
                     auto rowf = [&](int q) { return (uint32_t)((t0 + q) * nS); };
                     const typename AR::Acc tot = batch_dots<LPV, NCH, AR>(G, P.lutISO, rowf, cnt, nS, z);
                     if (writer && q_me < cnt) {
-                        const double d = AR::val(tot);
+                        double d = AR::val(tot);
+                        if (ez) d = d * pow2(ez);
                         for (uint32_t e = beg; e < end; ++e)
                             xout[P.iso_base + (size_t)(t0 + q_me) * P.nISOv + P.iso_col[e]] = d;
                     }

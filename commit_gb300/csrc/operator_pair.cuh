@@ -181,9 +181,10 @@ __device__ __forceinline__ void run_flags(const Group<LPV> &G, bool valid, uint3
     tail = valid && (G.sub == cntL - 1 || o_next != o);
 }
 
+// ex: range-guard exponent of x (ff_exp_x; 0 reads x unscaled, else x * 2^-ex)
 template <int LPV, int NP>
 __device__ __forceinline__ void forward_row_p(const Comps &C, const Group<LPV> &G, int v,
-                                              const double *__restrict__ x, DD2 (&acc)[NP]) {
+                                              const double *__restrict__ x, DD2 (&acc)[NP], int ex) {
 #pragma unroll
     for (int k = 0; k < NP; ++k) dd2_zero(acc[k]);
     const int base = 2 * G.sub;
@@ -211,7 +212,9 @@ __device__ __forceinline__ void forward_row_p(const Comps &C, const Group<LPV> &
                 float ch = 0.f, cl = 0.f;
                 if (valid) {
                     const int64_t q = (int64_t)i * cm.xstride + col;
-                    double c = (double)l * x[cm.xbase + q];
+                    double xv = x[cm.xbase + q];
+                    if (ex) xv = xv * pow2(-ex);
+                    double c = (double)l * xv;
                     if (cm.eval) c *= (double)cm.eval[q];
                     ch = __double2float_rn(c);
                     cl = __double2float_rn(c - (double)ch);
@@ -261,16 +264,21 @@ __global__ void __launch_bounds__(kBlock, MINB) k_forward_p(const OpDev P, const
     const int nS = P.nS;
     // 16-byte row stores need an even row length and 16-byte aligned outputs
     const bool even = (nS & 1) == 0 && vec_ok;
+    const int ex = ff_exp_x(P);
     double nrm = 0.0;
     for (int v = P.v0 + blockIdx.x * gpb + (int)threadIdx.x / LPV; v < P.nV; v += ngroups) {
         DD2 acc[NP];
-        forward_row_p<LPV, NP>(C, G, v, x, acc);
+        forward_row_p<LPV, NP>(C, G, v, x, acc, ex);
 #pragma unroll
         for (int k = 0; k < NP; ++k) {
             const int s = 2 * (G.sub + k * LPV);
             if (s < nS) {
                 double a0, a1;
                 dd2_val(acc[k], a0, a1);
+                if (ex) {
+                    a0 = a0 * pow2(ex);
+                    a1 = a1 * pow2(ex);
+                }
                 const size_t idx = (size_t)v * nS + s;
                 const bool two = s + 1 < nS;
                 if (yout) {
@@ -363,38 +371,54 @@ __global__ void __launch_bounds__(kBlock, MINB) k_adjoint_p(const OpDev P, const
     const int gpb = kBlock / LPV;
     const int ngroups = gridDim.x * gpb;
     const int nS = P.nS;
+    const int ex = FUSED && in_mode == 1 ? ff_exp_x(P) : 0;
     double nrm = 0.0;
     for (int v = P.v0 + blockIdx.x * gpb + (int)threadIdx.x / LPV; v < P.nV; v += ngroups) {
         double a[2 * NP];
         if (FUSED && in_mode == 1) {
             DD2 acc[NP];
-            forward_row_p<LPV, NP>(C, G, v, x, acc);
+            forward_row_p<LPV, NP>(C, G, v, x, acc, ex);
 #pragma unroll
-            for (int k = 0; k < NP; ++k) dd2_val(acc[k], a[2 * k], a[2 * k + 1]);
-        }
-        f2 zh[NP], zl[NP];
-#pragma unroll
-        for (int k = 0; k < NP; ++k) {
-            double zz[2];
-#pragma unroll
-            for (int u = 0; u < 2; ++u) {
-                const int s = 2 * (G.sub + k * LPV) + u;
-                zz[u] = 0.0;
-                if (s < nS) {
-                    const size_t idx = (size_t)v * nS + s;
-                    if (in_mode == 0) {
-                        zz[u] = yin[idx];
-                    } else {
-                        const double av = in_mode == 1 ? a[2 * k + u] : ca * ax_a[idx] + cb * ax_b[idx];
-                        double r = av - yobs[idx];
-                        if (sqw) r *= sqw[idx];
-                        nrm = fma(r, r, nrm);
-                        zz[u] = sqw ? sqw[idx] * r : r;
-                    }
+            for (int k = 0; k < NP; ++k) {
+                dd2_val(acc[k], a[2 * k], a[2 * k + 1]);
+                if (ex) {
+                    a[2 * k] = a[2 * k] * pow2(ex);
+                    a[2 * k + 1] = a[2 * k + 1] * pow2(ex);
                 }
             }
+        }
+        // element u of this lane's pair k of the input row z (y, or the weighted residual);
+        // `first` adds the residual norm
+        auto zval = [&](int k, int u, bool first) -> double {
+            const int s = 2 * (G.sub + k * LPV) + u;
+            if (s >= nS) return 0.0;
+            const size_t idx = (size_t)v * nS + s;
+            if (in_mode == 0) return yin[idx];
+            const double av = FUSED && in_mode == 1 ? a[2 * k + u] : ca * ax_a[idx] + cb * ax_b[idx];
+            double r = av - yobs[idx];
+            if (sqw) r *= sqw[idx];
+            if (first) nrm = fma(r, r, nrm);
+            return sqw ? sqw[idx] * r : r;
+        };
+        f2 zh[NP], zl[NP];
+        unsigned zmax = 0;
+#pragma unroll
+        for (int k = 0; k < NP; ++k) {
+            const double z0 = zval(k, 0, true), z1 = zval(k, 1, true);
+            const unsigned h0 = abs_hi(z0), h1 = abs_hi(z1);
+            zmax = h0 > zmax ? h0 : zmax;
+            zmax = h1 > zmax ? h1 : zmax;
             f2 unused;
-            split2(zz[0], zz[1], zh[k], zl[k], unused);
+            split2(z0, z1, zh[k], zl[k], unused);
+        }
+        // range guard: a row outside float-float's range is split again, scaled (exact)
+        const int ez = ff_exp_hi(group_max_u<LPV>(zmax, G.mask), P.lut_exp_adj);
+        if (ez) {
+#pragma unroll
+            for (int k = 0; k < NP; ++k) {
+                f2 unused;
+                split2(zval(k, 0, false) * pow2(-ez), zval(k, 1, false) * pow2(-ez), zh[k], zl[k], unused);
+            }
         }
 #pragma unroll 1
         for (int ci = 0; ci < C.n; ++ci) {
@@ -440,7 +464,8 @@ __global__ void __launch_bounds__(kBlock, MINB) k_adjoint_p(const OpDev P, const
                         const double tot = batch_dots_p<LPV, NP>(G, cm.lut, rowf, cnt, zh, zl);
                         const int q = my_item - u0;
                         const bool mine = valid && q >= 0 && q < cnt;
-                        const double t = __shfl_sync(G.mask, tot, mine ? q * SPAN : 0, LPV);
+                        double t = __shfl_sync(G.mask, tot, mine ? q * SPAN : 0, LPV);
+                        if (ez) t = t * pow2(ez);
                         if (mine) {
                             if (cm.to_scratch) scratch[(size_t)i * P.n + j] = (double)l * t;
                             else xout[cm.xbase + (size_t)i * cm.xstride + col] = t;

@@ -1,0 +1,331 @@
+// Reduced-precision A'*y voxel pass on the tensor cores (tcgen05, BF16 operands, FP32
+// accumulation), followed by the per-fibre FP64 sums.
+//
+// The voxel pass of A' needs, for every item of voxel v, the dot product of its LUT row k
+// with the voxel's input row z (setup_operator.py:591-710 forms one per segment).  Over a
+// tile of 128 voxels these are the entries of the dense product G = Z * L^T (128 x every
+// LUT row): the kernel loads the tile's rows of z (y, or the weighted residual of the FISTA
+// gradient) once, splits them into BF16 high and low parts in shared memory (K-major, 64
+// samples per K-block), and multiplies them with the BF16 LUT rows, 256 rows per round,
+// into one half of tensor memory while the previous round's half is read back: for each
+// item of the round's rows the drain warps form l * G[v, k] and write it -- IC items to a
+// term array in entry order (the tile-ordered entry stream of tc_forward.cu), EC / ISO
+// items straight to their column of x.  The IC columns are then the sums of their terms,
+// gathered per fibre in entry order through an entry-order fibre index (deterministic,
+// FP64 sums, as the CUDA-core path).
+//
+// Warp roles (256 threads, one CTA per SM): all threads load and split Z; warp 4's first
+// lane fetches the LUT row images (bulk copies, 2 stages) and issues the MMAs; warps 0-3
+// (one per TMEM lane quarter) drain the accumulators.  Every wait is bounded (tc_ptx.cuh).
+#include <cub/cub.cuh>
+
+#include "operator_launch.cuh"
+#include "tc_ptx.cuh"
+
+namespace cgb {
+namespace detail {
+namespace {
+
+constexpr int kAThreads = 256;
+constexpr int kATile = 128;
+constexpr int kARows = 256;         // LUT rows per round (one TMEM half)
+constexpr int kANh = 128;           // LUT rows per MMA (N)
+constexpr int kAMaxKBS = 5;         // sample K-blocks of 64: nS <= 320
+constexpr int kADrainStride = 33;   // floats per drain staging row
+constexpr uint32_t kAColBits = 26;
+
+struct TcAdjArgs {
+    int nV, nS, KBS, R, NKB, kb_ec, ntiles;
+    const uint32_t *ent_ptr, *ent_co;
+    const __half *ent_l;
+    float l_scale;
+    const __nv_bfloat16 *bimg;  // [R][KBS][2][128 x 64] swizzled
+    int mode;                   // 0: z = yin; 2: r = sqw*(ca*axa + cb*axb - yobs), z = sqw*r, |r|^2 partials
+    const float *yin, *axa, *axb, *yobs, *sqw;
+    float ca, cb;
+    float *terms;
+    double *xout;
+    double *partials;
+    int *err;
+};
+
+__host__ __device__ constexpr size_t tca_smem_bytes(int KBS) {
+    return 1024 + (size_t)KBS * 2 * 16384 + 2 * 16384 + 4 * 32 * kADrainStride * 4 + 128;
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    float a[16], b[16];
+    tc::tmem_ld16(taddr, a);
+    tc::tmem_ld16(taddr + 16, b);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        v[i] = a[i];
+        v[16 + i] = b[i];
+    }
+}
+
+__global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    uint8_t *a_hi = sm;                                  // KBS x 16384
+    uint8_t *a_lo = sm + (size_t)A.KBS * 16384;          // KBS x 16384
+    uint8_t *b_img = sm + (size_t)A.KBS * 2 * 16384;     // 2 x 16384
+    float *dstage = reinterpret_cast<float *>(b_img + 2 * 16384);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(dstage + 4 * 32 * kADrainStride);
+    uint64_t *bfull = bars, *bfree = bars + 2, *gfull = bars + 4, *drained = bars + 6;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 8);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        for (int i = 0; i < 2; ++i) {
+            tc::mbar_init(&bfull[i], 1);
+            tc::mbar_init(&bfree[i], 1);
+            tc::mbar_init(&gfull[i], 1);
+            tc::mbar_init(&drained[i], 128);
+        }
+        tc::mbar_init_fence();
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(tmem_slot, 512);
+        tc::tmem_relinquish();
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t idesc = tc::idesc_bf16(kATile, kANh);
+    const int Q = A.R * A.KBS * 2;  // B items per tile
+    constexpr uint32_t kNone = 0xffffffffu;
+    // issuer state (warp 4, lane 0): items and rounds issued so far, last copy / commit per stage
+    uint32_t gq = 0, rgi = 0;
+    uint32_t last_b[2] = {kNone, kNone}, last_c[2] = {kNone, kNone};
+    // drain state (warps 0-3): rounds drained so far
+    uint32_t rgd = 0;
+    int bad = 0;
+    double nrm = 0.0;
+
+    for (int tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
+        // (1) the tile's input rows -> BF16 hi / lo, K-major swizzled, one tile per K-block
+        float vn = 0.f;
+        for (int q = tid; q < A.KBS * kATile * 8; q += kAThreads) {
+            const int kb = q >> 10, rem = q & 1023, m = rem >> 3, p = rem & 7, cl = p ^ (m & 7);
+            const int v = tile * kATile + m;
+            float z[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const int s = kb * 64 + cl * 8 + e;
+                float zz = 0.f;
+                if (v < A.nV && s < A.nS) {
+                    const size_t idx = (size_t)v * A.nS + s;
+                    if (A.mode == 0) {
+                        zz = A.yin[idx];
+                    } else {
+                        float r = A.ca * A.axa[idx] + (A.axb ? A.cb * A.axb[idx] : 0.f) - A.yobs[idx];
+                        if (A.sqw) r *= A.sqw[idx];
+                        vn = fmaf(r, r, vn);
+                        zz = A.sqw ? A.sqw[idx] * r : r;
+                    }
+                }
+                z[e] = zz;
+            }
+            uint32_t hw[4], lw[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const __nv_bfloat162 h = __floats2bfloat162_rn(z[2 * e], z[2 * e + 1]);
+                const float2 hf = __bfloat1622float2(h);
+                const __nv_bfloat162 l = __floats2bfloat162_rn(z[2 * e] - hf.x, z[2 * e + 1] - hf.y);
+                hw[e] = *reinterpret_cast<const uint32_t *>(&h);
+                lw[e] = *reinterpret_cast<const uint32_t *>(&l);
+            }
+            const uint32_t off = (uint32_t)kb * 16384u + (uint32_t)(m >> 3) * 1024u + (uint32_t)(m & 7) * 128u +
+                                 (uint32_t)p * 16u;
+            *reinterpret_cast<uint4 *>(a_hi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+            *reinterpret_cast<uint4 *>(a_lo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+        }
+        nrm += (double)vn;
+        tc::fence_async_smem();
+        __syncthreads();
+
+        if (warp == 4) {
+            // (2) issuer: LUT row images through 2 shared-memory stages, MMAs into TMEM half rg & 1
+            if (lane == 0 && !bad) {
+                auto issue = [&](int qi, uint32_t g) {
+                    const int r = qi / (A.KBS * 2), kb = (qi / 2) % A.KBS, nh = qi & 1;
+                    const uint32_t st = g & 1u;
+                    tc::mbar_arrive_expect_tx(&bfull[st], 16384u);
+                    tc::bulk_g2s(b_img + st * 16384, A.bimg + (((size_t)r * A.KBS + kb) * 2 + nh) * (kARows / 2 * 64),
+                                 16384u, &bfull[st]);
+                    last_b[st] = g;
+                };
+                bool ok = true;
+                if (gq >= 2 && !tc::mbar_wait(&bfree[gq & 1u], ((gq >> 1) + 1u) & 1u)) ok = false;
+                if (ok) issue(0, gq);
+                for (int qi = 0; qi < Q && ok; ++qi) {
+                    const uint32_t g = gq + (uint32_t)qi;
+                    const int r = qi / (A.KBS * 2), kb = (qi / 2) % A.KBS, nh = qi & 1;
+                    if (qi + 1 < Q) {
+                        const uint32_t g1 = g + 1;
+                        if (g1 >= 2 && !tc::mbar_wait(&bfree[g1 & 1u], ((g1 >> 1) + 1u) & 1u)) {
+                            ok = false;
+                            break;
+                        }
+                        issue(qi + 1, g1);
+                    }
+                    if (!tc::mbar_wait(&bfull[g & 1u], (g >> 1) & 1u)) {
+                        ok = false;
+                        break;
+                    }
+                    const uint32_t rg = rgi + (uint32_t)r;
+                    if (kb == 0 && nh == 0 && rg >= 2 && !tc::mbar_wait(&drained[rg & 1u], ((rg >> 1) + 1u) & 1u)) {
+                        ok = false;
+                        break;
+                    }
+                    tc::tc_fence_after();
+                    const uint32_t bb = tc::smem_u32(b_img + (g & 1u) * 16384);
+                    const uint32_t ah = tc::smem_u32(a_hi + kb * 16384), al = tc::smem_u32(a_lo + kb * 16384);
+                    const uint32_t d = tmem + (rg & 1u) * kARows + (uint32_t)nh * kANh;
+#pragma unroll
+                    for (int kk = 0; kk < 4; ++kk) {
+                        const uint64_t db = tc::desc_sw128(bb + kk * 32);
+                        tc::mma_bf16(d, tc::desc_sw128(ah + kk * 32), db, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+                        tc::mma_bf16(d, tc::desc_sw128(al + kk * 32), db, idesc, 1u);
+                    }
+                    tc::mma_commit(&bfree[g & 1u]);
+                    last_c[g & 1u] = g;
+                    if (kb == A.KBS - 1 && nh == 1) tc::mma_commit(&gfull[rg & 1u]);
+                }
+                if (!ok) {
+                    bad = 1;
+                    atomicExch(A.err, 11);
+                }
+                gq += (uint32_t)Q;
+                rgi += (uint32_t)A.R;
+            }
+        } else if (warp < 4) {
+            // (3) drain: each thread is one voxel (TMEM lane); items of the round's LUT rows
+            const int vloc = warp * 32 + lane;
+            float *row = dstage + (warp * 32 + lane) * kADrainStride;
+            for (int r = 0; r < A.R; ++r) {
+                const uint32_t rg = rgd + (uint32_t)r;
+                if (!bad && !tc::mbar_wait(&gfull[rg & 1u], (rg >> 1) & 1u)) {
+                    bad = 1;
+                    atomicExch(A.err, 12);
+                }
+                if (__any_sync(0xffffffffu, bad)) break;
+                tc::tc_fence_after();
+                for (int kbl = 0; kbl < kARows / 64; ++kbl) {
+                    const int kbf = r * (kARows / 64) + kbl;
+                    if (kbf >= A.NKB) break;
+                    const size_t pb = ((size_t)tile * A.NKB + kbf) * kATile + vloc;
+                    uint32_t j = A.ent_ptr[pb];
+                    const uint32_t p1 = A.ent_ptr[pb + 1];
+                    const float lsc = kbf < A.kb_ec ? A.l_scale : 1.f;
+                    for (int c = 0; c < 2; ++c) {
+                        __syncwarp();
+                        float g[32];
+                        tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (rg & 1u) * kARows + (uint32_t)(kbl * 64 + c * 32),
+                                  g);
+#pragma unroll
+                        for (int i = 0; i < 32; ++i) row[i] = g[i];
+                        const uint32_t lim = (uint32_t)(c + 1) * 32u;
+                        while (j < p1) {
+                            const uint32_t co = A.ent_co[j];
+                            const uint32_t o = co >> kAColBits;
+                            if (o >= lim) break;
+                            const float t = row[o - (uint32_t)c * 32u] * (__half2float(A.ent_l[j]) * lsc);
+                            if (kbf < A.kb_ec) A.terms[j] = t;
+                            else A.xout[co & ((1u << kAColBits) - 1u)] = (double)t;
+                            ++j;
+                        }
+                    }
+                }
+                tc::tc_fence_before();
+                tc::mbar_arrive(&drained[rg & 1u]);
+            }
+            rgd += (uint32_t)A.R;
+        }
+        if (__syncthreads_or(bad)) break;
+    }
+    // drain (a no-op after a normal exit) before TMEM is freed
+    if (warp == 4 && lane == 0) {
+        for (int st = 0; st < 2; ++st) {
+            if (last_b[st] != kNone && !tc::mbar_wait(&bfull[st], (last_b[st] >> 1) & 1u)) atomicExch(A.err, 13);
+            if (last_c[st] != kNone && !tc::mbar_wait(&bfree[st], (last_c[st] >> 1) & 1u)) atomicExch(A.err, 14);
+        }
+    }
+    if (A.partials) block_sum_store(nrm, A.partials + (size_t)blockIdx.x * kRedSlots);
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    if (warp == 0) tc::tmem_dealloc(tmem, 512);
+}
+
+// x[q] = eval[q] * sum of the IC column's terms, gathered in entry order (FP64 sums)
+__global__ void k_fibre_sum_entries(const uint32_t *__restrict__ fptr, const uint32_t *__restrict__ fperm,
+                                    const float *__restrict__ terms, const uint32_t *__restrict__ eval, int64_t ncols,
+                                    double *__restrict__ xout) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < ncols;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (uint32_t k = fptr[q]; k < fptr[q + 1]; ++k) s += (double)terms[fperm[k]];
+        xout[q] = s * (double)eval[q];
+    }
+}
+
+}  // namespace
+}  // namespace detail
+
+using namespace detail;
+
+int adjoint_tc(cgb_op *op, int mode, const float *yin, const float *axa, const float *axb, float ca, float cb,
+               const float *yobs, const float *sqw, double *xout, double *partials, cudaStream_t st, int *grid) {
+    CGB_TRY(ensure_tc(op));
+    if (grid) *grid = 0;
+    static bool attr_set[64] = {false};
+    if (op->device >= 0 && op->device < 64 && !attr_set[op->device]) {
+        CGB_CUDA(cudaFuncSetAttribute(k_adjoint_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)tca_smem_bytes(kAMaxKBS)));
+        attr_set[op->device] = true;
+    }
+    if (op->tc_kbs > kAMaxKBS) return fail(CGB_ERR_UNSUPPORTED, "tensor-core adjoint: nS > 320");
+    TcAdjArgs A;
+    A.nV = op->nV;
+    A.nS = op->nS;
+    A.KBS = op->tc_kbs;
+    A.R = op->tc_rounds;
+    A.NKB = op->tc_nkb;
+    A.kb_ec = op->tc_kb_ec;
+    A.ntiles = op->tc_ntiles;
+    A.ent_ptr = op->tc_ptr;
+    A.ent_co = op->tc_co;
+    A.ent_l = op->tc_l;
+    A.l_scale = op->tc_lscale;
+    A.bimg = op->tc_abimg;
+    A.mode = mode;
+    A.yin = yin;
+    A.axa = axa;
+    A.axb = axb;
+    A.yobs = yobs;
+    A.sqw = sqw;
+    A.ca = ca;
+    A.cb = cb;
+    A.terms = op->tc_terms;
+    A.xout = xout;
+    A.partials = partials;
+    A.err = op->tc_err;
+    int g = op->nsm < A.ntiles ? op->nsm : A.ntiles;
+    if (g > reduction_blocks(op)) g = reduction_blocks(op);
+    k_adjoint_tc<<<g, kAThreads, tca_smem_bytes(A.KBS), st>>>(A);
+    CGB_CUDA(cudaGetLastError());
+    const int64_t nic = (int64_t)op->nF * op->nIC;
+    if (nic > 0) {
+        int64_t gb = (nic + 255) / 256;
+        if (gb > (int64_t)op->nsm * 16) gb = (int64_t)op->nsm * 16;
+        k_fibre_sum_entries<<<(int)gb, 256, 0, st>>>(op->tc_fptr, op->tc_fperm, op->tc_terms, op->eval, nic, xout);
+        CGB_CUDA(cudaGetLastError());
+    }
+    if (grid) *grid = g;
+    return CGB_OK;
+}
+
+}  // namespace cgb

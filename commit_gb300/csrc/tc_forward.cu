@@ -1,0 +1,647 @@
+// Reduced-precision A*x on the tensor cores (tcgen05, BF16 operands, FP32 accumulation).
+//
+// A*x is, voxel by voxel, y[v, :] = sum_k C[v, k] * L[k, :] where k runs over the LUT rows
+// of every compartment (IC response i and orientation o, EC response i and orientation o,
+// ISO response i) and C[v, k] is the sum of l * x * eval over the voxel's items that use
+// row k (setup_operator.py:50-218 computes the same sums item by item).  Over a tile of 128
+// voxels this is a dense product C[128 x K] * L[K x nS]: the kernel builds C in shared
+// memory 64 LUT rows at a time, splits it into BF16 high and low parts (C = hi + lo to
+// about 16 bits), and multiplies both with the BF16 LUT on the tensor cores into one FP32
+// accumulator of 128 x nS in tensor memory.  The LUT is the only reduced-precision
+// operand, as in the CUDA-core BF16 path (operator_mixed.cuh).
+//
+// Data (built once per handle, ensure_tc):
+//  - entries: every (item, response) pair of the operator, ordered by (tile of 128
+//    voxels, K-block of 64 LUT rows, voxel, LUT row) -- ent_co = column of x | row in the
+//    K-block << 26, ent_l = FP16 length * 2^k (1 for EC / ISO) -- and ent_ptr, the
+//    first entry of each (tile, K-block, voxel), so a voxel's entries of one K-block are
+//    contiguous;
+//  - B images: per K-block the LUT rows transposed to [Np samples x 64 rows] BF16 in the
+//    K-major 128-byte-swizzled layout of tc_ptx.cuh, fetched whole by one bulk copy.
+//
+// Kernel: one CTA of 256 threads per SM (persistent over tiles), 2-stage pipeline over the
+// K-blocks of a tile: while the tensor cores multiply K-block b, the threads build the C
+// tile of block b+1 (two threads per voxel walk its entries into FP32 rows in shared
+// memory, in order, so results are deterministic) and one thread fetches its B image.
+// The 128 x Np accumulator (two MMAs of N = Np/2 per 16-row K step) is read back by the
+// 8 warps (lane quarter = warp % 4, column half = warp / 4) into y, with the residual-norm
+// epilogue of the CUDA-core kernel.
+#include <cub/cub.cuh>
+
+#include "operator_launch.cuh"
+#include "tc_ptx.cuh"
+
+namespace cgb {
+namespace detail {
+namespace {
+
+constexpr int kTcThreads = 256;
+constexpr int kTcTile = 128;           // voxels per tile (MMA M)
+constexpr int kTcKB = 64;              // LUT rows per K-block
+constexpr int kStageStride = 68;       // floats per FP32 staging row (64 + padding, 16-byte rows)
+constexpr uint32_t kColBits = 26;      // ent_co: column in the low 26 bits
+constexpr int kTcMaxNp = 320;          // padded samples the shared-memory budget allows
+
+struct TcFwdArgs {
+    int nV, nS, Np, NKB, ntiles;
+    int kb_ec;  // first K-block of EC / ISO rows (lengths 1, no 2^-k scale)
+    const uint32_t *ent_ptr;
+    const uint32_t *ent_co;
+    const __half *ent_l;
+    float l_scale;
+    const float *xe;
+    const __nv_bfloat16 *bimg;
+    float *yout, *axout;
+    const float *yobs, *sqw;
+    double *partials;
+    int *err;
+};
+
+__host__ __device__ constexpr size_t tc_smem_bytes(int Np) {
+    return 1024 /* alignment slack */ + 4 * 16384 /* A hi / lo x 2 stages */ + 2 * (size_t)Np * 128 /* B x 2 */ +
+           2 * kTcTile * kStageStride * 4 /* FP32 staging, 2 parts */ + 128 /* barriers, TMEM slot, flags */;
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1) k_forward_tc(const TcFwdArgs A) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    const uint32_t bbytes = (uint32_t)A.Np * 128u;
+    uint8_t *a_hi = sm;                       // 2 x 16384
+    uint8_t *a_lo = sm + 2 * 16384;           // 2 x 16384
+    uint8_t *b_img = sm + 4 * 16384;          // 2 x bbytes
+    float *stage = reinterpret_cast<float *>(b_img + 2 * bbytes);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(stage + 2 * kTcTile * kStageStride);  // bfull[2], mdone[2]
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 4);
+    uint64_t *bfull = bars, *mdone = bars + 2;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        tc::mbar_init(&bfull[0], 1);
+        tc::mbar_init(&bfull[1], 1);
+        tc::mbar_init(&mdone[0], 1);
+        tc::mbar_init(&mdone[1], 1);
+        tc::mbar_init_fence();
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(tmem_slot, 512);
+        tc::tmem_relinquish();
+    }
+    for (int i = tid; i < 2 * kTcTile * kStageStride; i += kTcThreads) stage[i] = 0.f;
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const int half = A.Np / 2;
+    const uint32_t idesc = tc::idesc_bf16(kTcTile, half);
+    const int vloc = tid & (kTcTile - 1), part = tid >> 7;
+    float *myrow = stage + (part * kTcTile + vloc) * kStageStride;
+    uint32_t it = 0;  // K-blocks processed by this CTA (pipeline stage = it & 1)
+    // thread 0: iteration of the last bulk copy issued / MMA group committed per stage, for
+    // draining on an early exit (kNone: none)
+    constexpr uint32_t kNone = 0xffffffffu;
+    uint32_t last_b[2] = {kNone, kNone}, last_c[2] = {kNone, kNone};
+    const bool vec4 = (A.nS & 3) == 0 && (reinterpret_cast<uintptr_t>(A.yout) & 15) == 0 &&
+                      (reinterpret_cast<uintptr_t>(A.axout) & 15) == 0;
+    double nrm = 0.0;
+    // a wait that ran out sets `bad` in its thread; every exit decision is taken on the OR
+    // of all threads' flags at a barrier (__syncthreads_or), so all threads leave together
+    int bad = 0;
+    bool stop = false;
+
+    for (int tile = blockIdx.x; tile < A.ntiles && !stop; tile += gridDim.x) {
+        for (int kb = 0; kb < A.NKB; ++kb, ++it) {
+            const uint32_t s = it & 1u;
+            // stage s is free once the MMAs of its previous use (two K-blocks ago) completed
+            if (it >= 2 && !tc::mbar_wait(&mdone[s], ((it >> 1) + 1u) & 1u)) {
+                bad = 1;
+                atomicExch(A.err, 1);
+            }
+            if (tid == 0 && !bad) {
+                tc::mbar_arrive_expect_tx(&bfull[s], bbytes);
+                tc::bulk_g2s(b_img + s * bbytes, A.bimg + (size_t)kb * A.Np * kTcKB, bbytes, &bfull[s]);
+                last_b[s] = it;
+            }
+            // C rows of this K-block: two threads per voxel, each over half of its entries
+            const size_t pb = ((size_t)tile * A.NKB + kb) * kTcTile + vloc;
+            const uint32_t p0 = A.ent_ptr[pb], p1 = A.ent_ptr[pb + 1];
+            const uint32_t hcount = (p1 - p0 + 1) >> 1;
+            const uint32_t j0 = part ? p0 + hcount : p0, j1 = part ? p1 : p0 + hcount;
+            for (uint32_t j = j0; j < j1; j += 8) {
+                uint32_t co[8];
+                float c[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    co[u] = 0;
+                    c[u] = 0.f;
+                    if (j + u < j1) {
+                        co[u] = __ldg(A.ent_co + j + u);
+                        c[u] = __half2float(A.ent_l[j + u]);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    if (j + u < j1) c[u] *= __ldg(A.xe + (co[u] & ((1u << kColBits) - 1u)));
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    if (j + u < j1) myrow[co[u] >> kColBits] += c[u];
+            }
+            __syncthreads();
+            // FP32 rows -> BF16 hi / lo in the swizzled layout; staging back to zero
+            uint8_t *ah = a_hi + s * 16384, *al = a_lo + s * 16384;
+            const float lsc = kb < A.kb_ec ? A.l_scale : 1.f;
+#pragma unroll
+            for (int q = tid; q < kTcTile * 8; q += kTcThreads) {
+                const int m = q >> 3, p = q & 7, cl = p ^ (m & 7);
+                float4 *r0 = reinterpret_cast<float4 *>(stage + m * kStageStride + cl * 8);
+                float4 *r1 = reinterpret_cast<float4 *>(stage + (kTcTile + m) * kStageStride + cl * 8);
+                const float4 x0 = r0[0], x1 = r0[1], y0 = r1[0], y1 = r1[1];
+                const float v[8] = {x0.x + y0.x, x0.y + y0.y, x0.z + y0.z, x0.w + y0.w,
+                                    x1.x + y1.x, x1.y + y1.y, x1.z + y1.z, x1.w + y1.w};
+                uint32_t hw[4], lw[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const float a = v[2 * e] * lsc, b = v[2 * e + 1] * lsc;
+                    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+                    const float2 hf = __bfloat1622float2(h);
+                    const __nv_bfloat162 l = __floats2bfloat162_rn(a - hf.x, b - hf.y);
+                    hw[e] = *reinterpret_cast<const uint32_t *>(&h);
+                    lw[e] = *reinterpret_cast<const uint32_t *>(&l);
+                }
+                const uint32_t off = (uint32_t)(m >> 3) * 1024u + (uint32_t)(m & 7) * 128u + (uint32_t)p * 16u;
+                *reinterpret_cast<uint4 *>(ah + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                *reinterpret_cast<uint4 *>(al + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+                const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+                r0[0] = z;
+                r0[1] = z;
+                r1[0] = z;
+                r1[1] = z;
+            }
+            tc::fence_async_smem();
+            if (__syncthreads_or(bad)) {
+                stop = true;
+                break;
+            }
+            if (tid == 0) {
+                if (!tc::mbar_wait(&bfull[s], (it >> 1) & 1u)) {
+                    bad = 1;
+                    atomicExch(A.err, 2);
+                } else {
+                    tc::tc_fence_after();
+                    const uint32_t ab_hi = tc::smem_u32(ah), ab_lo = tc::smem_u32(al);
+                    const uint32_t bb = tc::smem_u32(b_img + s * bbytes);
+#pragma unroll
+                    for (int kk = 0; kk < kTcKB / 16; ++kk) {
+                        const uint64_t dh = tc::desc_sw128(ab_hi + kk * 32), dl = tc::desc_sw128(ab_lo + kk * 32);
+#pragma unroll
+                        for (int h = 0; h < 2; ++h) {
+                            const uint64_t db = tc::desc_sw128(bb + (uint32_t)h * (uint32_t)half * 128u + kk * 32);
+                            const uint32_t d = tmem + (uint32_t)(h * half);
+                            tc::mma_bf16(d, dh, db, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+                            tc::mma_bf16(d, dl, db, idesc, 1u);
+                        }
+                    }
+                    tc::mma_commit(&mdone[s]);
+                    last_c[s] = it;
+                }
+            }
+        }
+        if (stop) break;
+        // epilogue: the accumulator is complete once the tile's last MMA group is
+        const uint32_t last = it - 1;
+        if (!tc::mbar_wait(&mdone[last & 1u], (last >> 1) & 1u)) {
+            bad = 1;
+            atomicExch(A.err, 3);
+        }
+        tc::tc_fence_after();
+        if (__syncthreads_or(bad)) break;
+        const int q = warp & 3, colh = warp >> 2;
+        const int v = tile * kTcTile + q * 32 + lane;
+        float vn = 0.f;
+        for (int c0 = colh * half; c0 < (colh + 1) * half; c0 += 16) {
+            float r[16];
+            tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, r);
+            if (v < A.nV && vec4 && c0 + 16 <= A.nS && !A.partials) {
+                const size_t idx = (size_t)v * A.nS + c0;
+#pragma unroll
+                for (int i = 0; i < 16; i += 4) {
+                    const float4 w = make_float4(r[i], r[i + 1], r[i + 2], r[i + 3]);
+                    if (A.yout) *reinterpret_cast<float4 *>(A.yout + idx + i) = w;
+                    if (A.axout) *reinterpret_cast<float4 *>(A.axout + idx + i) = w;
+                }
+            } else if (v < A.nV) {
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    const int sidx = c0 + i;
+                    if (sidx < A.nS) {
+                        const size_t idx = (size_t)v * A.nS + sidx;
+                        if (A.yout) A.yout[idx] = r[i];
+                        if (A.axout) A.axout[idx] = r[i];
+                        if (A.partials) {
+                            float rr = A.yobs ? r[i] - A.yobs[idx] : r[i];
+                            if (A.sqw) rr *= A.sqw[idx];
+                            vn = fmaf(rr, rr, vn);
+                        }
+                    }
+                }
+            }
+        }
+        nrm += (double)vn;
+        tc::tc_fence_before();
+        __syncthreads();
+    }
+    // drain (a no-op after a normal exit): the last copy and MMA group of each stage have
+    // completed before TMEM is freed; waits that run out are recorded
+    __syncthreads();
+    if (tid == 0) {
+        for (int st = 0; st < 2; ++st) {
+            if (last_b[st] != kNone && !tc::mbar_wait(&bfull[st], (last_b[st] >> 1) & 1u)) atomicExch(A.err, 4);
+            if (last_c[st] != kNone && !tc::mbar_wait(&mdone[st], (last_c[st] >> 1) & 1u)) atomicExch(A.err, 5);
+        }
+    }
+    if (A.partials) block_sum_store(nrm, A.partials + (size_t)blockIdx.x * kRedSlots);
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    if (warp == 0) tc::tmem_dealloc(tmem, 512);
+}
+
+// ------------------------------------------------------------------ one-time layout
+__device__ __forceinline__ int owner_of(const uint32_t *ptr, int nV, uint32_t j) {
+    // the voxel v with ptr[v] <= j < ptr[v+1]
+    int lo = 0, hi = nV;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (ptr[mid] <= j) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+struct TcLayoutArgs {
+    const OpDev P;
+    int NKB, nkbd, kb_ec, kb_iso;
+    __half one;  // the length of an EC / ISO item (1; IC lengths are scaled by 2^k)
+};
+
+__global__ void k_tc_entries(const TcLayoutArgs L, const __half *__restrict__ l16, uint32_t *__restrict__ key,
+                             unsigned long long *__restrict__ val) {
+    const OpDev &P = L.P;
+    const int64_t nic = P.n * P.nIC, nec = (int64_t)P.nE * P.nEC, niso = (int64_t)P.nISOv * P.nISO;
+    const int64_t total = nic + nec + niso;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        int v, kb;
+        uint32_t col, row;
+        __half l;
+        if (q < nic) {
+            const int i = (int)(q / P.n);
+            const uint32_t j = (uint32_t)(q - (int64_t)i * P.n);
+            v = owner_of(P.vox_ptr, P.nV, j);
+            const uint32_t o = P.seg_o[j];
+            kb = i * L.nkbd + (int)(o >> 6);
+            row = o & 63u;
+            col = (uint32_t)i * (uint32_t)P.nF + P.seg_f[j];
+            l = l16[j];
+        } else if (q < nic + nec) {
+            const int64_t r = q - nic;
+            const int i = (int)(r / P.nE);
+            const uint32_t e = (uint32_t)(r - (int64_t)i * P.nE);
+            v = owner_of(P.ec_ptr, P.nV, e);
+            const uint32_t o = P.ec_o[e];
+            kb = L.kb_ec + i * L.nkbd + (int)(o >> 6);
+            row = o & 63u;
+            col = (uint32_t)(P.ec_base + (int64_t)i * P.nE + P.ec_col[e]);
+            l = L.one;
+        } else {
+            const int64_t r = q - nic - nec;
+            const int i = (int)(r / P.nISOv);
+            const uint32_t e = (uint32_t)(r - (int64_t)i * P.nISOv);
+            v = owner_of(P.iso_ptr, P.nV, e);
+            kb = L.kb_iso;
+            row = (uint32_t)i;
+            col = (uint32_t)(P.iso_base + (int64_t)i * P.nISOv + P.iso_col[e]);
+            l = L.one;
+        }
+        key[q] = ((uint32_t)(v >> 7) * (uint32_t)L.NKB + (uint32_t)kb) * (uint32_t)kTcTile + (uint32_t)(v & 127);
+        val[q] = (unsigned long long)(col | (row << kColBits)) |
+                 ((unsigned long long)__half_as_ushort(l) << 32);
+    }
+}
+
+__global__ void k_tc_split(const unsigned long long *__restrict__ val, int64_t n, uint32_t *__restrict__ co,
+                           __half *__restrict__ l, const uint32_t *__restrict__ key, uint32_t *__restrict__ count) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned long long w = val[q];
+        co[q] = (uint32_t)w;
+        l[q] = __ushort_as_half((unsigned short)(w >> 32));
+        atomicAdd(count + key[q], 1u);
+    }
+}
+
+// LUT rows of every K-block as [Np samples x 64 rows] BF16, K-major, 128-byte swizzle
+__global__ void k_tc_bimg(const OpDev P, int Np, int NKB, int nkbd, int kb_ec, int kb_iso,
+                          __nv_bfloat16 *__restrict__ img) {
+    const int64_t total = (int64_t)NKB * Np * kTcKB;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int kb = (int)(q / ((int64_t)Np * kTcKB));
+        const int r = (int)(q - (int64_t)kb * Np * kTcKB);
+        const int s = r / kTcKB, k = r - s * kTcKB;
+        float v = 0.f;
+        if (s < P.nS) {
+            if (kb < kb_ec) {
+                const int i = kb / nkbd, o = (kb - i * nkbd) * kTcKB + k;
+                if (o < P.ndirs) v = P.lutIC[((size_t)i * P.ndirs + o) * P.nS + s];
+            } else if (kb < kb_iso) {
+                const int i = (kb - kb_ec) / nkbd, o = (kb - kb_ec - i * nkbd) * kTcKB + k;
+                if (o < P.ndirs) v = P.lutEC[((size_t)i * P.ndirs + o) * P.nS + s];
+            } else if (k < P.nISO) {
+                v = P.lutISO[(size_t)k * P.nS + s];
+            }
+        }
+        img[(size_t)kb * Np * kTcKB + tc::sw128_offset((uint32_t)s, (uint32_t)k) / 2] = __float2bfloat16_rn(v);
+    }
+}
+
+// IC entries (K-blocks before kb_ec) keyed by their column, for the entry-order fibre index
+__global__ void k_tc_fib_keys(const uint32_t *__restrict__ key, const uint32_t *__restrict__ co, int64_t n, int NKB,
+                              int kb_ec, uint32_t *__restrict__ ckey, uint32_t *__restrict__ pos,
+                              unsigned long long *__restrict__ nic) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const int kb = (int)((key[q] / (uint32_t)kTcTile) % (uint32_t)NKB);
+        const bool ic = kb < kb_ec;
+        ckey[q] = ic ? (co[q] & ((1u << kColBits) - 1u)) : 0xffffffffu;
+        pos[q] = (uint32_t)q;
+        if (ic) atomicAdd(nic, 1ull);
+    }
+}
+
+__global__ void k_tc_count(const uint32_t *__restrict__ ckey, int64_t n, uint32_t *__restrict__ count) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(count + ckey[q], 1u);
+}
+
+// LUT rows as the B operand of the adjoint: per round of 256 rows, sample K-block and half,
+// [128 rows x 64 samples] BF16, K-major, 128-byte swizzle; row g is the forward's K index g
+__global__ void k_tca_bimg(const OpDev P, int R, int KBS, int NKB, int nkbd, int kb_ec, int kb_iso,
+                           __nv_bfloat16 *__restrict__ img) {
+    const int64_t total = (int64_t)R * KBS * 2 * 128 * 64;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t item = q / (128 * 64);
+        const int rr = (int)(q - item * 128 * 64), row = rr / 64, k = rr - row * 64;
+        const int nh = (int)(item & 1), kb = (int)((item >> 1) % KBS), r = (int)((item >> 1) / KBS);
+        const int g = r * 256 + nh * 128 + row, s = kb * 64 + k;
+        const int kbf = g / kTcKB, kk = g - kbf * kTcKB;
+        float v = 0.f;
+        if (s < P.nS && kbf < NKB) {
+            if (kbf < kb_ec) {
+                const int i = kbf / nkbd, o = (kbf - i * nkbd) * kTcKB + kk;
+                if (o < P.ndirs) v = P.lutIC[((size_t)i * P.ndirs + o) * P.nS + s];
+            } else if (kbf < kb_iso) {
+                const int i = (kbf - kb_ec) / nkbd, o = (kbf - kb_ec - i * nkbd) * kTcKB + kk;
+                if (o < P.ndirs) v = P.lutEC[((size_t)i * P.ndirs + o) * P.nS + s];
+            } else if (kk < P.nISO) {
+                v = P.lutISO[(size_t)kk * P.nS + s];
+            }
+        }
+        img[item * 128 * 64 + tc::sw128_offset((uint32_t)row, (uint32_t)k) / 2] = __float2bfloat16_rn(v);
+    }
+}
+
+__global__ void k_tc_xe(const double *__restrict__ x, const uint32_t *__restrict__ eval, int64_t nic, int64_t ncols,
+                        float *__restrict__ xe) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < ncols;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        float v = (float)x[q];
+        if (q < nic) v *= (float)eval[q];
+        xe[q] = v;
+    }
+}
+
+int grid_of(int64_t n, int nsm) {
+    int64_t g = (n + 255) / 256;
+    if (g > (int64_t)nsm * 16) g = (int64_t)nsm * 16;
+    return g < 1 ? 1 : (int)g;
+}
+
+}  // namespace
+}  // namespace detail
+
+using namespace detail;
+
+// Whether the tensor-core forward handles this operator: padded samples within the
+// shared-memory budget, columns within ent_co's 26 bits, at most 64 ISO responses.
+bool tc_supported(const cgb_op *op) {
+    const int Np = (op->nS + 31) / 32 * 32;
+    const int64_t nent = op->n * op->nIC + (int64_t)op->nE * op->nEC + (int64_t)op->nISOv * op->nISO;
+    return !op->nolut && op->nV > 0 && Np <= kTcMaxNp && op->ncols < ((int64_t)1 << kColBits) && op->nISO <= 64 &&
+           nent > 0 && nent < ((int64_t)1 << 32);
+}
+
+bool tc_forward_enabled(const cgb_op *op) { return op->tc_mode != 1 && tc_supported(op); }
+
+// entries, their per-(tile, K-block, voxel) offsets and the B images; needs the FP16
+// lengths of ensure_reduced
+int ensure_tc(cgb_op *op) {
+    if (op->tc_ready) return CGB_OK;
+    if (!tc_supported(op)) return fail(CGB_ERR_UNSUPPORTED, "tensor-core forward: operator shape not supported");
+    const OpDev P = op->dev();
+    const int nkbd = (op->ndirs + kTcKB - 1) / kTcKB;
+    const int kb_ec = op->nIC * nkbd;
+    const int kb_iso = kb_ec + ((op->nE > 0 && op->nEC > 0) ? op->nEC * nkbd : 0);
+    const int NKB = kb_iso + ((op->nISOv > 0 && op->nISO > 0) ? 1 : 0);
+    const int Np = (op->nS + 31) / 32 * 32;
+    const int ntiles = (op->nV + kTcTile - 1) / kTcTile;
+    const int64_t nent = op->n * op->nIC + (int64_t)op->nE * op->nEC + (int64_t)op->nISOv * op->nISO;
+    const int64_t nkeys = (int64_t)ntiles * NKB * kTcTile;
+    if (nkeys >= ((int64_t)1 << 32) - 1) return fail(CGB_ERR_UNSUPPORTED, "tensor-core forward: too many tiles");
+    const int64_t ncount = nkeys + 1 > (int64_t)op->nF * op->nIC + 1 ? nkeys + 1 : (int64_t)op->nF * op->nIC + 1;
+    const float lscale = op->len16_inv_scale > 0.f ? op->len16_inv_scale : 1.f;
+    TcLayoutArgs L{P, NKB, nkbd, kb_ec, kb_iso, __float2half_rn(1.f)};
+
+    uint32_t *key = nullptr, *key2 = nullptr, *count = nullptr;
+    unsigned long long *val = nullptr, *val2 = nullptr;
+    void *tmp = nullptr;
+    size_t tmp_bytes = 0;
+    int rc = CGB_OK;
+    auto cu = [&](cudaError_t e, const char *what) {
+        if (e != cudaSuccess && rc == CGB_OK) rc = cuda_fail(e, what);
+        return rc == CGB_OK;
+    };
+    int bits = 1;
+    while (bits < 32 && (((uint64_t)nkeys) >> bits) != 0) ++bits;
+    cu(cudaMalloc((void **)&op->tc_co, nent * sizeof(uint32_t)), "cudaMalloc");
+    cu(cudaMalloc((void **)&op->tc_l, nent * sizeof(__half)), "cudaMalloc");
+    cu(cudaMalloc((void **)&op->tc_ptr, (nkeys + 1) * sizeof(uint32_t)), "cudaMalloc");
+    cu(cudaMalloc((void **)&op->tc_bimg, (size_t)(NKB > 0 ? NKB : 1) * Np * kTcKB * sizeof(__nv_bfloat16)),
+       "cudaMalloc");
+    cu(cudaMalloc((void **)&op->tc_xe, (size_t)(op->ncols > 0 ? op->ncols : 1) * sizeof(float)), "cudaMalloc");
+    cu(cudaMalloc((void **)&op->tc_err, sizeof(int)), "cudaMalloc");
+    cu(cudaMalloc((void **)&key, nent * sizeof(uint32_t)), "cudaMalloc");
+    cu(cudaMalloc((void **)&key2, nent * sizeof(uint32_t)), "cudaMalloc");
+    cu(cudaMalloc((void **)&val, nent * sizeof(unsigned long long)), "cudaMalloc");
+    cu(cudaMalloc((void **)&val2, nent * sizeof(unsigned long long)), "cudaMalloc");
+    cu(cudaMalloc((void **)&count, ncount * sizeof(uint32_t)), "cudaMalloc");
+    if (rc == CGB_OK) {
+        cu(cudaMemset(op->tc_err, 0, sizeof(int)), "cudaMemset");
+        cu(cudaMemset(count, 0, (nkeys + 1) * sizeof(uint32_t)), "cudaMemset");
+        k_tc_entries<<<grid_of(nent, op->nsm), 256>>>(L, op->seg_l16, key, val);
+        cu(cudaGetLastError(), "k_tc_entries");
+        cu(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, key, key2, val, val2, nent, 0, bits), "cub sort");
+        size_t scan_bytes = 0;
+        cu(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, count, op->tc_ptr, nkeys + 1), "cub scan");
+        if (scan_bytes > tmp_bytes) tmp_bytes = scan_bytes;
+        cu(cudaMalloc(&tmp, tmp_bytes), "cudaMalloc");
+    }
+    if (rc == CGB_OK) {
+        cu(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, key, key2, val, val2, nent, 0, bits), "cub sort");
+        k_tc_split<<<grid_of(nent, op->nsm), 256>>>(val2, nent, op->tc_co, op->tc_l, key2, count);
+        cu(cudaGetLastError(), "k_tc_split");
+        cu(cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, count, op->tc_ptr, nkeys + 1), "cub scan");
+        const int64_t nimg = (int64_t)NKB * Np * kTcKB;
+        k_tc_bimg<<<grid_of(nimg, op->nsm), 256>>>(P, Np, NKB, nkbd, kb_ec, kb_iso, op->tc_bimg);
+        cu(cudaGetLastError(), "k_tc_bimg");
+        cu(cudaFuncSetAttribute(k_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes(Np)),
+           "cudaFuncSetAttribute");
+    }
+    // adjoint: the IC entries' positions grouped by column (stable: ascending positions),
+    // their CSR offsets per column, the LUT images of the adjoint and the term array
+    const int KBS = (op->nS + 63) / 64;
+    const int R = (NKB * kTcKB + 255) / 256;
+    const int64_t nic_cols = (int64_t)op->nF * op->nIC;
+    if (rc == CGB_OK) {
+        unsigned long long *dnic = nullptr;
+        cu(cudaMalloc((void **)&dnic, sizeof(unsigned long long)), "cudaMalloc");
+        cu(cudaMemset(dnic, 0, sizeof(unsigned long long)), "cudaMemset");
+        // key / val buffers are reused: key <- column keys, (uint32 view of val) <- positions
+        uint32_t *pos = reinterpret_cast<uint32_t *>(val), *pos2 = reinterpret_cast<uint32_t *>(val2);
+        k_tc_fib_keys<<<grid_of(nent, op->nsm), 256>>>(key2, op->tc_co, nent, NKB, kb_ec, key, pos, dnic);
+        cu(cudaGetLastError(), "k_tc_fib_keys");
+        unsigned long long hnic = 0;
+        cu(cudaMemcpy(&hnic, dnic, sizeof(hnic), cudaMemcpyDeviceToHost), "cudaMemcpy");
+        cudaFree(dnic);
+        int cbits = 1;
+        while (cbits < 32 && (((uint64_t)nic_cols) >> cbits) != 0) ++cbits;
+        // non-IC entries carry key 0xffffffff: sort all 32 bits so they go last
+        size_t need = 0;
+        cu(cub::DeviceRadixSort::SortPairs(nullptr, need, key, key2, pos, pos2, nent, 0, 32), "cub sort");
+        if (need > tmp_bytes) {
+            cudaFree(tmp);
+            tmp = nullptr;
+            tmp_bytes = need;
+            cu(cudaMalloc(&tmp, tmp_bytes), "cudaMalloc");
+        }
+        cu(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, key, key2, pos, pos2, nent, 0, 32), "cub sort");
+        cu(cudaMalloc((void **)&op->tc_fperm, (hnic > 0 ? hnic : 1) * sizeof(uint32_t)), "cudaMalloc");
+        cu(cudaMalloc((void **)&op->tc_fptr, (nic_cols + 1) * sizeof(uint32_t)), "cudaMalloc");
+        if (rc == CGB_OK && hnic > 0)
+            cu(cudaMemcpy(op->tc_fperm, pos2, hnic * sizeof(uint32_t), cudaMemcpyDeviceToDevice), "cudaMemcpy");
+        cu(cudaMemset(count, 0, (nic_cols + 1) * sizeof(uint32_t)), "cudaMemset");
+        if (rc == CGB_OK && hnic > 0) {
+            k_tc_count<<<grid_of((int64_t)hnic, op->nsm), 256>>>(key2, (int64_t)hnic, count);
+            cu(cudaGetLastError(), "k_tc_count");
+        }
+        size_t scan_need = 0;
+        cu(cub::DeviceScan::ExclusiveSum(nullptr, scan_need, count, op->tc_fptr, nic_cols + 1), "cub scan");
+        if (scan_need > tmp_bytes) {
+            cudaFree(tmp);
+            tmp = nullptr;
+            tmp_bytes = scan_need;
+            cu(cudaMalloc(&tmp, tmp_bytes), "cudaMalloc");
+        }
+        cu(cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, count, op->tc_fptr, nic_cols + 1), "cub scan");
+        cu(cudaMalloc((void **)&op->tc_abimg, (size_t)R * KBS * 2 * 128 * 64 * sizeof(__nv_bfloat16)), "cudaMalloc");
+        if (rc == CGB_OK) {
+            k_tca_bimg<<<grid_of((int64_t)R * KBS * 2 * 128 * 64, op->nsm), 256>>>(P, R, KBS, NKB, nkbd, kb_ec, kb_iso,
+                                                                                   op->tc_abimg);
+            cu(cudaGetLastError(), "k_tca_bimg");
+        }
+        cu(cudaMalloc((void **)&op->tc_terms, nent * sizeof(float)), "cudaMalloc");
+        cu(cudaDeviceSynchronize(), "tensor-core layout");
+    }
+    cudaFree(key);
+    cudaFree(key2);
+    cudaFree(val);
+    cudaFree(val2);
+    cudaFree(count);
+    cudaFree(tmp);
+    if (rc != CGB_OK) return rc;
+    op->tc_np = Np;
+    op->tc_nkb = NKB;
+    op->tc_kb_ec = kb_ec;
+    op->tc_ntiles = ntiles;
+    op->tc_lscale = lscale;
+    op->tc_kbs = KBS;
+    op->tc_rounds = R;
+    op->tc_nent = nent;
+    op->bytes += nent * 6 + (nkeys + 1) * 4 + (size_t)NKB * Np * kTcKB * 2 + (size_t)op->ncols * 4 + nent * 8 +
+                 (size_t)(nic_cols + 1) * 4 + (size_t)R * KBS * 2 * 128 * 64 * 2;
+    op->tc_ready = 1;
+    return CGB_OK;
+}
+
+int forward_tc(cgb_op *op, const double *x, float *y, float *ax, const float *yobs, const float *sqw,
+               double *partials, cudaStream_t st, int *grid) {
+    CGB_TRY(ensure_tc(op));
+    if (grid) *grid = 0;
+    if (op->ncols > 0) {
+        k_tc_xe<<<grid_of(op->ncols, op->nsm), 256, 0, st>>>(x, op->eval, (int64_t)op->nF * op->nIC, op->ncols,
+                                                                 op->tc_xe);
+        CGB_CUDA(cudaGetLastError());
+    }
+    TcFwdArgs A;
+    A.nV = op->nV;
+    A.nS = op->nS;
+    A.Np = op->tc_np;
+    A.NKB = op->tc_nkb;
+    A.kb_ec = op->tc_kb_ec;
+    A.ntiles = op->tc_ntiles;
+    A.ent_ptr = op->tc_ptr;
+    A.ent_co = op->tc_co;
+    A.ent_l = op->tc_l;
+    A.l_scale = op->tc_lscale;
+    A.xe = op->tc_xe;
+    A.bimg = op->tc_bimg;
+    A.yout = y;
+    A.axout = ax;
+    A.yobs = yobs;
+    A.sqw = sqw;
+    A.partials = partials;
+    A.err = op->tc_err;
+    int g = op->nsm < A.ntiles ? op->nsm : A.ntiles;
+    if (g > reduction_blocks(op)) g = reduction_blocks(op);
+    k_forward_tc<<<g, kTcThreads, tc_smem_bytes(A.Np), st>>>(A);
+    CGB_CUDA(cudaGetLastError());
+    if (grid) *grid = g;
+    return CGB_OK;
+}
+
+}  // namespace cgb
+
+extern "C" int cgb_op_tensor_cores(cgb_op *op, int mode, int *out) {
+    if (!op) return cgb::fail(CGB_ERR_INVALID, "null handle");
+    if (mode > 2) return cgb::fail(CGB_ERR_INVALID, "mode must be 0 (automatic), 1 (off) or 2 (on)");
+    if (mode == 2 && !cgb::tc_supported(op))
+        return cgb::fail(CGB_ERR_UNSUPPORTED, "tensor-core forward: operator shape not supported");
+    if (mode >= 0) op->tc_mode = mode;
+    if (out) *out = cgb::tc_forward_enabled(op) ? 1 : 0;
+    return CGB_OK;
+}
+
+extern "C" int cgb_op_device_status(cgb_op *op) {
+    if (!op) return cgb::fail(CGB_ERR_INVALID, "null handle");
+    int dev = 0;
+    CGB_CUDA(cudaGetDevice(&dev));
+    CGB_CUDA(cudaSetDevice(op->device));
+    cudaError_t e = cudaDeviceSynchronize();
+    int h = 0;
+    if (e == cudaSuccess && op->tc_err) {
+        e = cudaMemcpy(&h, op->tc_err, sizeof(int), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess && h) e = cudaMemset(op->tc_err, 0, sizeof(int));
+    }
+    cudaSetDevice(dev);
+    CGB_CUDA(e);
+    if (h) return cgb::fail(CGB_ERR_CUDA, "a tensor-core kernel gave up waiting (code " + std::to_string(h) + ")");
+    return CGB_OK;
+}

@@ -500,6 +500,7 @@ int cgb_trk2dict(const cgb_t2d_params *prm, const float *pts, const int64_t *off
                  const uint8_t *iso_mask, cgb_t2d_result *out, void *stream) {
     if (!prm || !out || !hash || (nfib > 0 && (!pts || !offsets))) return fail(CGB_ERR_INVALID, "null argument");
     if (nfib < 0) return fail(CGB_ERR_INVALID, "negative streamline count");
+    NvtxRange nv("cgb_trk2dict");
     if (prm->dim[0] <= 0 || prm->dim[1] <= 0 || prm->dim[2] <= 0 || prm->dim[0] > 65535 || prm->dim[1] > 65535 ||
         prm->dim[2] > 65535)
         return fail(CGB_ERR_INVALID, "grid dimensions must be in 1..65535");

@@ -208,6 +208,17 @@ class LinearOperator:
         check(lib().cgb_op_ff_kernels(self._h.ptr, -1 if variant is None else int(variant), ctypes.byref(out)))
         return int(out.value)
 
+    def tensor_cores(self, mode: int | None = None) -> bool:
+        """Reduced-precision BF16 A*x on the tensor cores: mode 0 whenever the shape allows,
+        1 CUDA cores only, 2 required; None only reads.  Returns whether it is in use."""
+        out = ctypes.c_int32()
+        check(lib().cgb_op_tensor_cores(self._h.ptr, -1 if mode is None else int(mode), ctypes.byref(out)))
+        return bool(out.value)
+
+    def device_status(self) -> None:
+        """Synchronise and raise CgbError if a tensor-core kernel gave up a bounded wait."""
+        check(lib().cgb_op_device_status(self._h.ptr))
+
     def host_mode(self, mode: int | None = None) -> int:
         """Host-buffer products: 0 automatic (direct row access for page-locked rows),
         1 staged copies, 2 direct; None only reads."""

@@ -375,3 +375,50 @@ def make_signal(Ax: np.ndarray, seed: int) -> np.ndarray:
 
 def make_x(ncols: int, seed: int) -> np.ndarray:
     return np.random.default_rng(seed).uniform(0.0, 1.0, size=ncols)
+
+
+def voxel_slab(D: dict, K: dict, frac: float) -> dict:
+    """A central slab of voxels holding about ``frac`` of the IC segments, as a dictionary of
+    its own (voxels renumbered from 0, every streamline kept as a column, the slab's EC and
+    ISO elements renumbered in voxel order).  The slab's operator is the restriction of A to
+    the slab's rows: its A x is rows [lo*nS, hi*nS) of the full A x once x is mapped with
+    ``cols`` (the full column of each slab column), and its A' y is the full A' of y zeroed
+    outside those rows, read at ``cols``.  IC/EC/ISO arrays must be voxel-sorted, as
+    load_dictionary leaves them (commit/core.pyx:508-562).
+
+    Returns {'D': slab dictionary, 'share': its fraction of the IC segments, 'voxels':
+    (lo, hi), 'cols': int64 array of full-column indices}."""
+    vox = D['IC']['vox']
+    nV = int(D['IC']['nVOX'])
+    counts = np.bincount(vox, minlength=nV)
+    c = np.cumsum(counts)
+    n = int(c[-1])
+    mid = int(np.searchsorted(c, n // 2))
+    lo, hi = mid, mid
+    target = max(1, int(frac * n))
+    while (int(c[hi - 1]) if hi > 0 else 0) - (int(c[lo - 1]) if lo > 0 else 0) < target and (lo > 0 or hi < nV):
+        lo = max(0, lo - max(1, (hi - lo) // 2 + 16))
+        hi = min(nV, hi + max(1, (hi - lo) // 2 + 16))
+    s0 = int(c[lo - 1]) if lo > 0 else 0
+    s1 = int(c[hi - 1]) if hi > 0 else 0
+    nIC, nEC, nISO = K['wmr'].shape[0], K['wmh'].shape[0], K['iso'].shape[0]
+    IC = {k: np.ascontiguousarray(D['IC'][k][s0:s1]) for k in ('str', 'vox', 'dir', 'len')}
+    IC['vox'] = (IC['vox'] - lo).astype(np.uint32)
+    IC['n'] = s1 - s0
+    IC['nSTR'] = D['IC']['nSTR']
+    IC['nVOX'] = hi - lo
+    ev = D['IC'].get('eval')
+    IC['eval'] = np.ones(IC['nSTR'] * nIC, np.uint32) if ev is None else ev
+    ecv = D['EC']['vox']
+    e0, e1 = int(np.searchsorted(ecv, lo)), int(np.searchsorted(ecv, hi))
+    EC = {'vox': (ecv[e0:e1] - lo).astype(np.uint32), 'dir': np.ascontiguousarray(D['EC']['dir'][e0:e1]),
+          'n': e1 - e0}
+    iv = D['ISO']['vox']
+    i0, i1 = int(np.searchsorted(iv, lo)), int(np.searchsorted(iv, hi))
+    ISO = {'vox': (iv[i0:i1] - lo).astype(np.uint32), 'n': i1 - i0}
+    nF, nE, nI = int(D['IC']['nSTR']), int(D['EC']['n']), int(D['ISO']['n'])
+    cols = [np.arange(nF * nIC, dtype=np.int64)]
+    cols += [nF * nIC + i * nE + np.arange(e0, e1, dtype=np.int64) for i in range(nEC)]
+    cols += [nF * nIC + nE * nEC + i * nI + np.arange(i0, i1, dtype=np.int64) for i in range(nISO)]
+    return {'D': {'IC': IC, 'EC': EC, 'ISO': ISO}, 'share': (s1 - s0) / n if n else 0.0, 'voxels': (lo, hi),
+            'cols': np.concatenate(cols)}

@@ -141,7 +141,10 @@ int cgb_op_set_arith(cgb_op *op, int arith);
  * `stream` (a cudaStream_t; NULL = legacy default stream).  `out` is fully written (no
  * pre-zeroing needed).  dtype CGB_DTYPE_F64 uses the handle's FP64 arithmetic;
  * CGB_DTYPE_F32 uses the reduced-precision path `arith` (CGB_ARITH_BF16/FP16/F32).
- * in_len/out_len are checked against the operator shape (CGB_ERR_DIMENSION).
+ * in_len/out_len are checked against the operator shape (CGB_ERR_DIMENSION).  FP64 inputs
+ * may have any finite magnitude: the float-float kernels scale operands whose products
+ * with the LUT would leave FP32's exponent range by an exact power of two (the forward
+ * input as a whole, the adjoint input per voxel row) and scale the results back in FP64.
  */
 int cgb_op_apply(cgb_op *op, int adjoint, const void *in, int64_t in_len, void *out, int64_t out_len, int dtype,
                  int arith, void *stream);
@@ -164,16 +167,25 @@ int cgb_op_apply_host(cgb_op *op, int adjoint, const double *in, int64_t in_len,
  * elements sorted by voxel (as load_dictionary leaves them, commit/core.pyx:508-562),
  * the eval mask and the f32 LUTs, plus a fibre index computed once by the caller:
  * fib_perm[n] lists segment indices grouped by fibre and fib_ptr[nF+1] gives each
- * fibre's range (a stable argsort of ICf and its counts).  x (nF*nIC + nE*nEC +
- * nISOv*nISO doubles) is fully written.  Float-float arithmetic, as cgb_op_apply.
+ * fibre's range (a stable argsort of ICf and its counts).  ICf itself is not read (the
+ * fibre index replaces it) and may be NULL.  x (nF*nIC + nE*nEC + nISOv*nISO doubles) is
+ * fully written.  Float-float arithmetic with the range guard of cgb_op_apply.
  *
- * Working memory is a static device array of CGB_NOALLOC_MAX_TERMS doubles (8 MiB),
- * held by every GPU that loads the library until the process exits; calls with
- * n*nIC > CGB_NOALLOC_MAX_TERMS return CGB_ERR_UNSUPPORTED.  The first call on a device
- * looks up that array's device address (cudaGetSymbolAddress) with the device current;
- * make this first call before any stream capture.  All calls share the array: calls
- * whose work overlaps on the GPU (different streams, or different host threads) race and
- * must be serialised by the caller.  Enqueued on `stream`; returns without synchronising.
+ * Working memory is a static device array of CGB_NOALLOC_MAX_TERMS doubles (8 MiB) in
+ * this library's module; calls with n*nIC > CGB_NOALLOC_MAX_TERMS return
+ * CGB_ERR_UNSUPPORTED.  Under CUDA's lazy module loading (the default since CUDA 12.2) a
+ * module's static memory is allocated, and its kernels' code loaded, on first use, so
+ * the FIRST call on each device does that set-up, with the device current: it looks up
+ * the array's address (cudaGetSymbolAddress) and loads every kernel this entry point
+ * uses.  That first call may therefore allocate and synchronise: make it before
+ * reserving the device's memory and before any stream capture (or run with
+ * CUDA_MODULE_LOADING=EAGER).  A call with nS = 1, ndirs = 1, every other size 0 and any
+ * non-null y does only this set-up.  Later calls allocate and load nothing; the array
+ * then stays allocated on that device until the process exits.  The address is cached
+ * per device: after cudaDeviceReset on a device, do not call this entry point there.
+ * All calls share the array: calls whose work overlaps on the GPU (different streams, or
+ * different host threads) race and must be serialised by the caller.  Enqueued on
+ * `stream`; returns without synchronising.
  */
 #define CGB_NOALLOC_MAX_TERMS (1 << 20)
 int cgb_op_adjoint_noalloc(int nS, int ndirs, int nF, int64_t n, int nE, int nV, int nISOv, const double *y,
@@ -182,6 +194,26 @@ int cgb_op_adjoint_noalloc(int nS, int ndirs, int nF, int64_t n, int nE, int nV,
                            const uint32_t *ISOv, const float *lutIC, const float *lutEC, const float *lutISO,
                            int nIC, int nEC, int nISO, const uint32_t *fib_ptr, const uint32_t *fib_perm,
                            void *stream);
+
+/*
+ * Reduced-precision A*x with a BF16 LUT on the tensor cores (tcgen05): per tile of 128
+ * voxels the voxel-by-LUT-row coefficient matrix is built in shared memory, split into
+ * BF16 high and low parts and multiplied with the BF16 LUT into an FP32 accumulator in
+ * tensor memory.  mode 0 uses it whenever the operator's shape allows (nS <= 320, fewer
+ * than 2^26 columns), 1 keeps the CUDA-core kernels, 2 requires it (CGB_ERR_UNSUPPORTED
+ * when the shape does not allow it); a negative mode only reads.  *out (may be NULL)
+ * receives 1 when the tensor-core forward is in use.  The first use on a handle builds its
+ * tile-ordered entry stream and LUT images (about 6 bytes per item).  No counterpart in
+ * the reference (setup_operator.py:50-218 is its CPU A).
+ */
+int cgb_op_tensor_cores(cgb_op *op, int mode, int *out);
+
+/*
+ * Synchronises the handle's device and reports whether a tensor-core kernel gave up a
+ * bounded wait since the last check (CGB_ERR_CUDA; the kernel then returned early and its
+ * output is incomplete).  No counterpart in the reference.
+ */
+int cgb_op_device_status(cgb_op *op);
 
 /* ------------------------------------------------------------------ regularisation */
 #define CGB_REG_NONE 0

@@ -324,3 +324,56 @@ def test_float_float_voxel_shapes_match_golden(name):
         assert G.rel(x, f['x']) <= 1e-8
     assert G.rel(out[1][0], out[2][0]) <= 1e-13
     assert G.rel(out[1][1], out[2][1]) <= 1e-13
+
+
+@pytest.mark.parametrize('scale', [1e30, 1e-30, 1e45, 1e-45, 1e200, 1e-200])
+@pytest.mark.parametrize('arith', ['ff', 'f64'])
+@pytest.mark.parametrize('name', ['szb', 'multi_rf'])
+def test_range_guard_scaled_inputs(name, arith, scale):
+    """FP64 inputs far outside FP32's exponent range (the float-float words are FP32): the
+    kernels scale them by an exact power of two, so A(s x) and A'(s y) stay within the FP64
+    bar of the oracle run on the same scaled inputs, on host and device vectors."""
+    c = G.load_case(name)
+    A = _op(c, arith)
+    P = O.PortOperator(c['D'], c['K'], None)
+    xs, ys = c['x_in'] * scale, c['y_in'] * scale
+    ax, aty = P.dot(xs), P.T.dot(ys)
+    assert np.all(np.isfinite(ax)) and np.all(np.isfinite(aty))
+
+    def rel(a, b):  # on the unscaled magnitudes, so the norms themselves do not overflow
+        return G.rel(np.asarray(a) / scale, np.asarray(b) / scale)
+
+    assert rel(A.dot(xs), ax) <= TOL
+    assert rel(A.T.dot(ys), aty) <= TOL
+    assert rel(A.dot(torch.from_numpy(xs).cuda()).cpu().numpy(), ax) <= TOL
+    assert rel(A.T.dot(torch.from_numpy(ys).cuda()).cpu().numpy(), aty) <= TOL
+
+
+def test_range_guard_mixed_row_magnitudes():
+    """Rows of y spanning 1e-40 .. 1e40 (each voxel row is scaled on its own) and x mixing
+    1e40 and O(1) entries stay within the FP64 bar."""
+    c = G.load_case('szb')
+    A = _op(c)
+    P = O.PortOperator(c['D'], c['K'], None)
+    nS = c['K']['wmr'].shape[2]
+    rng = np.random.default_rng(7)
+    y = c['y_in'] * np.repeat(10.0 ** rng.choice([-40.0, 0.0, 40.0], size=c['y_in'].size // nS), nS)
+    x = c['x_in'] * np.where(rng.uniform(size=c['x_in'].size) < 0.5, 1e40, 1.0)
+    assert G.rel(A.T.dot(y), P.T.dot(y)) <= TOL
+    assert G.rel(A.dot(x), P.dot(x)) <= TOL
+
+
+def test_range_guard_in_fista():
+    """FISTA on y * 2^140 (beyond FP32's range) follows the unscaled solve: the iterates
+    scale exactly with the data (nnls, fixed iteration count)."""
+    from commit_gb300 import solvers
+    c = G.load_case('szb')
+    A = _op(c)
+    rp = O.reg_params(c['D'], c['K'])
+    s = 2.0 ** 140
+    kw = dict(tol_fun=0.0, tol_x=0.0, max_iter=30, verbose=0)
+    x1, d1 = solvers.solve(c['y_obs'], A, A.T, regularisation=solvers.init_regularisation(dict(rp)), **kw)
+    x2, d2 = solvers.solve(c['y_obs'] * s, A, A.T, regularisation=solvers.init_regularisation(dict(rp)), **kw)
+    assert d1['iterations'] == d2['iterations']
+    assert np.all(np.isfinite(x2))
+    assert G.rel(x2 / s, x1) <= 1e-8
