@@ -55,9 +55,11 @@ def parse():
     p.add_argument('--slabs', type=int, default=-1,
                    help='adjoint slab count (0 automatic, 1 off; default: the handle\'s own choice)')
     p.add_argument('--fista', action='store_true', help='FISTA time-to-tolerance, plain vs mixed + refinement')
-    p.add_argument('--fista-iters', type=int, default=1500)
-    p.add_argument('--fista-arith', default='bf16',
-                   help='comma-separated LUT formats of the reduced-precision phase (bf16, fp16, f32)')
+    p.add_argument('--fista-iters', type=int, default=3000, help='iterations of each plain arm')
+    p.add_argument('--mixed-iters', type=int, default=3000, help='reduced-precision iterations of a mixed arm')
+    p.add_argument('--refine-iters', type=int, default=1500, help='FP64 refinement iterations of a mixed arm')
+    p.add_argument('--xstar-iters', type=int, default=12000, help='cap on the iterations computing x*')
+    p.add_argument('--xstar-chunk', type=int, default=1000, help='iterations per warm-started chunk of x*')
     p.add_argument('--demo', action='store_true',
                    help='demo-scale case (5k streamlines, nS=66): A*x, A\'y and 200 FISTA nnls iterations, '
                         'host-driven loop vs graph-captured loop, next to the reference CPU operator')
@@ -497,9 +499,16 @@ def run_ours(args):
 
 
 def run_fista(args, spec, D, K, dev):
-    """FISTA time-to-tolerance (nnls on all compartments): plain FP64-accurate solver vs
-    reduced precision (BF16 LUT) followed by FP64 refinement, both measured against a
-    reference solution from a 4x longer plain solve.  Prints one JSON line."""
+    """FISTA time-to-tolerance at the 1M-streamline workload (nnls on all compartments).
+
+    x*: the FP64-accurate (float-float) solver with function-value momentum restart, run in
+    chunks warm-started from each other until a chunk changes x by less than 1e-9 relative
+    (or --xstar-iters iterations); the last chunk's change is reported as x*'s own accuracy.
+    Arms, each traced against x* (|x_k - x*| / |x*| per accepted iteration, seconds from
+    the start of the solve): the plain FP64-accurate solver as the reference runs it (no
+    restart), the same with restart, and reduced precision + FP64 refinement with restart:
+    BF16 LUT on the tensor cores, and FP32 LUT on the CUDA cores.  Also the relative errors
+    of y = A x*, of the arms' x and of their cost against FP64.  Prints one JSON line."""
     import torch
     from commit_gb300 import solvers, synth
     from commit_gb300.operator import LinearOperator
@@ -512,42 +521,76 @@ def run_fista(args, spec, D, K, dev):
           'regIC': None, 'regEC': None, 'regISO': None, 'nnIC': True, 'nnEC': True, 'nnISO': True,
           'dictIC_params': None, 'dictEC_params': None, 'dictISO_params': None}
     reg = lambda: solvers.init_regularisation(dict(rp))  # noqa: E731
-    n = args.fista_iters
+    rel = lambda a, b: float(torch.linalg.norm(a - b) / torch.linalg.norm(b))  # noqa: E731
+    # ---- x*: restarted FP64-accurate FISTA in warm-started chunks
     t0 = time.perf_counter()
-    x_ref, d_ref = solvers.solve(y, A, A.T, tol_fun=0.0, tol_x=0.0, max_iter=4 * n, verbose=0, regularisation=reg())
-    t_ref = time.perf_counter() - t0
-    _, d_plain = solvers.solve(y, A, A.T, tol_fun=0.0, tol_x=0.0, max_iter=n, verbose=0, regularisation=reg(),
-                               x_ref=x_ref)
+    x = torch.zeros(A.nCOLS, dtype=torch.float64, device=dev)
+    chunks, done, change = [], 0, None
+    while done < args.xstar_iters:
+        xn, d = solvers.solve(y, A, A.T, tol_fun=1e-15, tol_x=0.0, max_iter=args.xstar_chunk, verbose=0, x0=x,
+                              regularisation=reg(), restart=True)
+        change = rel(xn, x) if done else 1.0
+        x = xn
+        done += d['iterations']
+        chunks.append({'iterations': done, 'change': change, 'cost': d['cost_function'],
+                       'criterion': d['stopping_criterion']})
+        print(json.dumps({'xstar_chunk': chunks[-1]}), file=sys.stderr, flush=True)
+        if change < 1e-9:
+            break
+    x_star = x
+    t_star = time.perf_counter() - t0
+    cost_star = chunks[-1]['cost']
+
     def first_below(tr, tol):
         idx = np.flatnonzero(tr[:, 1] <= tol)
         return (float(tr[idx[0], 0]), int(idx[0]) + 1) if idx.size else (None, None)
 
-    tr_p = d_plain['trace']
-    n_mix = (3 * n) // 4
-    mixed = {}
-    for ar in [a.strip() for a in args.fista_arith.split(',') if a.strip()]:
-        # warm the reduced-precision LUT copies (one-time) before timing the mixed solve
-        A.dot(torch.zeros(A.nCOLS, dtype=torch.float32, device=dev), arith=ar)
-        _, d_mix = solvers.solve_mixed(y, A, tol_fun=0.0, tol_x=0.0, max_iter=n_mix, verbose=0,
-                                       regularisation=reg(), arith=ar, refine_max_iter=n - n_mix, x_ref=x_ref)
-        tr_m = d_mix['trace']
-        res = {}
-        for tol in (1e-2, 1e-3, 1e-4):
-            tp, ip = first_below(tr_p, tol)
-            tm, im = first_below(tr_m, tol)
-            res[f'{tol:g}'] = {'plain_s': tp, 'plain_iter': ip, 'mixed_s': tm, 'mixed_iter': im,
-                               'speedup': (tp / tm) if (tp and tm) else None}
-        mixed[ar] = {'iterations': int(d_mix['iterations']), 'mixed_iterations': n_mix,
-                     'seconds': float(tr_m[-1, 0]),
-                     'ms_per_mixed_iteration': 1000.0 * float(d_mix['mixed']['trace'][-1, 0]) / n_mix,
-                     'final_rel': float(tr_m[-1, 1]), 'time_to_tol': res}
-    out = {'metric': 'FISTA time-to-tolerance, plain (float-float FP64) vs reduced-precision LUT + FP64 refinement',
+    def summary(det, phases=None):
+        tr = det['trace']
+        out = {'iterations': int(det['iterations']), 'seconds': float(tr[-1, 0]), 'final_rel': float(tr[-1, 1]),
+               'cost_rel': abs(det['cost_function'] - cost_star) / cost_star,
+               'time_to': {f'{tol:g}': dict(zip(('seconds', 'iteration'), first_below(tr, tol)))
+                           for tol in (1e-2, 1e-3, 1e-4)}}
+        if phases:
+            out.update(phases)
+        return out
+
+    arms = {}
+    n = args.fista_iters
+    _, d = solvers.solve(y, A, A.T, tol_fun=0.0, tol_x=0.0, max_iter=n, verbose=0, regularisation=reg(), x_ref=x_star)
+    arms['plain'] = summary(d)
+    arms['plain']['ms_per_iteration'] = 1000.0 * arms['plain']['seconds'] / len(d['trace'])
+    _, d = solvers.solve(y, A, A.T, tol_fun=0.0, tol_x=0.0, max_iter=n, verbose=0, regularisation=reg(), x_ref=x_star,
+                         restart=True)
+    arms['plain_restart'] = summary(d)
+    arms['plain_restart']['ms_per_iteration'] = 1000.0 * arms['plain_restart']['seconds'] / len(d['trace'])
+    n1, n2 = args.mixed_iters, args.refine_iters
+    y_errors = {}
+    yf = A.dot(x_star)
+    for name, ar, tcm in (('bf16_tensor_cores', 'bf16', 2), ('f32_lut', 'f32', 1)):
+        if tcm == 2 and not A.tensor_cores(0):
+            continue
+        A.tensor_cores(tcm)
+        y_errors[name] = rel(A.dot(x_star.float(), arith=ar).double(), yf)
+        xm, dm = solvers.solve_mixed(y, A, tol_fun=0.0, tol_x=0.0, max_iter=n1, verbose=0, regularisation=reg(),
+                                     arith=ar, refine_max_iter=n2, x_ref=x_star, restart=True)
+        mix = dm['mixed']['trace']
+        arms[name + '_refined'] = summary(dm, {
+            'reduced_iterations': n1, 'refine_iterations': n2,
+            'ms_per_reduced_iteration': 1000.0 * float(mix[-1, 0]) / len(mix),
+            'reduced_phase_final_rel': float(mix[-1, 1])})
+    A.tensor_cores(1)
+    plain_t = {k: v['seconds'] for k, v in arms['plain']['time_to'].items()}
+    for k, v in arms.items():
+        v['speedup_vs_plain'] = {t: (plain_t[t] / v['time_to'][t]['seconds']
+                                     if plain_t[t] and v['time_to'][t]['seconds'] else None) for t in plain_t}
+    out = {'metric': 'FISTA time-to-tolerance |x_k - x*|/|x*| (1M-streamline workload, nnls)',
            'unit': 's', 'higher_is_better': False, 'data': 'synthetic',
-           'config': workload_config(spec, D, K, args) | {'regulariser': 'nnls (all compartments)',
-                                                           'reference': f'plain FISTA, {4 * n} iterations'},
-           'plain': {'iterations': int(d_plain['iterations']), 'seconds': float(tr_p[-1, 0]),
-                     'ms_per_iteration': 1000.0 * float(tr_p[-1, 0]) / len(tr_p), 'final_rel': float(tr_p[-1, 1])},
-           'mixed': mixed, 'reference_solve_s': t_ref}
+           'config': workload_config(spec, D, K, args) | {'regulariser': 'nnls (all compartments)'},
+           'x_star': {'method': 'float-float FISTA with function-value restart, warm-started chunks',
+                      'iterations': done, 'seconds': t_star, 'last_chunk_change': change, 'cost': cost_star,
+                      'chunks': chunks[-5:]},
+           'arms': arms, 'y_rel_error_vs_fp64': y_errors}
     if not args.no_cpu:
         out['cpu_baseline'] = cpu_reference_fista(D, K, args.sample_frac, 5)
     print(json.dumps(out))

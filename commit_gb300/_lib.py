@@ -11,7 +11,7 @@ import os
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, 'libcommit_gb300.so')
 
-CGB_OK, CGB_ERR_INVALID, CGB_ERR_CUDA, CGB_ERR_NOMEM, CGB_ERR_UNSUPPORTED, CGB_ERR_DIMENSION = range(6)
+CGB_OK, CGB_ERR_INVALID, CGB_ERR_CUDA, CGB_ERR_NOMEM, CGB_ERR_UNSUPPORTED, CGB_ERR_DIMENSION, CGB_ERR_BACKTRACK = range(7)
 ARITH = {'f64': 0, 'ff': 1, 'bf16': 2, 'fp16': 3, 'f32': 4}
 DTYPE_F64, DTYPE_F32 = 0, 1
 REG = {None: 0, 'lasso': 1, 'group_lasso': 2, 'sparse_group_lasso': 3}
@@ -36,7 +36,7 @@ class CgbReg(ctypes.Structure):
 class CgbFistaParams(ctypes.Structure):
     _fields_ = [('tol_fun', c_f64), ('tol_x', c_f64), ('max_iter', c_i32), ('verbose', c_i32),
                 ('arith', c_i32), ('momentum_reuse', c_i32), ('x_ref', c_vp), ('trace', c_vp), ('trace_len', c_i32),
-                ('graph', c_i32)]
+                ('graph', c_i32), ('max_backtracks', c_i32), ('restart', c_i32)]
 
 
 class CgbFistaResult(ctypes.Structure):
@@ -99,6 +99,8 @@ def lib() -> ctypes.CDLL:
                                       ctypes.POINTER(c_vp), ctypes.POINTER(CgbFistaResult), P]
     L.cgb_op_host_mode.argtypes = [P, c_i32, ctypes.POINTER(c_i32)]
     L.cgb_op_tensor_cores.argtypes = [P, c_i32, ctypes.POINTER(c_i32)]
+    L.cgb_dict_relayout.argtypes = [P, c_i64, c_i64, c_i32, P, P, P, P, P, c_i32, c_i64, P, P, c_i64, P,
+                                    ctypes.POINTER(c_i64), P]
     L.cgb_op_device_status.argtypes = [P]
     L.cgb_op_ff_shape.argtypes = [P, c_i32, ctypes.POINTER(c_i32), ctypes.POINTER(c_i32)]
     L.cgb_op_ff_kernels.argtypes = [P, c_i32, ctypes.POINTER(c_i32)]

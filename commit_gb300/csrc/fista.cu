@@ -258,6 +258,7 @@ struct GState {
     double group_coef;
     int nterms, group_in_omega;
     int it, crit, backtracks, max_iter;
+    int bt_iter, max_bt;  // backtracks of the current iteration and their cap
 };
 
 __device__ __forceinline__ double g_omega(const GState &S, const double *h) {
@@ -271,6 +272,7 @@ __device__ __forceinline__ double g_omega(const GState &S, const double *h) {
 __global__ void k_ctl_begin(GState *S, const double *h) {
     const double r = __dsqrt_rn(h[12]);
     S->qfval = S->it == 1 ? S->prev_obj : __dmul_rn(__dmul_rn(0.5, r), r);
+    S->bt_iter = 0;
 }
 
 // objective and quadratic model of the evaluated x (solvers.py:315-333); on failure of the
@@ -285,9 +287,13 @@ __global__ void k_ctl_judge(GState *S, const double *h, cudaGraphConditionalHand
     S->reg_x = reg;
     S->res_norm = rn;
     S->curr_obj = cur;
-    if (cur > q) {
+    if (cur > q && S->bt_iter >= S->max_bt) {
+        S->crit = -1;  // cap reached: leave the backtracking loop, k_ctl_stop ends the solve
+        cudaGraphSetConditional(bt, 0);
+    } else if (cur > q) {
         S->step = __dmul_rn(0.9, S->step);
         S->backtracks += 1;
+        S->bt_iter += 1;
         cudaGraphSetConditional(bt, 1);
     } else {
         cudaGraphSetConditional(bt, 0);
@@ -297,6 +303,11 @@ __global__ void k_ctl_judge(GState *S, const double *h, cudaGraphConditionalHand
 // stopping tests (solvers.py:335-357) and the FISTA coefficients (solvers.py:359-368)
 __global__ void k_ctl_stop(GState *S, const double *h, cudaGraphConditionalHandle hmain,
                            cudaGraphConditionalHandle hcont) {
+    if (S->crit == -1) {
+        cudaGraphSetConditional(hmain, 0);
+        cudaGraphSetConditional(hcont, 0);
+        return;
+    }
     const double eps = 2.220446049250313e-16;
     const double a = fabs(__dsub_rn(S->curr_obj, S->prev_obj));
     S->abs_obj = a;
@@ -356,6 +367,91 @@ __global__ void k_momentum_dev(double *__restrict__ xh, const double *__restrict
     }
 }
 
+// One elementwise pass of an evaluation of x (regularisers without groups): optionally the
+// deferred momentum of the iteration (xhat = x + c*(x - prev), prev = x, exactly as
+// k_momentum), then x = prox(xhat - a*grad) (k_prox_elem / k_prox_elem_dev) and the
+// statistics of k_stats, with the fixed-order final sums of k_finalize done by the last
+// block to finish (out[0..9]; out[10], the group penalty, is 0).  Same expressions and the
+// same summation order as the separate kernels, so the iterates are bitwise the same.
+template <bool DEV>
+__global__ void k_prox_stats(double *__restrict__ x, double *__restrict__ xh, const double *__restrict__ g,
+                             double *__restrict__ p, double a, RegDev R, int64_t n, int mom, double c,
+                             const GState *__restrict__ S, L1Terms T, const double *__restrict__ xref,
+                             double *__restrict__ partials, unsigned int *__restrict__ counter,
+                             double *__restrict__ out) {
+    if (DEV) {
+        const double s = S->step;
+        a = s;
+        R.lam_ic = __dmul_rn(s, R.lam_ic);
+        R.lam_ec = __dmul_rn(s, R.lam_ec);
+        R.lam_iso = __dmul_rn(s, R.lam_iso);
+    }
+    double v[kStatSlots] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double xhi, pi;
+        if (mom) {
+            const double xo = x[i];
+            xhi = __dadd_rn(xo, __dmul_rn(c, __dsub_rn(xo, p[i])));
+            xh[i] = xhi;
+            p[i] = xo;
+            pi = xo;
+        } else {
+            xhi = xh[i];
+            pi = p[i];
+        }
+        const double gi = g[i];
+        double w = __dsub_rn(xhi, __dmul_rn(a, gi));
+        if (i >= R.sISO && i < R.sISO + R.nISO) {
+            if (R.reg_iso == CGB_REG_LASSO) w = soft(w, R.weighted_iso ? R.w[i] * R.lam_iso : R.lam_iso);
+            if (R.nn_iso && w <= 0.0) w = 0.0;
+        } else if (i >= R.sEC && i < R.sEC + R.nEC) {
+            if (R.reg_ec == CGB_REG_LASSO) w = soft(w, R.lam_ec);
+            if (R.nn_ec && w <= 0.0) w = 0.0;
+        } else if (i >= R.sIC && i < R.sIC + R.nIC) {
+            if (R.reg_ic == CGB_REG_LASSO || R.reg_ic == CGB_REG_SPARSE_GROUP_LASSO)
+                w = soft(w, R.weighted_ic ? R.w[i] * R.lam_ic : R.lam_ic);
+            if (R.nn_ic && (R.reg_ic == CGB_REG_NONE || R.reg_ic == CGB_REG_LASSO) && w <= 0.0) w = 0.0;
+        }
+        x[i] = w;
+        const double d = w - xhi;
+        v[0] = fma(d, gi, v[0]);
+        v[1] = fma(d, d, v[1]);
+        const double e = w - pi;
+        v[2] = fma(e, e, v[2]);
+        v[3] = fma(w, w, v[3]);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k < T.n && i >= T.t[k].a && i < T.t[k].b) v[4 + k] += fabs(T.t[k].w ? T.t[k].w[i] * w : w);
+        if (xref) {
+            const double r = xref[i];
+            const double dd = w - r;
+            v[8] = fma(dd, dd, v[8]);
+            v[9] = fma(r, r, v[9]);
+        }
+    }
+    block_sum_store_n<kStatSlots>(v, partials + (size_t)blockIdx.x * kRedSlots);
+    // the last block to finish forms the final sums, in k_finalize's order
+    __shared__ unsigned int is_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) is_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    for (int j = 0; j < kStatSlots; ++j) {
+        double t[1] = {0.0};
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) t[0] += __ldcg(partials + (size_t)b * kRedSlots + j);
+        double tot[1];
+        block_sum_store_n<1>(t, tot);
+        if (threadIdx.x == 0) out[j] = tot[0];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[kStatSlots] = 0.0;
+        *counter = 0u;
+    }
+}
+
 // lam = lam_base * step for the group prox of the graph (the host path passes it directly)
 __global__ void k_scale_lam(const GState *__restrict__ S, double lam_base, double *__restrict__ out) {
     *out = __dmul_rn(S->step, lam_base);
@@ -368,11 +464,12 @@ struct FistaWS {
     int64_t ncols = 0, nrows = 0;
     double *xhat = nullptr, *prev = nullptr, *grad = nullptr, *ax[2] = {nullptr, nullptr};
     double *pstats = nullptr, *pgrp = nullptr, *pres = nullptr;
+    unsigned int *counter = nullptr;  // arrival counter of the fused elementwise pass (k_prox_stats)
     // reduced-precision path: FP32 copies of y and sqrt(W), FP32 A*x buffers
     float *y32 = nullptr, *sqw32 = nullptr, *ax32[2] = {nullptr, nullptr};
     cudaStream_t st = nullptr;  // allocations are stream-ordered on the solver's stream
     ~FistaWS() {
-        void *ps[] = {xhat, prev, grad, ax[0], ax[1], pstats, pgrp, pres, y32, sqw32, ax32[0], ax32[1]};
+        void *ps[] = {xhat, prev, grad, ax[0], ax[1], pstats, pgrp, pres, y32, sqw32, ax32[0], ax32[1], counter};
         for (void *p : ps)
             if (p) cudaFreeAsync(p, st);
     }
@@ -398,6 +495,7 @@ struct Solver {
     L1Terms terms;
     double l1coef[4];
     int has_group_prox = 0, group_in_omega = 0;
+    int fused_elem = 0;  // regulariser without groups: one fused elementwise pass per evaluation
     double group_omega_coef = 0.0;
     int calls = 0;
 
@@ -476,6 +574,27 @@ struct Solver {
         }
         if ((R.weighted_ic || R.weighted_iso) && !R.coeff_weights)
             return fail(CGB_ERR_INVALID, "weighted regulariser without coeff_weights");
+        const bool grp = R.reg_ic == CGB_REG_GROUP_LASSO || R.reg_ic == CGB_REG_SPARSE_GROUP_LASSO;
+        fused_elem = nc > 0 && !has_group_prox && !group_in_omega && !grp;
+        if (fused_elem) {
+            CGB_TRY(ws_alloc(&ws.counter, 1, st));
+            CGB_CUDA(cudaMemsetAsync(ws.counter, 0, sizeof(unsigned int), st));
+        }
+        return CGB_OK;
+    }
+
+    // x = prox(xhat - a*grad) and its statistics in one pass (fused_elem); mom: apply the
+    // iteration's deferred momentum with coefficient c first
+    int prox_stats(double *x, double a, int mom, double c) {
+        const int64_t nc = op->ncols;
+        const int gb = elem_grid(op, nc);
+        if (gdev)
+            k_prox_stats<true><<<gb, kBlock, 0, st>>>(x, ws.xhat, ws.grad, ws.prev, 0.0, regdev(1.0), nc, 0, 0.0, gdev,
+                                                      terms, prm->x_ref, ws.pstats, ws.counter, dsc + 1);
+        else
+            k_prox_stats<false><<<gb, kBlock, 0, st>>>(x, ws.xhat, ws.grad, ws.prev, a, regdev(a), nc, mom, c, nullptr,
+                                                       terms, prm->x_ref, ws.pstats, ws.counter, dsc + 1);
+        CGB_CUDA(cudaGetLastError());
         return CGB_OK;
     }
 
@@ -605,6 +724,7 @@ struct Solver {
     }
 
     int run(double *x, cgb_fista_result *res) {
+        const int max_bt = prm->max_backtracks > 0 ? prm->max_backtracks : (prm->max_backtracks < 0 ? 0 : 1000);
         const int64_t nc = op->ncols;
         const double eps = 2.220446049250313e-16;
         double *h = op->h_scal;
@@ -657,11 +777,18 @@ struct Solver {
         int have_prev_ax = 0; // ax[1-cur] holds A*prev_x
         double curr_obj = 0, reg_term_x = 0, abs_obj = 0, rel_obj = 0, abs_x = 0, rel_x = 0;
         int crit = 4;
+        int pend_mom = 0;     // momentum deferred into the next evaluation's fused pass
+        double pend_c = 0.0;
         while (true) {
             NvtxRange nvi("fista iteration");
             auto eval_x = [&](double s) -> int {
-                CGB_TRY(prox(x, ws.xhat, ws.grad, s, s));
-                CGB_TRY(stats(x, ws.xhat, ws.grad, ws.prev));
+                if (fused_elem) {
+                    CGB_TRY(prox_stats(x, s, pend_mom, pend_c));
+                    pend_mom = 0;
+                } else {
+                    CGB_TRY(prox(x, ws.xhat, ws.grad, s, s));
+                    CGB_TRY(stats(x, ws.xhat, ws.grad, ws.prev));
+                }
                 CGB_TRY(objective(x, prm->momentum_reuse ? cur : -1));
                 return fetch(h);
             };
@@ -672,7 +799,12 @@ struct Solver {
             double q = qfval + h[1] + 0.5 / step * (sqrt(h[2]) * sqrt(h[2])) + reg_term_x;
             res_norm = sqrt(h[0]);
             curr_obj = 0.5 * res_norm * res_norm + reg_term_x;
+            int bt_iter = 0;
             while (curr_obj > q) {
+                if (bt_iter >= max_bt)
+                    return fail(CGB_ERR_BACKTRACK, "FISTA: backtracking of iteration " + std::to_string(it) +
+                                                       " reached its cap of " + std::to_string(max_bt) + " step reductions");
+                ++bt_iter;
                 step = beta * step;
                 backtracks++;
                 CGB_TRY(eval_x(step));
@@ -697,15 +829,25 @@ struct Solver {
             if (abs_x < eps) { crit = 2; break; }
             if (rel_x < prm->tol_x) { crit = 3; break; }
             if (it >= prm->max_iter) { crit = 4; break; }
-            // FISTA update (solvers.py:359-368)
+            // FISTA update (solvers.py:359-368); with restart, a rise of the objective resets
+            // the momentum
+            if (prm->restart && curr_obj > prev_obj) told = 1.0;
             const double t = 0.5 * (1.0 + sqrt(1.0 + 4.0 * told * told));
             const double c = (told - 1.0) / t;
-            k_momentum<<<elem_grid(op, nc), kBlock, 0, st>>>(ws.xhat, x, ws.prev, c, nc);
-            CGB_CUDA(cudaGetLastError());
             if (prm->momentum_reuse && (c == 0.0 || have_prev_ax)) {
-                // A*xhat = (1+c) A*x - c A*prev_x
+                // A*xhat = (1+c) A*x - c A*prev_x: the gradient does not read xhat, so with a
+                // fused elementwise pass the momentum itself waits for the next evaluation
+                if (fused_elem) {
+                    pend_mom = 1;
+                    pend_c = c;
+                } else {
+                    k_momentum<<<elem_grid(op, nc), kBlock, 0, st>>>(ws.xhat, x, ws.prev, c, nc);
+                    CGB_CUDA(cudaGetLastError());
+                }
                 CGB_TRY(gradient(ws.xhat, ws.grad, cur, have_prev_ax ? 1 - cur : cur, 1.0 + c, -c));
             } else {
+                k_momentum<<<elem_grid(op, nc), kBlock, 0, st>>>(ws.xhat, x, ws.prev, c, nc);
+                CGB_CUDA(cudaGetLastError());
                 CGB_TRY(gradient(ws.xhat, ws.grad, -1, -1, 0.0, 0.0));
             }
             if (prm->momentum_reuse) {
@@ -740,8 +882,12 @@ struct Solver {
     // --------------------------------------------------------------- graph mode
     // One evaluation of x = prox(xhat - step*grad) with its statistics and objective.
     int eval_dev(double *x) {
-        CGB_TRY(prox(x, ws.xhat, ws.grad, 0.0, 0.0));
-        CGB_TRY(stats(x, ws.xhat, ws.grad, ws.prev));
+        if (fused_elem) {
+            CGB_TRY(prox_stats(x, 0.0, 0, 0.0));
+        } else {
+            CGB_TRY(prox(x, ws.xhat, ws.grad, 0.0, 0.0));
+            CGB_TRY(stats(x, ws.xhat, ws.grad, ws.prev));
+        }
         return objective(x, -1);
     }
 
@@ -822,6 +968,7 @@ struct Solver {
         G.it = 1;
         G.crit = 4;
         G.max_iter = prm->max_iter;
+        G.max_bt = prm->max_backtracks > 0 ? prm->max_backtracks : (prm->max_backtracks < 0 ? 0 : 1000);
         GState *gs = nullptr;
         CGB_TRY(ws_alloc(&gs, 1, st));
         CGB_TRY(ws_alloc(&glam, 1, st));
@@ -901,6 +1048,9 @@ struct Solver {
         cudaFreeAsync(glam, st);
         glam = nullptr;
         CGB_TRY(rc);
+        if (G.crit == -1)
+            return fail(CGB_ERR_BACKTRACK, "FISTA (graph): backtracking of iteration " + std::to_string(G.it) +
+                                               " reached its cap of " + std::to_string(G.max_bt) + " step reductions");
         res->residual = 0.5 * G.res_norm * G.res_norm;
         res->regterm = G.reg_x;
         res->cost_function = G.curr_obj;
@@ -1383,8 +1533,9 @@ int cgb_fista_run(cgb_op *op, const double *y, const double *sqrt_w, const cgb_r
     if ((reg->reg_ic == CGB_REG_GROUP_LASSO || reg->reg_ic == CGB_REG_SPARSE_GROUP_LASSO) && reg->ngroups > 0 &&
         (!reg->level_ptr || reg->nlevels < 1))
         return fail(CGB_ERR_INVALID, "group regulariser needs a level schedule");
-    if (params->graph && (params->momentum_reuse || (params->trace && params->x_ref) || params->verbose == 4))
-        return fail(CGB_ERR_UNSUPPORTED, "graph mode runs without momentum reuse, trace or verbose output");
+    if (params->graph && (params->momentum_reuse || (params->trace && params->x_ref) || params->verbose == 4 ||
+                          params->restart))
+        return fail(CGB_ERR_UNSUPPORTED, "graph mode runs without momentum reuse, restart, trace or verbose output");
     NvtxRange nv("cgb_fista_run");
     DevGuard g(op->device);
     Solver S;

@@ -100,7 +100,7 @@ int dalloc(cgb_op *op, T **p, size_t count) {
 template <class T>
 int upload(T *dst, const T *src, size_t count) {
     if (count == 0 || src == nullptr) return CGB_OK;
-    CGB_CUDA(cudaMemcpy(dst, src, count * sizeof(T), cudaMemcpyHostToDevice));
+    CGB_CUDA(cudaMemcpy(dst, src, count * sizeof(T), cudaMemcpyDefault));  // host or device source
     return CGB_OK;
 }
 
@@ -383,11 +383,11 @@ static int create_impl(int device, int nS, int ndirs, int nF, int64_t n, int nE,
         CGB_CUDA(cudaMemset(op->lutISO_p, 0, padded((size_t)nISO)));
         if (!nolut) {
             if (lutIC_n) CGB_CUDA(cudaMemcpy2D(op->lutIC_p, sp * sizeof(float), lutIC, nS * sizeof(float),
-                                               nS * sizeof(float), (size_t)nIC * op->ndirs, cudaMemcpyHostToDevice));
+                                               nS * sizeof(float), (size_t)nIC * op->ndirs, cudaMemcpyDefault));
             if (lutEC_n) CGB_CUDA(cudaMemcpy2D(op->lutEC_p, sp * sizeof(float), lutEC, nS * sizeof(float),
-                                               nS * sizeof(float), (size_t)nEC * op->ndirs, cudaMemcpyHostToDevice));
+                                               nS * sizeof(float), (size_t)nEC * op->ndirs, cudaMemcpyDefault));
             if (lutISO_n) CGB_CUDA(cudaMemcpy2D(op->lutISO_p, sp * sizeof(float), lutISO, nS * sizeof(float),
-                                                nS * sizeof(float), (size_t)nISO, cudaMemcpyHostToDevice));
+                                                nS * sizeof(float), (size_t)nISO, cudaMemcpyDefault));
         }
     }
     CGB_TRY(dalloc(op, &op->eval, (size_t)nF * (nIC > 0 ? nIC : 1)));

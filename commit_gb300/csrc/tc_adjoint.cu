@@ -16,7 +16,8 @@
 //
 // Warp roles (256 threads, one CTA per SM): all threads load and split Z; warp 4's first
 // lane fetches the LUT row images (bulk copies, 2 stages) and issues the MMAs; warps 0-3
-// (one per TMEM lane quarter) drain the accumulators.  Every wait is bounded (tc_ptx.cuh).
+// (one per TMEM lane quarter) drain the accumulators, 64 LUT rows (one K-block) at a time.
+// Every wait is bounded (tc_ptx.cuh).
 #include <cub/cub.cuh>
 
 #include "operator_launch.cuh"
@@ -31,7 +32,7 @@ constexpr int kATile = 128;
 constexpr int kARows = 256;         // LUT rows per round (one TMEM half)
 constexpr int kANh = 128;           // LUT rows per MMA (N)
 constexpr int kAMaxKBS = 5;         // sample K-blocks of 64: nS <= 320
-constexpr int kADrainStride = 33;   // floats per drain staging row
+constexpr int kADrainStride = 65;   // floats per drain staging row (64 columns + padding)
 constexpr uint32_t kAColBits = 26;
 
 struct TcAdjArgs {
@@ -220,23 +221,24 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
                     uint32_t j = A.ent_ptr[pb];
                     const uint32_t p1 = A.ent_ptr[pb + 1];
                     const float lsc = kbf < A.kb_ec ? A.l_scale : 1.f;
+                    // the K-block's 64 columns of this voxel into its private row; the items
+                    // of the K-block may come in any row order (EC items keep their file order)
+                    __syncwarp();
+#pragma unroll
                     for (int c = 0; c < 2; ++c) {
-                        __syncwarp();
                         float g[32];
                         tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (rg & 1u) * kARows + (uint32_t)(kbl * 64 + c * 32),
                                   g);
 #pragma unroll
-                        for (int i = 0; i < 32; ++i) row[i] = g[i];
-                        const uint32_t lim = (uint32_t)(c + 1) * 32u;
-                        while (j < p1) {
-                            const uint32_t co = A.ent_co[j];
-                            const uint32_t o = co >> kAColBits;
-                            if (o >= lim) break;
-                            const float t = row[o - (uint32_t)c * 32u] * (__half2float(A.ent_l[j]) * lsc);
-                            if (kbf < A.kb_ec) A.terms[j] = t;
-                            else A.xout[co & ((1u << kAColBits) - 1u)] = (double)t;
-                            ++j;
-                        }
+                        for (int i = 0; i < 32; ++i) row[c * 32 + i] = g[i];
+                    }
+                    for (; j < p1; ++j) {
+                        const uint32_t co = A.ent_co[j];
+                        const uint32_t o = co >> kAColBits;
+                        if (o >= 64u) continue;  // not produced by the layout; never indexes outside the row
+                        const float t = row[o] * (__half2float(A.ent_l[j]) * lsc);
+                        if (kbf < A.kb_ec) A.terms[j] = t;
+                        else A.xout[co & ((1u << kAColBits) - 1u)] = (double)t;
                     }
                 }
                 tc::tc_fence_before();

@@ -19,13 +19,25 @@ from . import _lib
 from ._lib import check, lib
 
 
-def _host(a, dtype) -> np.ndarray:
+def _host(a, dtype):
+    """A contiguous array of `dtype`: numpy for host data; a CUDA tensor of the same width
+    (its bits) stays on the device (cgb_op_create takes device pointers as well)."""
+    if isinstance(a, torch.Tensor) and a.is_cuda:
+        if a.element_size() != np.dtype(dtype).itemsize:
+            raise TypeError(f'CUDA dictionary array of element size {a.element_size()}, expected {np.dtype(dtype)}')
+        return a.contiguous()
     a = np.ascontiguousarray(np.asarray(a, dtype=dtype))
     return a
 
 
-def _ptr(a: np.ndarray):
+def _ptr(a):
+    if isinstance(a, torch.Tensor):
+        return ctypes.c_void_p(a.data_ptr()) if a.numel() else None
     return a.ctypes.data_as(ctypes.c_void_p) if a.size else None
+
+
+def _size(a) -> int:
+    return int(a.numel()) if isinstance(a, torch.Tensor) else int(a.size)
 
 
 class _Handle:
@@ -85,7 +97,7 @@ class LinearOperator:
         ln = _host(IC['len'], np.float32)
         ev = IC.get('eval')
         ev = _host(ev if ev is not None else np.ones(self.ICnSTR * self.ICnRF, np.uint32), np.uint32)
-        if ev.size < self.ICnSTR * self.ICnRF:
+        if _size(ev) < self.ICnSTR * self.ICnRF:
             raise ValueError('DICTIONARY["IC"]["eval"] is shorter than nSTR * nIC')
         ecv = _host(EC['vox'], np.uint32)
         eco = _host(EC['dir'], np.uint16)
@@ -93,9 +105,9 @@ class LinearOperator:
         lic = _host(KERNELS['wmr'], np.float32)
         lec = _host(KERNELS['wmh'], np.float32)
         liso = _host(KERNELS['iso'], np.float32)
-        if f.size != self.ICn or v.size != self.ICn or ln.size != self.ICn or (not nolut and o.size != self.ICn):
+        if _size(f) != self.ICn or _size(v) != self.ICn or _size(ln) != self.ICn or (not nolut and _size(o) != self.ICn):
             raise ValueError('IC arrays do not match DICTIONARY["IC"]["n"]')
-        if ecv.size != self.ECn or isov.size != self.ISOn:
+        if _size(ecv) != self.ECn or _size(isov) != self.ISOn:
             raise ValueError('EC/ISO arrays do not match their "n"')
         out = ctypes.c_void_p()
         check(lib().cgb_op_create(self.device, self.nSAMPLES, max(self.ndirs, 1), self.ICnSTR, self.ICn, self.ECn,

@@ -204,12 +204,17 @@ def evaluate_model(y, A, x, regularisation=None):
 
 
 def solve(y, A, At, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, verbose=True, x0=None, regularisation=None,
-          confidence_array=None, arith=None, momentum_reuse=True, x_ref=None, graph=False):
+          confidence_array=None, arith=None, momentum_reuse=True, x_ref=None, graph=False, max_backtracks=0,
+          restart=False):
     """solvers.py:218-241: regularised least squares by FISTA, on the GPU.
 
     graph=True runs the iteration loop as one CUDA graph launch whose backtracking and
     stopping decisions are taken on the device (conditional graph nodes); it implies
-    momentum_reuse=False and takes no x_ref / verbose output."""
+    momentum_reuse=False and takes no x_ref / verbose output.  max_backtracks caps the step
+    reductions of one iteration (0: 1000, negative: none); reaching the cap raises CgbError (the
+    reference's backtracking loop has no cap, solvers.py:322-333).  restart=True resets the
+    momentum after an iteration whose objective rose (function-value restart; not in the
+    reference, whose FISTA never restarts: solvers.py:359-368)."""
     if regularisation is None:
         spec = _no_reg_spec(A.shape[1])
     else:
@@ -222,7 +227,8 @@ def solve(y, A, At, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, verbose=True, x0=No
             else torch.sqrt(confidence_array)
     if graph:
         momentum_reuse = False
-    return _fista(y, A, spec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, arith, momentum_reuse, x_ref, graph)
+    return _fista(y, A, spec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, arith, momentum_reuse, x_ref, graph,
+                  max_backtracks, restart)
 
 
 def fista(y, A, At, omega, prox, sqrt_W=None, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, verbose=False, x0=None,
@@ -247,7 +253,7 @@ def _is_identity(prox, n) -> bool:
 
 
 def _fista(y, A, spec: RegSpec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, arith, momentum_reuse, x_ref=None,
-           graph=False):
+           graph=False, max_backtracks=0, restart=False):
     """With x_ref given, details['trace'] holds, per accepted iteration, the seconds since
     the solve started and |x_k - x_ref| / |x_ref|."""
     if not isinstance(A, LinearOperator):
@@ -275,6 +281,8 @@ def _fista(y, A, spec: RegSpec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, a
     prm = _lib.CgbFistaParams(float(tol_fun), float(tol_x), int(max_iter), int(verbose) if verbose is not True else 1,
                               _lib.ARITH[arith or A.arith], int(bool(momentum_reuse)))
     prm.graph = int(bool(graph))
+    prm.max_backtracks = int(max_backtracks)
+    prm.restart = int(bool(restart))
     if graph and (x_ref is not None or verbose == 4):
         raise ValueError('graph mode takes no x_ref and no verbose output')
     trace = None
@@ -305,7 +313,7 @@ def _fista(y, A, spec: RegSpec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, a
 
 def solve_mixed(y, A, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, verbose=0, x0=None, regularisation=None,
                 confidence_array=None, arith='fp16', refine_arith=None, refine_max_iter=None,
-                refine_tol_fun=None, refine_tol_x=None, x_ref=None):
+                refine_tol_fun=None, refine_tol_x=None, x_ref=None, restart=False):
     """Reduced-precision FISTA followed by an FP64 refinement solve.
 
     Phase 1 runs FISTA with the operator in ``arith`` ('bf16', 'fp16' or 'f32': LUT in
@@ -315,17 +323,20 @@ def solve_mixed(y, A, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, verbose=0, x0=Non
     (solution within 4e-4 instead of 4e-3 of the FP64 one on the demo case).  Phase 2 restarts the plain FP64
     solver (float-float by default) from the phase-1 solution, which removes the bias of
     the reduced-precision operator.  Returns (x, details) with details['mixed'] and
-    details['refine'] holding each phase's opt_details.
+    details['refine'] holding each phase's opt_details.  restart applies the function-value
+    momentum restart of ``solve`` in both phases.
     """
     import time
     t0 = time.perf_counter()
     x1, d1 = solve(y, A, A.T, tol_fun=tol_fun, tol_x=tol_x, max_iter=max_iter, verbose=verbose, x0=x0,
-                   regularisation=regularisation, confidence_array=confidence_array, arith=arith, x_ref=x_ref)
+                   regularisation=regularisation, confidence_array=confidence_array, arith=arith, x_ref=x_ref,
+                   restart=restart)
     t1 = time.perf_counter() - t0
     x2, d2 = solve(y, A, A.T, tol_fun=refine_tol_fun if refine_tol_fun is not None else tol_fun,
                    tol_x=refine_tol_x if refine_tol_x is not None else tol_x,
                    max_iter=refine_max_iter if refine_max_iter is not None else max_iter, verbose=verbose, x0=x1,
-                   regularisation=regularisation, confidence_array=confidence_array, arith=refine_arith, x_ref=x_ref)
+                   regularisation=regularisation, confidence_array=confidence_array, arith=refine_arith, x_ref=x_ref,
+                   restart=restart)
     det = dict(d2)
     if x_ref is not None:
         tr2 = d2['trace'].copy()

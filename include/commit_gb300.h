@@ -35,6 +35,7 @@ extern "C" {
 #define CGB_ERR_NOMEM 3       /* device allocation failed                                          */
 #define CGB_ERR_UNSUPPORTED 4 /* shape outside what the kernels handle (e.g. nS > 1024)            */
 #define CGB_ERR_DIMENSION 5   /* vector length does not match the operator ("dimensions do not match") */
+#define CGB_ERR_BACKTRACK 6   /* FISTA: one iteration's backtracking reached its cap (max_backtracks) */
 
 /* arithmetic of the FP64 operator path */
 #define CGB_ARITH_F64 0 /* native FP64 FMA, the reference's own arithmetic                             */
@@ -58,7 +59,7 @@ const char *cgb_last_error(void);
 const char *cgb_version(void);
 
 /*
- * Create an operator on device `device` from the dictionary and LUT arrays (HOST
+ * Create an operator on device `device` from the dictionary and LUT arrays (host or device
  * pointers, layout of LinearOperator.__init__, operator.pyx:40-94):
  *   IC: ICf[n] fibre (column) index, ICv[n] voxel, ICo[n] orientation, ICl[n] length,
  *       ICeval[nF*nIC] per-column 0/1 mask;
@@ -76,6 +77,20 @@ int cgb_op_create(int device, int nS, int ndirs, int nF, int64_t n, int nE, int 
                   const float *ICl, const uint32_t *ECv, const uint16_t *ECo, const uint32_t *ISOv,
                   const float *lutIC, const float *lutEC, const float *lutISO, int nIC, int nEC, int nISO,
                   int nolut, int arith, cgb_op **out);
+
+/*
+ * Evaluation.load_dictionary's re-layout (commit/core.pyx:493-580) on DEVICE arrays, in
+ * place: the raw arrays of the dictionary_*.dict files (voxel ids as linear grid indices
+ * x + X*(y + Y*z), IC lengths in mm) are sorted by voxel (stable, as numpy's argsort), IC
+ * lengths are divided by trk_norm[ICf] (FP32) when `normalize` is set, and voxel ids become
+ * indices among the mask voxels in the same linear order (mask: ngrid bytes in that order;
+ * ids outside the mask map to 0, as the reference's zero-filled table does).  *nV_out
+ * receives the number of mask voxels.  ICo / ECo may be NULL.  Synchronises `stream`.
+ * The results can be passed to cgb_op_create directly (it accepts device pointers).
+ */
+int cgb_dict_relayout(const uint8_t *mask, int64_t ngrid, int64_t n, int nF, uint32_t *ICf, uint32_t *ICv,
+                      uint16_t *ICo, float *ICl, const float *trk_norm, int normalize, int64_t nE, uint32_t *ECv,
+                      uint16_t *ECo, int64_t nISOv, uint32_t *ISOv, int64_t *nV_out, void *stream);
 
 /* Release the handle and every device buffer it owns. */
 int cgb_op_destroy(cgb_op *op);
@@ -260,6 +275,12 @@ typedef struct {
     int trace_len;
     int graph;            /* 1: the iteration loop runs as one CUDA graph launch with device-side */
                           /* decisions (conditional nodes); needs momentum_reuse 0, no trace    */
+    int max_backtracks;   /* step reductions allowed per iteration (0: 1000, negative: none);    */
+                          /* one more ends the solve with CGB_ERR_BACKTRACK (the reference's    */
+                          /* loop has no cap, commit/solvers.py:322-333)                        */
+    int restart;          /* 1: reset the momentum (t = 1) after an iteration whose objective     */
+                          /* rose (function-value restart, O'Donoghue & Candes 2015); 0 is the   */
+                          /* reference's FISTA.  Host-driven loop only.                          */
 } cgb_fista_params;
 
 typedef struct {

@@ -138,3 +138,31 @@ def test_graph_mode_with_adjoint_slabs():
     xg, dg = solvers.solve(y, A, A.T, graph=True, **kw)
     assert dg['iterations'] == dh['iterations']
     assert np.array_equal(xg, xh)
+
+
+def test_backtracking_cap_ends_the_solve():
+    """A fit that backtracks, run with no step reduction allowed, stops with the
+    backtracking status in both the host loop and the graph (whose backtracking WHILE node
+    is bounded); with the default cap it finishes as before."""
+    from commit_gb300 import _lib, solvers
+    from commit_gb300.operator import LinearOperator
+    found = False
+    for name, variant in _fit_cases():
+        c = G.load_case(name)
+        f = c['fits'][variant]
+        A = LinearOperator(c['D'], c['K'], None, nolut=c['nolut'])
+        kw = dict(tol_fun=1e-5, tol_x=1e-7, max_iter=f['details']['iterations'], verbose=0,
+                  confidence_array=f['conf'], momentum_reuse=False)
+        reg = lambda: solvers.init_regularisation(G.fresh_reg(f['reg']))  # noqa: E731
+        _, d = solvers.solve(c['y_obs'], A, A.T, regularisation=reg(), **kw)
+        if d['backtracks'] == 0:
+            continue
+        found = True
+        for graph in (False, True):
+            with pytest.raises(_lib.CgbError, match='backtracking') as ei:
+                solvers.solve(c['y_obs'], A, A.T, regularisation=reg(), graph=graph, max_backtracks=-1, **kw)
+            assert ei.value.code == _lib.CGB_ERR_BACKTRACK
+        _, d2 = solvers.solve(c['y_obs'], A, A.T, regularisation=reg(), graph=True, **kw)
+        assert d2['iterations'] == d['iterations'] and d2['backtracks'] == d['backtracks']
+        break
+    assert found, 'no golden fit backtracks'
