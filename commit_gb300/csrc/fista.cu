@@ -17,6 +17,7 @@
 #include <string.h>
 
 #include <chrono>
+#include <functional>
 #include <vector>
 
 #include "cgb_internal.cuh"
@@ -452,6 +453,25 @@ __global__ void k_prox_stats(double *__restrict__ x, double *__restrict__ xh, co
     }
 }
 
+// graph mode with momentum reuse: A x_hat = (1+c) A x - c A x_prev from the stored rows,
+// with c the device-side momentum coefficient and the rounding of the gradient kernels'
+// own combination (ax_combine), so the graph's iterates are those of the host loop
+__global__ void k_ax_combine_dev(double *__restrict__ out, const double *__restrict__ a, const double *__restrict__ b,
+                                 const GState *__restrict__ S, int64_t n) {
+    const double c = S->c;
+    const double ca = __dadd_rn(1.0, c), cb = -c;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = detail::ax_combine(ca, a[i], cb, b[i]);
+}
+
+__global__ void k_ax_combine32_dev(float *__restrict__ out, const float *__restrict__ a, const float *__restrict__ b,
+                                   const GState *__restrict__ S, int64_t n) {
+    const double c = S->c;
+    const float ca = (float)__dadd_rn(1.0, c), cb = (float)(-c);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = detail::ax_combine(ca, a[i], cb, b[i]);
+}
+
 // lam = lam_base * step for the group prox of the graph (the host path passes it directly)
 __global__ void k_scale_lam(const GState *__restrict__ S, double lam_base, double *__restrict__ out) {
     *out = __dmul_rn(S->step, lam_base);
@@ -462,14 +482,15 @@ __global__ void k_scale_lam(const GState *__restrict__ S, double lam_base, doubl
 // ------------------------------------------------------------------ solver workspace
 struct FistaWS {
     int64_t ncols = 0, nrows = 0;
-    double *xhat = nullptr, *prev = nullptr, *grad = nullptr, *ax[2] = {nullptr, nullptr};
+    double *xhat = nullptr, *prev = nullptr, *grad = nullptr, *ax[3] = {nullptr, nullptr, nullptr};
     double *pstats = nullptr, *pgrp = nullptr, *pres = nullptr;
     unsigned int *counter = nullptr;  // arrival counter of the fused elementwise pass (k_prox_stats)
     // reduced-precision path: FP32 copies of y and sqrt(W), FP32 A*x buffers
-    float *y32 = nullptr, *sqw32 = nullptr, *ax32[2] = {nullptr, nullptr};
+    float *y32 = nullptr, *sqw32 = nullptr, *ax32[3] = {nullptr, nullptr, nullptr};
     cudaStream_t st = nullptr;  // allocations are stream-ordered on the solver's stream
     ~FistaWS() {
-        void *ps[] = {xhat, prev, grad, ax[0], ax[1], pstats, pgrp, pres, y32, sqw32, ax32[0], ax32[1], counter};
+        void *ps[] = {xhat, prev, grad, ax[0], ax[1], ax[2], pstats, pgrp, pres, y32, sqw32, ax32[0], ax32[1], ax32[2],
+                      counter};
         for (void *p : ps)
             if (p) cudaFreeAsync(p, st);
     }
@@ -526,10 +547,12 @@ struct Solver {
             if (prm->momentum_reuse) {
                 CGB_TRY(ws_alloc(&ws.ax32[0], nr, st));
                 CGB_TRY(ws_alloc(&ws.ax32[1], nr, st));
+                if (prm->graph) CGB_TRY(ws_alloc(&ws.ax32[2], nr, st));
             }
         } else if (prm->momentum_reuse) {
             CGB_TRY(ws_alloc(&ws.ax[0], nr, st));
             CGB_TRY(ws_alloc(&ws.ax[1], nr, st));
+            if (prm->graph) CGB_TRY(ws_alloc(&ws.ax[2], nr, st));
         }
         CGB_TRY(ws_alloc(&ws.pstats, (size_t)rb * kRedSlots, st));
         CGB_TRY(ws_alloc(&ws.pgrp, (size_t)rb * kRedSlots, st));
@@ -881,14 +904,14 @@ struct Solver {
 
     // --------------------------------------------------------------- graph mode
     // One evaluation of x = prox(xhat - step*grad) with its statistics and objective.
-    int eval_dev(double *x) {
+    int eval_dev(double *x, int slot) {
         if (fused_elem) {
             CGB_TRY(prox_stats(x, 0.0, 0, 0.0));
         } else {
             CGB_TRY(prox(x, ws.xhat, ws.grad, 0.0, 0.0));
             CGB_TRY(stats(x, ws.xhat, ws.grad, ws.prev));
         }
-        return objective(x, -1);
+        return objective(x, slot);
     }
 
     // add a conditional node at the current point of the capture on `cap`, capture its body
@@ -921,9 +944,11 @@ struct Solver {
         return CGB_OK;
     }
 
-    // FISTA with the iteration loop as one graph launch (no momentum reuse, no trace).
+    // FISTA with the iteration loop as one graph launch (no trace).  With momentum reuse the
+    // body holds two iterations, so the two stored A x rows alternate with fixed pointers.
     int run_graph(double *x, cgb_fista_result *res) {
         const int64_t nc = op->ncols;
+        const bool reuse = prm->momentum_reuse != 0;
         double *h = op->h_scal;
         // initialisation on the host path (solvers.py:260-286), as in run()
         CGB_CUDA(cudaMemcpyAsync(ws.xhat, x, nc * sizeof(double), cudaMemcpyDeviceToDevice, st));
@@ -975,8 +1000,15 @@ struct Solver {
         CGB_CUDA(cudaMemcpyAsync(gs, &G, sizeof(G), cudaMemcpyHostToDevice, st));
         CGB_CUDA(cudaStreamSynchronize(st));
         gdev = gs;
-        // graph: WHILE(main) { begin; eval; judge; WHILE(bt) { eval; judge }; stop; IF(cont) { momentum; gradient } }
-        cudaStream_t s0 = nullptr, s1 = nullptr, s2 = nullptr;
+        if (reuse) {
+            // the first iteration combines A x with a zero "previous" row (c = 0 there)
+            if (mixed) CGB_CUDA(cudaMemsetAsync(ws.ax32[1], 0, op->nrows * sizeof(float), st));
+            else CGB_CUDA(cudaMemsetAsync(ws.ax[1], 0, op->nrows * sizeof(double), st));
+        }
+        // graph: WHILE(main) { ITER(0) } without reuse, WHILE(main) { ITER(0, IF(cont) { ITER(1) }) }
+        // with it, where ITER(s) = begin; eval; judge; WHILE(bt) { eval; judge }; stop;
+        // IF(cont) { momentum; gradient; ... } and eval writes A x to stored row s
+        cudaStream_t s0 = nullptr, s1 = nullptr, s2 = nullptr, s3 = nullptr, s4 = nullptr;
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
         const cudaStream_t user = st;
@@ -985,11 +1017,54 @@ struct Solver {
             CGB_CUDA(cudaStreamCreateWithFlags(&s0, cudaStreamNonBlocking));
             CGB_CUDA(cudaStreamCreateWithFlags(&s1, cudaStreamNonBlocking));
             CGB_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+            CGB_CUDA(cudaStreamCreateWithFlags(&s3, cudaStreamNonBlocking));
+            CGB_CUDA(cudaStreamCreateWithFlags(&s4, cudaStreamNonBlocking));
             CGB_CUDA(cudaGraphCreate(&graph, 0));
-            cudaGraphConditionalHandle hmain, hbt, hcont;
+            cudaGraphConditionalHandle hmain, hbt, hcont, hbt2, hcont2;
             CGB_CUDA(cudaGraphConditionalHandleCreate(&hmain, graph, 1, cudaGraphCondAssignDefault));
             CGB_CUDA(cudaGraphConditionalHandleCreate(&hbt, graph, 0, cudaGraphCondAssignDefault));
             CGB_CUDA(cudaGraphConditionalHandleCreate(&hcont, graph, 0, cudaGraphCondAssignDefault));
+            CGB_CUDA(cudaGraphConditionalHandleCreate(&hbt2, graph, 0, cudaGraphCondAssignDefault));
+            CGB_CUDA(cudaGraphConditionalHandleCreate(&hcont2, graph, 0, cudaGraphCondAssignDefault));
+            const int64_t nr = op->nrows;
+            // one iteration captured on `cap`: evaluation into stored row `slot` (-1: none),
+            // backtracking, stopping test, and for a continuing iteration the momentum, the
+            // gradient at x_hat and then `more`
+            std::function<int(cudaStream_t, cudaStream_t, cudaStream_t, cudaGraphConditionalHandle,
+                              cudaGraphConditionalHandle, int, std::function<int()>)>
+                iteration = [&](cudaStream_t cap, cudaStream_t sbt, cudaStream_t sif, cudaGraphConditionalHandle hb,
+                                cudaGraphConditionalHandle hc, int slot, std::function<int()> more) -> int {
+                k_ctl_begin<<<1, 1, 0, cap>>>(gs, d);
+                CGB_CUDA(cudaGetLastError());
+                CGB_TRY(eval_dev(x, slot));
+                k_ctl_judge<<<1, 1, 0, cap>>>(gs, d, hb);
+                CGB_CUDA(cudaGetLastError());
+                CGB_TRY(conditional(cap, sbt, hb, cudaGraphCondTypeWhile, [&]() -> int {
+                    CGB_TRY(eval_dev(x, slot));
+                    k_ctl_judge<<<1, 1, 0, st>>>(gs, d, hb);
+                    CGB_CUDA(cudaGetLastError());
+                    return CGB_OK;
+                }));
+                k_ctl_stop<<<1, 1, 0, cap>>>(gs, d, hmain, hc);
+                CGB_CUDA(cudaGetLastError());
+                return conditional(cap, sif, hc, cudaGraphCondTypeIf, [&]() -> int {
+                    k_momentum_dev<<<elem_grid(op, nc), kBlock, 0, st>>>(ws.xhat, x, ws.prev, gs, nc);
+                    CGB_CUDA(cudaGetLastError());
+                    if (slot < 0) {
+                        CGB_TRY(gradient(ws.xhat, ws.grad, -1, -1, 0.0, 0.0));
+                    } else {
+                        if (mixed)
+                            k_ax_combine32_dev<<<elem_grid(op, nr), kBlock, 0, st>>>(ws.ax32[2], ws.ax32[slot],
+                                                                                     ws.ax32[1 - slot], gs, nr);
+                        else
+                            k_ax_combine_dev<<<elem_grid(op, nr), kBlock, 0, st>>>(ws.ax[2], ws.ax[slot],
+                                                                                   ws.ax[1 - slot], gs, nr);
+                        CGB_CUDA(cudaGetLastError());
+                        CGB_TRY(gradient(ws.xhat, ws.grad, 2, 2, 1.0, 0.0));
+                    }
+                    return more();
+                });
+            };
             cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
             np.conditional.handle = hmain;
             np.conditional.type = cudaGraphCondTypeWhile;
@@ -1000,25 +1075,10 @@ struct Solver {
             st = s0;
             CGB_CUDA(cudaStreamBeginCaptureToGraph(s0, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
             int rc = [&]() -> int {
-                k_ctl_begin<<<1, 1, 0, s0>>>(gs, d);
-                CGB_CUDA(cudaGetLastError());
-                CGB_TRY(eval_dev(x));
-                k_ctl_judge<<<1, 1, 0, s0>>>(gs, d, hbt);
-                CGB_CUDA(cudaGetLastError());
-                CGB_TRY(conditional(s0, s1, hbt, cudaGraphCondTypeWhile, [&]() -> int {
-                    CGB_TRY(eval_dev(x));
-                    k_ctl_judge<<<1, 1, 0, st>>>(gs, d, hbt);
-                    CGB_CUDA(cudaGetLastError());
-                    return CGB_OK;
-                }));
-                k_ctl_stop<<<1, 1, 0, s0>>>(gs, d, hmain, hcont);
-                CGB_CUDA(cudaGetLastError());
-                CGB_TRY(conditional(s0, s2, hcont, cudaGraphCondTypeIf, [&]() -> int {
-                    k_momentum_dev<<<elem_grid(op, nc), kBlock, 0, st>>>(ws.xhat, x, ws.prev, gs, nc);
-                    CGB_CUDA(cudaGetLastError());
-                    return gradient(ws.xhat, ws.grad, -1, -1, 0.0, 0.0);
-                }));
-                return CGB_OK;
+                if (!reuse) return iteration(s0, s1, s2, hbt, hcont, -1, [] { return CGB_OK; });
+                return iteration(s0, s1, s2, hbt, hcont, 0, [&]() -> int {
+                    return iteration(s2, s3, s4, hbt2, hcont2, 1, [] { return CGB_OK; });
+                });
             }();
             cudaGraph_t done = nullptr;
             const cudaError_t e = cudaStreamEndCapture(s0, &done);
@@ -1041,7 +1101,7 @@ struct Solver {
         }
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
-        for (cudaStream_t q : {s0, s1, s2})
+        for (cudaStream_t q : {s0, s1, s2, s3, s4})
             if (q) cudaStreamDestroy(q);
         gdev = nullptr;
         cudaFreeAsync(gs, st);
@@ -1061,8 +1121,9 @@ struct Solver {
         res->iterations = G.it;
         res->stopping_criterion = G.crit;
         res->backtracks = G.backtracks;
-        // init: 2 (gradient) + 1 (Rayleigh quotient); per evaluation 1; per gradient 2
-        res->operator_calls = calls + (G.it + G.backtracks) + 2 * (G.it - 1);
+        // init: 2 (gradient) + 1 (Rayleigh quotient); per evaluation 1; per gradient 2, or 1
+        // when A x_hat comes from the stored rows
+        res->operator_calls = calls + (G.it + G.backtracks) + (reuse ? 1 : 2) * (G.it - 1);
         return CGB_OK;
     }
 };
@@ -1533,9 +1594,8 @@ int cgb_fista_run(cgb_op *op, const double *y, const double *sqrt_w, const cgb_r
     if ((reg->reg_ic == CGB_REG_GROUP_LASSO || reg->reg_ic == CGB_REG_SPARSE_GROUP_LASSO) && reg->ngroups > 0 &&
         (!reg->level_ptr || reg->nlevels < 1))
         return fail(CGB_ERR_INVALID, "group regulariser needs a level schedule");
-    if (params->graph && (params->momentum_reuse || (params->trace && params->x_ref) || params->verbose == 4 ||
-                          params->restart))
-        return fail(CGB_ERR_UNSUPPORTED, "graph mode runs without momentum reuse, restart, trace or verbose output");
+    if (params->graph && ((params->trace && params->x_ref) || params->verbose == 4 || params->restart))
+        return fail(CGB_ERR_UNSUPPORTED, "graph mode runs without restart, trace or verbose output");
     NvtxRange nv("cgb_fista_run");
     DevGuard g(op->device);
     Solver S;

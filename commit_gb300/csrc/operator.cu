@@ -93,7 +93,7 @@ __global__ void k_adjoint_nolut(const OpDev P, const double *__restrict__ yin, i
                         if (x0 != 0) a += x0;
                     }
             } else {
-                a = ca * ax_a[v] + cb * ax_b[v];
+                a = ax_combine(ca, ax_a[v], cb, ax_b[v]);
             }
             double r = a - yobs[v];
             if (sqw) r *= sqw[v];

@@ -139,6 +139,15 @@ __device__ __forceinline__ int ff_exp_hi(unsigned hi, int lut_exp) {
     return e < -1000 ? -1000 : (e > 1000 ? 1000 : e);
 }
 
+// A x from stored rows (momentum reuse): ca*a + cb*b with one explicit rounding order, so
+// that a separate pass forming the same row (the graph-captured FISTA) gives the same bits
+__device__ __forceinline__ double ax_combine(double ca, double a, double cb, double b) {
+    return __fma_rn(ca, a, __dmul_rn(cb, b));
+}
+__device__ __forceinline__ float ax_combine(float ca, float a, float cb, float b) {
+    return __fmaf_rn(ca, a, __fmul_rn(cb, b));
+}
+
 // 2^e as a double for |e| <= 1000 (exponent field only)
 __device__ __forceinline__ double pow2(int e) { return __hiloint2double((e + 1023) << 20, 0); }
 
@@ -382,7 +391,7 @@ __global__ void __launch_bounds__(kBlock) k_adjoint(const OpDev P, const double 
             if (s >= nS) return 0.0;
             const size_t idx = (size_t)v * nS + s;
             if (in_mode == 0) return yin[idx];
-            const double av = in_mode == 1 ? a[k] : ca * ax_a[idx] + cb * ax_b[idx];
+            const double av = in_mode == 1 ? a[k] : ax_combine(ca, ax_a[idx], cb, ax_b[idx]);
             double r = av - yobs[idx];
             if (sqw) r *= sqw[idx];
             if (first) nrm = fma(r, r, nrm);

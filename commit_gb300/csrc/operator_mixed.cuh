@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_adjoint_mix(const int v0, cons
                     if (in_mode == 0) {
                         zz[u] = yin[idx];
                     } else {
-                        const float av = in_mode == 1 ? a[u] : ca * ax_a[idx] + cb * ax_b[idx];
+                        const float av = in_mode == 1 ? a[u] : ax_combine(ca, ax_a[idx], cb, ax_b[idx]);
                         float r = av - yobs[idx];
                         if (sqw) r *= sqw[idx];
                         vn = fmaf(r, r, vn);

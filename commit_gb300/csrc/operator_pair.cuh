@@ -394,7 +394,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_adjoint_p(const OpDev P, const
             if (s >= nS) return 0.0;
             const size_t idx = (size_t)v * nS + s;
             if (in_mode == 0) return yin[idx];
-            const double av = FUSED && in_mode == 1 ? a[2 * k + u] : ca * ax_a[idx] + cb * ax_b[idx];
+            const double av = FUSED && in_mode == 1 ? a[2 * k + u] : ax_combine(ca, ax_a[idx], cb, ax_b[idx]);
             double r = av - yobs[idx];
             if (sqw) r *= sqw[idx];
             if (first) nrm = fma(r, r, nrm);

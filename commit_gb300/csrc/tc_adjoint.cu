@@ -121,7 +121,8 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
                     if (A.mode == 0) {
                         zz = A.yin[idx];
                     } else {
-                        float r = A.ca * A.axa[idx] + (A.axb ? A.cb * A.axb[idx] : 0.f) - A.yobs[idx];
+                        const float av = A.axb ? ax_combine(A.ca, A.axa[idx], A.cb, A.axb[idx]) : __fmul_rn(A.ca, A.axa[idx]);
+                        float r = av - A.yobs[idx];
                         if (A.sqw) r *= A.sqw[idx];
                         vn = fmaf(r, r, vn);
                         zz = A.sqw ? A.sqw[idx] * r : r;

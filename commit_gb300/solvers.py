@@ -209,8 +209,8 @@ def solve(y, A, At, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, verbose=True, x0=No
     """solvers.py:218-241: regularised least squares by FISTA, on the GPU.
 
     graph=True runs the iteration loop as one CUDA graph launch whose backtracking and
-    stopping decisions are taken on the device (conditional graph nodes); it implies
-    momentum_reuse=False and takes no x_ref / verbose output.  max_backtracks caps the step
+    stopping decisions are taken on the device (conditional graph nodes), with or without
+    momentum reuse; it takes no x_ref / verbose output and no restart.  max_backtracks caps the step
     reductions of one iteration (0: 1000, negative: none); reaching the cap raises CgbError (the
     reference's backtracking loop has no cap, solvers.py:322-333).  restart=True resets the
     momentum after an iteration whose objective rose (function-value restart; not in the
@@ -225,8 +225,6 @@ def solve(y, A, At, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, verbose=True, x0=No
     if confidence_array is not None:
         sqrt_W = np.sqrt(np.asarray(confidence_array)) if not isinstance(confidence_array, torch.Tensor) \
             else torch.sqrt(confidence_array)
-    if graph:
-        momentum_reuse = False
     return _fista(y, A, spec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, arith, momentum_reuse, x_ref, graph,
                   max_backtracks, restart)
 

@@ -274,7 +274,7 @@ typedef struct {
     double *trace;
     int trace_len;
     int graph;            /* 1: the iteration loop runs as one CUDA graph launch with device-side */
-                          /* decisions (conditional nodes); needs momentum_reuse 0, no trace    */
+                          /* decisions (conditional nodes); no trace, verbose output or restart */
     int max_backtracks;   /* step reductions allowed per iteration (0: 1000, negative: none);    */
                           /* one more ends the solve with CGB_ERR_BACKTRACK (the reference's    */
                           /* loop has no cap, commit/solvers.py:322-333)                        */

@@ -100,9 +100,11 @@ def test_mixed_fista_and_refinement(arith, tol):
     assert dm['cost_function'] <= d_ref['cost_function'] * (1 + 1e-9)
 
 
+@pytest.mark.parametrize('reuse', [False, True])
 @pytest.mark.parametrize('name,variant', [(n, v) for n, v in _fit_cases() if n in ('szb', 'multi_rf', 'eval_gaps')])
-def test_graph_mode_matches_host_loop(name, variant):
-    """The iteration loop as one CUDA graph (device-side backtracking and stopping) gives the
+def test_graph_mode_matches_host_loop(name, variant, reuse):
+    """The iteration loop as one CUDA graph (device-side backtracking and stopping; with
+    momentum reuse, A x_hat formed on the device from the two stored rows) gives the
     host-driven loop's iterates bit for bit, and the reference's fit."""
     from commit_gb300 import solvers
     from commit_gb300.operator import LinearOperator
@@ -110,7 +112,7 @@ def test_graph_mode_matches_host_loop(name, variant):
     f = c['fits'][variant]
     A = LinearOperator(c['D'], c['K'], None, nolut=c['nolut'])
     kw = dict(tol_fun=1e-5, tol_x=1e-7, max_iter=f['details']['iterations'], verbose=0,
-              confidence_array=f['conf'], momentum_reuse=False)
+              confidence_array=f['conf'], momentum_reuse=reuse)
     xh, dh = solvers.solve(c['y_obs'], A, A.T, regularisation=solvers.init_regularisation(G.fresh_reg(f['reg'])), **kw)
     xg, dg = solvers.solve(c['y_obs'], A, A.T, regularisation=solvers.init_regularisation(G.fresh_reg(f['reg'])),
                            graph=True, **kw)
@@ -123,7 +125,8 @@ def test_graph_mode_matches_host_loop(name, variant):
         assert dg[k] == dh[k], k
 
 
-def test_graph_mode_with_adjoint_slabs():
+@pytest.mark.parametrize('reuse', [False, True])
+def test_graph_mode_with_adjoint_slabs(reuse):
     """Inside the graph capture the slab schedule runs its steps in order on one stream; the
     iterates stay bit-identical to the host loop's (three-stream schedule)."""
     from commit_gb300 import solvers, synth
@@ -133,7 +136,7 @@ def test_graph_mode_with_adjoint_slabs():
     assert A.set_slabs(4) == 4
     x0 = synth.make_x(A.nCOLS, 1)
     y = synth.make_signal(A.dot(x0), 2)
-    kw = dict(tol_fun=1e-6, tol_x=1e-8, max_iter=60, verbose=0, momentum_reuse=False)
+    kw = dict(tol_fun=1e-6, tol_x=1e-8, max_iter=60, verbose=0, momentum_reuse=reuse)
     xh, dh = solvers.solve(y, A, A.T, **kw)
     xg, dg = solvers.solve(y, A, A.T, graph=True, **kw)
     assert dg['iterations'] == dh['iterations']
