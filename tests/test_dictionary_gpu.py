@@ -66,6 +66,8 @@ def test_operator_from_device_dictionary(name, tmp_path):
         D['IC']['eval'] = np.ones(H['IC']['nSTR'], np.uint32)
     Ah = LinearOperator(H, K, None)
     Ad = LinearOperator(Dd, K, None)
+    for A in (Ah, Ad):  # one voxel shape for both (the timed choice may differ, and so would the sum order)
+        A.ff_shape(1)
     x = rng.uniform(0.0, 1.0, Ah.nCOLS)
     y = rng.normal(size=Ah.nROWS)
     assert np.array_equal(Ah.dot(x), Ad.dot(x))
