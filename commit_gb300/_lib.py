@@ -36,13 +36,14 @@ class CgbReg(ctypes.Structure):
 class CgbFistaParams(ctypes.Structure):
     _fields_ = [('tol_fun', c_f64), ('tol_x', c_f64), ('max_iter', c_i32), ('verbose', c_i32),
                 ('arith', c_i32), ('momentum_reuse', c_i32), ('x_ref', c_vp), ('trace', c_vp), ('trace_len', c_i32),
-                ('graph', c_i32), ('max_backtracks', c_i32), ('restart', c_i32)]
+                ('graph', c_i32), ('max_backtracks', c_i32), ('restart', c_i32), ('trace_cost', c_i32)]
 
 
 class CgbFistaResult(ctypes.Structure):
     _fields_ = [('residual', c_f64), ('regterm', c_f64), ('cost_function', c_f64), ('abs_cost', c_f64),
                 ('rel_cost', c_f64), ('abs_x', c_f64), ('rel_x', c_f64), ('iterations', c_i32),
-                ('stopping_criterion', c_i32), ('backtracks', c_i32), ('operator_calls', c_i32)]
+                ('stopping_criterion', c_i32), ('backtracks', c_i32), ('operator_calls', c_i32),
+                ('anchors', c_i32)]
 
 
 class CgbT2DParams(ctypes.Structure):

@@ -260,6 +260,9 @@ struct GState {
     int nterms, group_in_omega;
     int it, crit, backtracks, max_iter;
     int bt_iter, max_bt;  // backtracks of the current iteration and their cap
+    int reuse;            // A x_hat of the gradient pass comes from the stored rows
+    int anchored;         // this iteration's qfval was evaluated again directly
+    int anchors;          // such evaluations over the solve
 };
 
 __device__ __forceinline__ double g_omega(const GState &S, const double *h) {
@@ -274,11 +277,24 @@ __global__ void k_ctl_begin(GState *S, const double *h) {
     const double r = __dsqrt_rn(h[12]);
     S->qfval = S->it == 1 ? S->prev_obj : __dmul_rn(__dmul_rn(0.5, r), r);
     S->bt_iter = 0;
+    S->anchored = 0;
+}
+
+// qfval from a direct evaluation of x_hat (slot 0 of h), replacing the stored-row one
+__global__ void k_ctl_anchor(GState *S, const double *h) {
+    const double r = __dsqrt_rn(h[0]);
+    S->qfval = __dmul_rn(__dmul_rn(0.5, r), r);
+    S->anchors += 1;
 }
 
 // objective and quadratic model of the evaluated x (solvers.py:315-333); on failure of the
-// sufficient-decrease test shrink the step and ask for another evaluation
-__global__ void k_ctl_judge(GState *S, const double *h, cudaGraphConditionalHandle bt) {
+// sufficient-decrease test shrink the step and ask for another evaluation.  A qfval taken
+// from the stored rows is rounded differently from the evaluation of x, so near convergence
+// the test can fail at the rounding level for every step; its first failure in an iteration
+// asks instead for f(x_hat) evaluated directly, as the reference computes it, and the same
+// step is judged again (`anchor`)
+__global__ void k_ctl_judge(GState *S, const double *h, cudaGraphConditionalHandle bt,
+                            cudaGraphConditionalHandle anchor) {
     const double reg = g_omega(*S, h);
     const double d2 = __dsqrt_rn(h[2]);
     const double q = __dadd_rn(__dadd_rn(__dadd_rn(S->qfval, h[1]), __dmul_rn(__ddiv_rn(0.5, S->step), __dmul_rn(d2, d2))),
@@ -288,15 +304,22 @@ __global__ void k_ctl_judge(GState *S, const double *h, cudaGraphConditionalHand
     S->reg_x = reg;
     S->res_norm = rn;
     S->curr_obj = cur;
-    if (cur > q && S->bt_iter >= S->max_bt) {
+    if (cur > q && S->reuse && S->it > 1 && !S->anchored) {
+        S->anchored = 1;
+        cudaGraphSetConditional(anchor, 1);
+        cudaGraphSetConditional(bt, 1);
+    } else if (cur > q && S->bt_iter >= S->max_bt) {
         S->crit = -1;  // cap reached: leave the backtracking loop, k_ctl_stop ends the solve
+        cudaGraphSetConditional(anchor, 0);
         cudaGraphSetConditional(bt, 0);
     } else if (cur > q) {
         S->step = __dmul_rn(0.9, S->step);
         S->backtracks += 1;
         S->bt_iter += 1;
+        cudaGraphSetConditional(anchor, 0);
         cudaGraphSetConditional(bt, 1);
     } else {
+        cudaGraphSetConditional(anchor, 0);
         cudaGraphSetConditional(bt, 0);
     }
 }
@@ -800,6 +823,8 @@ struct Solver {
         int have_prev_ax = 0; // ax[1-cur] holds A*prev_x
         double curr_obj = 0, reg_term_x = 0, abs_obj = 0, rel_obj = 0, abs_x = 0, rel_x = 0;
         int crit = 4;
+        int anchors = 0;      // direct evaluations of f(x_hat) (see k_ctl_judge)
+        bool q_rows = false;  // this iteration's qfval comes from the stored rows
         int pend_mom = 0;     // momentum deferred into the next evaluation's fused pass
         double pend_c = 0.0;
         while (true) {
@@ -823,7 +848,23 @@ struct Solver {
             res_norm = sqrt(h[0]);
             curr_obj = 0.5 * res_norm * res_norm + reg_term_x;
             int bt_iter = 0;
+            bool anchored = false;
             while (curr_obj > q) {
+                if (q_rows && !anchored) {
+                    // qfval from the stored rows: judge this step again against f(x_hat)
+                    // evaluated directly, as the reference computes it (see k_ctl_judge)
+                    anchored = true;
+                    anchors++;
+                    CGB_TRY(objective(ws.xhat, -1));
+                    CGB_TRY(fetch(h));
+                    qfval = 0.5 * sqrt(h[0]) * sqrt(h[0]);
+                    CGB_TRY(eval_x(step));
+                    reg_term_x = omega_from(h);
+                    q = qfval + h[1] + 0.5 / step * (sqrt(h[2]) * sqrt(h[2])) + reg_term_x;
+                    res_norm = sqrt(h[0]);
+                    curr_obj = 0.5 * res_norm * res_norm + reg_term_x;
+                    continue;
+                }
                 if (bt_iter >= max_bt)
                     return fail(CGB_ERR_BACKTRACK, "FISTA: backtracking of iteration " + std::to_string(it) +
                                                        " reached its cap of " + std::to_string(max_bt) + " step reductions");
@@ -837,8 +878,11 @@ struct Solver {
                 curr_obj = 0.5 * res_norm * res_norm + reg_term_x;
             }
             if (prm->trace && prm->x_ref && it <= prm->trace_len) {
-                prm->trace[2 * (it - 1)] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
-                prm->trace[2 * (it - 1) + 1] = sqrt(h[9]) / sqrt(h[10]);
+                const int w = prm->trace_cost ? 3 : 2;
+                double *t = prm->trace + (size_t)w * (it - 1);
+                t[0] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+                t[1] = sqrt(h[9]) / sqrt(h[10]);
+                if (w == 3) t[2] = curr_obj;
             }
             abs_obj = fabs(curr_obj - prev_obj);
             rel_obj = abs_obj / curr_obj;
@@ -868,10 +912,12 @@ struct Solver {
                     CGB_CUDA(cudaGetLastError());
                 }
                 CGB_TRY(gradient(ws.xhat, ws.grad, cur, have_prev_ax ? 1 - cur : cur, 1.0 + c, -c));
+                q_rows = true;
             } else {
                 k_momentum<<<elem_grid(op, nc), kBlock, 0, st>>>(ws.xhat, x, ws.prev, c, nc);
                 CGB_CUDA(cudaGetLastError());
                 CGB_TRY(gradient(ws.xhat, ws.grad, -1, -1, 0.0, 0.0));
+                q_rows = false;
             }
             if (prm->momentum_reuse) {
                 cur = 1 - cur;
@@ -898,6 +944,7 @@ struct Solver {
         res->stopping_criterion = crit;
         res->backtracks = backtracks;
         res->operator_calls = calls;
+        res->anchors = anchors;
         CGB_CUDA(cudaStreamSynchronize(st));
         return CGB_OK;
     }
@@ -994,6 +1041,7 @@ struct Solver {
         G.crit = 4;
         G.max_iter = prm->max_iter;
         G.max_bt = prm->max_backtracks > 0 ? prm->max_backtracks : (prm->max_backtracks < 0 ? 0 : 1000);
+        G.reuse = reuse;
         GState *gs = nullptr;
         CGB_TRY(ws_alloc(&gs, 1, st));
         CGB_TRY(ws_alloc(&glam, 1, st));
@@ -1020,7 +1068,9 @@ struct Solver {
             CGB_CUDA(cudaStreamCreateWithFlags(&s3, cudaStreamNonBlocking));
             CGB_CUDA(cudaStreamCreateWithFlags(&s4, cudaStreamNonBlocking));
             CGB_CUDA(cudaGraphCreate(&graph, 0));
-            cudaGraphConditionalHandle hmain, hbt, hcont, hbt2, hcont2;
+            cudaGraphConditionalHandle hmain, hbt, hcont, hbt2, hcont2, hq, hq2;
+            CGB_CUDA(cudaGraphConditionalHandleCreate(&hq, graph, 0, cudaGraphCondAssignDefault));
+            CGB_CUDA(cudaGraphConditionalHandleCreate(&hq2, graph, 0, cudaGraphCondAssignDefault));
             CGB_CUDA(cudaGraphConditionalHandleCreate(&hmain, graph, 1, cudaGraphCondAssignDefault));
             CGB_CUDA(cudaGraphConditionalHandleCreate(&hbt, graph, 0, cudaGraphCondAssignDefault));
             CGB_CUDA(cudaGraphConditionalHandleCreate(&hcont, graph, 0, cudaGraphCondAssignDefault));
@@ -1028,20 +1078,31 @@ struct Solver {
             CGB_CUDA(cudaGraphConditionalHandleCreate(&hcont2, graph, 0, cudaGraphCondAssignDefault));
             const int64_t nr = op->nrows;
             // one iteration captured on `cap`: evaluation into stored row `slot` (-1: none),
-            // backtracking, stopping test, and for a continuing iteration the momentum, the
-            // gradient at x_hat and then `more`
+            // backtracking (WHILE(bt) { IF(anchor) { f(x_hat) directly }; eval; judge }),
+            // stopping test, and for a continuing iteration the momentum, the gradient at
+            // x_hat and then `more`.  The anchor's body is captured on `sif`, which is free
+            // until the backtracking node is complete.
             std::function<int(cudaStream_t, cudaStream_t, cudaStream_t, cudaGraphConditionalHandle,
-                              cudaGraphConditionalHandle, int, std::function<int()>)>
+                              cudaGraphConditionalHandle, cudaGraphConditionalHandle, int, std::function<int()>)>
                 iteration = [&](cudaStream_t cap, cudaStream_t sbt, cudaStream_t sif, cudaGraphConditionalHandle hb,
-                                cudaGraphConditionalHandle hc, int slot, std::function<int()> more) -> int {
+                                cudaGraphConditionalHandle hc, cudaGraphConditionalHandle ha, int slot,
+                                std::function<int()> more) -> int {
                 k_ctl_begin<<<1, 1, 0, cap>>>(gs, d);
                 CGB_CUDA(cudaGetLastError());
                 CGB_TRY(eval_dev(x, slot));
-                k_ctl_judge<<<1, 1, 0, cap>>>(gs, d, hb);
+                k_ctl_judge<<<1, 1, 0, cap>>>(gs, d, hb, ha);
                 CGB_CUDA(cudaGetLastError());
                 CGB_TRY(conditional(cap, sbt, hb, cudaGraphCondTypeWhile, [&]() -> int {
+                    if (reuse) {
+                        CGB_TRY(conditional(st, sif, ha, cudaGraphCondTypeIf, [&]() -> int {
+                            CGB_TRY(objective(ws.xhat, -1));
+                            k_ctl_anchor<<<1, 1, 0, st>>>(gs, d);
+                            CGB_CUDA(cudaGetLastError());
+                            return CGB_OK;
+                        }));
+                    }
                     CGB_TRY(eval_dev(x, slot));
-                    k_ctl_judge<<<1, 1, 0, st>>>(gs, d, hb);
+                    k_ctl_judge<<<1, 1, 0, st>>>(gs, d, hb, ha);
                     CGB_CUDA(cudaGetLastError());
                     return CGB_OK;
                 }));
@@ -1075,9 +1136,9 @@ struct Solver {
             st = s0;
             CGB_CUDA(cudaStreamBeginCaptureToGraph(s0, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
             int rc = [&]() -> int {
-                if (!reuse) return iteration(s0, s1, s2, hbt, hcont, -1, [] { return CGB_OK; });
-                return iteration(s0, s1, s2, hbt, hcont, 0, [&]() -> int {
-                    return iteration(s2, s3, s4, hbt2, hcont2, 1, [] { return CGB_OK; });
+                if (!reuse) return iteration(s0, s1, s2, hbt, hcont, hq, -1, [] { return CGB_OK; });
+                return iteration(s0, s1, s2, hbt, hcont, hq, 0, [&]() -> int {
+                    return iteration(s2, s3, s4, hbt2, hcont2, hq2, 1, [] { return CGB_OK; });
                 });
             }();
             cudaGraph_t done = nullptr;
@@ -1088,6 +1149,7 @@ struct Solver {
             CGB_CUDA(cudaGraphInstantiate(&exec, graph, 0));
             return CGB_OK;
         };
+        const int calls_init = calls;  // the captures below count their calls once more
         int rc = build();
         st = user;
         if (rc == CGB_OK) {
@@ -1121,9 +1183,12 @@ struct Solver {
         res->iterations = G.it;
         res->stopping_criterion = G.crit;
         res->backtracks = G.backtracks;
-        // init: 2 (gradient) + 1 (Rayleigh quotient); per evaluation 1; per gradient 2, or 1
-        // when A x_hat comes from the stored rows
-        res->operator_calls = calls + (G.it + G.backtracks) + (reuse ? 1 : 2) * (G.it - 1);
+        res->anchors = G.anchors;
+        // init: 2 (gradient) + 1 (Rayleigh quotient); per evaluation 1 (an anchored iteration
+        // evaluates x once more and x_hat once); per gradient 2, or 1 when A x_hat comes from
+        // the stored rows
+        res->operator_calls =
+            calls_init + (G.it + G.backtracks + 2 * G.anchors) + (reuse ? 1 : 2) * (G.it - 1);
         return CGB_OK;
     }
 };
@@ -1451,7 +1516,10 @@ struct BatchSolver {
         CGB_TRY(fetch());
         std::vector<double> step(P), told(P, 1.0), prev_obj(P), qfval(P), res_norm(P), reg_x(P), curr(P, 0.0),
             abs_obj(P, 0.0), rel_obj(P, 0.0), abs_x(P, 0.0), rel_x(P, 0.0), cc(P, 0.0), ca(P), cb(P);
-        std::vector<int> crit(P, 4), iters(P, 1), bts(P, 0), cur(P, 0), sa(P), sb(P);
+        std::vector<int> crit(P, 4), iters(P, 1), bts(P, 0), cur(P, 0), sa(P), sb(P), bt_it(P, 0);
+        std::vector<char> anchored(P, 0);
+        std::vector<int> anchors(P, 0);
+        const int max_bt = prm->max_backtracks > 0 ? prm->max_backtracks : (prm->max_backtracks < 0 ? 0 : 1000);
         for (int p = 0; p < P; ++p) {
             const double *h = hb + 16 * p;
             res_norm[p] = sqrt(h[12]);
@@ -1487,14 +1555,41 @@ struct BatchSolver {
             for (int p : J) {
                 const double *h = hb + 16 * p;
                 qfval[p] = it == 1 ? prev_obj[p] : 0.5 * sqrt(h[12]) * sqrt(h[12]);
+                anchored[p] = 0;
+                bt_it[p] = 0;
                 double q;
                 judge(p, q);
                 if (curr[p] > q) B.push_back(p);
             }
             while (!B.empty()) {
+                // a qfval from the stored rows is evaluated again directly on the first
+                // failure of the test and the same step judged again (as in Solver::run)
+                std::vector<int> An;
                 for (int p : B) {
-                    step[p] *= beta;
-                    bts[p]++;
+                    if (reuse_on && it > 1 && !anchored[p]) {
+                        anchored[p] = 1;
+                        anchors[p]++;
+                        An.push_back(p);
+                    } else {
+                        if (bt_it[p] >= max_bt)
+                            return fail(CGB_ERR_BACKTRACK, "batched FISTA: backtracking of problem " +
+                                                                    std::to_string(p) + ", iteration " +
+                                                                    std::to_string(it) + " reached its cap of " +
+                                                                    std::to_string(max_bt) + " step reductions");
+                        bt_it[p]++;
+                        step[p] *= beta;
+                        bts[p]++;
+                    }
+                }
+                if (!An.empty()) {
+                    std::vector<double *> xh(P, nullptr);
+                    for (int p : An) xh[p] = S[p].ws.xhat;
+                    CGB_TRY(forward(An, xh.data(), y32, 0, nullptr));
+                    CGB_TRY(fetch());
+                    for (int p : An) {
+                        const double r = sqrt(hb[16 * p]);
+                        qfval[p] = 0.5 * r * r;
+                    }
                 }
                 CGB_TRY(eval(B));
                 std::vector<int> B2;
@@ -1559,6 +1654,7 @@ struct BatchSolver {
             r.stopping_criterion = crit[p];
             r.backtracks = bts[p];
             r.operator_calls = 0;
+            r.anchors = anchors[p];
         }
         if (P > 0) res[0].operator_calls = calls;
         CGB_CUDA(cudaStreamSynchronize(st));

@@ -253,7 +253,7 @@ def _is_identity(prox, n) -> bool:
 def _fista(y, A, spec: RegSpec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, arith, momentum_reuse, x_ref=None,
            graph=False, max_backtracks=0, restart=False):
     """With x_ref given, details['trace'] holds, per accepted iteration, the seconds since
-    the solve started and |x_k - x_ref| / |x_ref|."""
+    the solve started, |x_k - x_ref| / |x_ref| and the cost function."""
     if not isinstance(A, LinearOperator):
         raise TypeError('A must be a commit_gb300.operator.LinearOperator')
     if A.adjoint:
@@ -287,10 +287,11 @@ def _fista(y, A, spec: RegSpec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, a
     if x_ref is not None:
         xr = torch.as_tensor(np.asarray(x_ref, dtype=np.float64) if not isinstance(x_ref, torch.Tensor) else x_ref,
                              dtype=torch.float64).to(dev).contiguous()
-        trace = np.full((int(max_iter), 2), np.nan)
+        trace = np.full((int(max_iter), 3), np.nan)
         prm.x_ref = xr.data_ptr()
         prm.trace = trace.ctypes.data
         prm.trace_len = int(max_iter)
+        prm.trace_cost = 1
     res = _lib.CgbFistaResult()
     st = torch.cuda.current_stream(dev).cuda_stream
     check(lib().cgb_fista_run(A.handle, ctypes.c_void_p(yd.data_ptr()),
@@ -305,6 +306,7 @@ def _fista(y, A, spec: RegSpec, sqrt_W, tol_fun, tol_x, max_iter, verbose, x0, a
         details['trace'] = trace[:int(res.iterations)]
     details['backtracks'] = int(res.backtracks)
     details['operator_calls'] = int(res.operator_calls)
+    details['anchors'] = int(res.anchors)
     x = xd.cpu().numpy() if host else xd
     return x, details
 
@@ -416,7 +418,7 @@ def solve_batch(y, A, regularisations, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, 
         det = {'residual': r.residual, 'regterm': r.regterm, 'cost_function': r.cost_function,
                'abs_cost': r.abs_cost, 'rel_cost': r.rel_cost, 'abs_x': r.abs_x, 'rel_x': r.rel_x,
                'iterations': int(r.iterations), 'stopping_criterion': _lib.CRITERIA[r.stopping_criterion],
-               'backtracks': int(r.backtracks)}
+               'backtracks': int(r.backtracks), 'anchors': int(r.anchors)}
         if p == 0:
             det['batch_operator_calls'] = int(r.operator_calls)
         out.append((xs[p].cpu().numpy() if host else xs[p], det))

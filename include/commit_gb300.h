@@ -281,6 +281,8 @@ typedef struct {
     int restart;          /* 1: reset the momentum (t = 1) after an iteration whose objective     */
                           /* rose (function-value restart, O'Donoghue & Candes 2015); 0 is the   */
                           /* reference's FISTA.  Host-driven loop only.                          */
+    int trace_cost;       /* 1: the trace holds 3 doubles per iteration (3*trace_len), the third  */
+                          /* the cost function of accepted iteration k                           */
 } cgb_fista_params;
 
 typedef struct {
@@ -289,6 +291,9 @@ typedef struct {
     int stopping_criterion; /* 0 abs obj, 1 rel obj, 2 abs x, 3 rel x, 4 max iter          */
     int backtracks;
     int operator_calls;     /* number of A and A' products                                  */
+    int anchors;            /* with momentum reuse: iterations whose qfval was evaluated    */
+                            /* again directly after the test failed (f(x_hat) from the      */
+                            /* stored rows rounds differently from the evaluation of x)     */
 } cgb_fista_result;
 
 /*

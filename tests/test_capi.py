@@ -43,8 +43,8 @@ def test_library_loads_through_binding():
 
 def test_structs_match_header_layout():
     # field order/sizes of the ctypes mirrors (natural C alignment, LP64)
-    assert ctypes.sizeof(_lib.CgbFistaParams) == 8 * 2 + 4 * 4 + 8 * 2 + 4 * 4
-    assert ctypes.sizeof(_lib.CgbFistaResult) == 8 * 7 + 4 * 4
+    assert ctypes.sizeof(_lib.CgbFistaParams) == 8 * 2 + 4 * 4 + 8 * 2 + 4 * 6  # 5 ints, padded to 8 bytes
+    assert ctypes.sizeof(_lib.CgbFistaResult) == 8 * 7 + 4 * 6  # 5 ints, padded to 8 bytes
     assert _lib.CgbReg.coeff_weights.offset == 6 * 8 + 6 * 4 + 4 * 8
     assert _lib.CgbReg.level_ptr.offset == _lib.CgbReg.ngroups.offset + 8
 

@@ -119,6 +119,7 @@ def test_graph_mode_matches_host_loop(name, variant, reuse):
     assert dg['iterations'] == dh['iterations'] == f['details']['iterations']
     assert dg['stopping_criterion'] == dh['stopping_criterion'] == f['details']['stopping_criterion']
     assert dg['backtracks'] == dh['backtracks']
+    assert dg['anchors'] == dh['anchors']
     assert np.array_equal(xg, xh)
     assert G.rel(xg, f['x']) <= 1e-8
     for k in ('residual', 'regterm', 'cost_function', 'abs_cost', 'rel_cost', 'abs_x', 'rel_x'):
@@ -169,3 +170,32 @@ def test_backtracking_cap_ends_the_solve():
         assert d2['iterations'] == d['iterations'] and d2['backtracks'] == d['backtracks']
         break
     assert found, 'no golden fit backtracks'
+
+
+@pytest.mark.parametrize('name', ['szb', 'multi_rf'])
+def test_solve_far_past_convergence(name):
+    """Tolerances off, 4000 nnls iterations: near the minimum the sufficient-decrease test is
+    decided at the rounding level.  With momentum reuse qfval comes from the stored rows and
+    rounds differently from the evaluation of x; the solver then evaluates f(x_hat) directly
+    (an anchor) instead of shrinking the step without end.  Host loop (with and without
+    restart) and graph finish every iteration, the graph with the host loop's iterates bit
+    for bit, and all reach the no-reuse solution."""
+    from commit_gb300 import solvers
+    from commit_gb300.operator import LinearOperator
+    c = G.load_case(name)
+    f = c['fits']['nnls']
+    A = LinearOperator(c['D'], c['K'], None, nolut=c['nolut'])
+    kw = dict(tol_fun=0.0, tol_x=0.0, max_iter=4000, verbose=0)
+    reg = lambda: solvers.init_regularisation(G.fresh_reg(f['reg']))  # noqa: E731
+    x0, d0 = solvers.solve(c['y_obs'], A, A.T, regularisation=reg(), momentum_reuse=False, **kw)
+    xh, dh = solvers.solve(c['y_obs'], A, A.T, regularisation=reg(), **kw)
+    xg, dg = solvers.solve(c['y_obs'], A, A.T, regularisation=reg(), graph=True, **kw)
+    xr, dr = solvers.solve(c['y_obs'], A, A.T, regularisation=reg(), restart=True, **kw)
+    assert d0['anchors'] == 0
+    for d in (dh, dg, dr):
+        assert d['iterations'] == 4000
+    assert dh['anchors'] > 0 and dg['anchors'] == dh['anchors']
+    assert np.array_equal(xg, xh)
+    for x in (xh, xr):
+        assert G.rel(x, x0) <= 1e-8
+    assert dh['cost_function'] <= d0['cost_function'] * (1 + 1e-12)
