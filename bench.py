@@ -76,7 +76,7 @@ def parse():
                         'iterations): batched BF16 solves polished by a per-problem FP64 solve, against '
                         'sequential plain solves to the same tolerance')
     p.add_argument('--batch-max', type=int, default=1000, help='iteration cap per solve with --batch-tol')
-    p.add_argument('--batch-streams', type=int, default=4, help='tractograms solved concurrently (streams)')
+    p.add_argument('--batch-streams', type=int, default=8, help='tractograms solved concurrently (streams)')
     p.add_argument('--sample-frac', type=float, default=0.25, help='CPU sample: fraction of the segments')
     p.add_argument('--no-e2e', action='store_true')
     p.add_argument('--no-cpu', action='store_true')

@@ -64,6 +64,7 @@ struct OpDev {
     const uint32_t *eval;           // [nF*nIC]
     const uint32_t *fib_ptr;        // [nF+1] fibre f owns fib_perm[fib_ptr[f] .. fib_ptr[f+1])
     const uint32_t *fib_perm;       // [n] voxel-order positions grouped by fibre
+    const uint32_t *fib_order;      // [nF] fibres by their first position (fibre-pass order)
     const uint32_t *ec_ptr;         // [nV+1]
     const uint32_t *ec_col;         // [nE] EC element (column) of each voxel-ordered entry
     const uint16_t *ec_o;           // [nE]
@@ -117,7 +118,7 @@ struct cgb_op {
     int batch_reuse;                // batched FISTA momentum reuse chosen by timing (0: not tuned, 1 off, 2 on)
     int occ_choice[24];             // occupancy build per tuned kernel (0: not tuned, 1 or 2), see occ_launch
     float occ_ms[24][2];            // the two builds' times measured by the tuning
-    uint32_t *vox_ptr, *seg_f, *eval, *fib_ptr, *fib_perm, *ec_ptr, *ec_col, *iso_ptr, *iso_col;
+    uint32_t *vox_ptr, *seg_f, *eval, *fib_ptr, *fib_perm, *fib_order, *ec_ptr, *ec_col, *iso_ptr, *iso_col;
     uint16_t *seg_o, *ec_o;
     float *seg_l;
     double *scratch;                // [nIC*n] per-segment adjoint terms (FP64 path)
@@ -137,15 +138,16 @@ struct cgb_op {
     // slab gathers them from L2 right after the voxel pass wrote them (see run_adjoint)
     int nslab;                      // 1: no slabs
     int *slab_v;                    // host [nslab+1] voxel boundaries
-    uint32_t *fib_slab;             // device [(nslab+1) * nF]: fibre f's fib_perm index where slab s starts
+    uint32_t *fib_slab;             // device [(nslab+1) * nF]: where slab s starts in the position list of
+                                    // the fibre at pass position fq (fib_order[fq])
+    double *fib_acc;                // device [nF * nIC]: running fibre sums between slabs, pass order
     cudaStream_t slab_st[3];        // slab schedule streams (created on first use)
     cudaEvent_t slab_ev[68];
     cudaEvent_t pipe_ev[8];
     // tensor-core BF16 forward (tc_forward.cu), laid out on first use
     int tc_mode;                    // 0 automatic, 1 CUDA cores only, 2 tensor cores
     int tc_ready;                   // entries and LUT images built
-    int tc_np, tc_nkb, tc_ntiles;   // padded samples, K-blocks of 64 LUT rows, tiles of 128 voxels
-    int tc_kb_ec;                   // first K-block of the EC / ISO rows
+    int tc_np, tc_nkb, tc_ntiles;   // padded samples, IC K-blocks of 64 LUT rows, tiles of 128 voxels
     float tc_lscale;                // 2^-k of the FP16 lengths
     uint32_t *tc_ptr, *tc_co;       // entry offsets per (tile, K-block, voxel); column | row << 26
     __half *tc_l;                   // entry lengths (FP16, scaled by 2^k)
@@ -155,9 +157,11 @@ struct cgb_op {
     int tc_kbs, tc_rounds;          // adjoint: sample K-blocks of 64, rounds of 256 LUT rows
     int64_t tc_nent;                // entries
     uint32_t *tc_fptr, *tc_fperm;   // adjoint: IC entry positions grouped by column, CSR offsets
+    uint32_t *tc_ford;              // adjoint: IC columns by their first entry position (fibre-pass order)
     __nv_bfloat16 *tc_abimg;        // adjoint LUT images
     float *tc_terms;                // adjoint IC terms in entry order
     float *tc_ax;                   // A x rows for the gradient (FISTA), on demand
+    __nv_bfloat16 *tc_ec16, *tc_iso16;  // EC / ISO LUT rows as BF16, row stride tc_np
     size_t bytes;
     int nsm;
     cgb::OpDev dev() const;

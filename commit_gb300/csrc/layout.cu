@@ -141,6 +141,13 @@ int csr_offsets(const uint32_t *keys, int64_t n, int nkeys, uint32_t *ptr, Temp 
 }
 
 // stable sort of (key, iota) pairs; returns the permutation in perm_out.
+// first voxel-order position of each fibre's segments (n for a fibre without segments)
+__global__ void k_fib_first(const uint32_t *__restrict__ fib_ptr, const uint32_t *__restrict__ fib_perm, int nF,
+                            uint32_t n, uint32_t *__restrict__ key) {
+    const int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (f < nF) key[f] = fib_ptr[f] < fib_ptr[f + 1] ? fib_perm[fib_ptr[f]] : n;
+}
+
 template <class K>
 int sort_perm(const K *keys, int64_t n, int end_bit, uint32_t *perm_out, Temp &tmp) {
     if (n == 0) return CGB_OK;
@@ -179,7 +186,7 @@ cgb::OpDev cgb_op::dev() const {
     d.lutIC = lutIC; d.lutEC = lutEC; d.lutISO = lutISO;
     d.lutIC_r = lutIC_r; d.lutEC_r = lutEC_r;
     d.vox_ptr = vox_ptr; d.seg_f = seg_f; d.seg_o = seg_o; d.seg_l = seg_l; d.seg_l16 = seg_l16;
-    d.eval = eval; d.fib_ptr = fib_ptr; d.fib_perm = fib_perm;
+    d.eval = eval; d.fib_ptr = fib_ptr; d.fib_perm = fib_perm; d.fib_order = fib_order;
     d.ec_ptr = ec_ptr; d.ec_col = ec_col; d.ec_o = ec_o;
     d.iso_ptr = iso_ptr; d.iso_col = iso_col;
     d.xmax = xmax_on ? d_xmax : nullptr;
@@ -195,18 +202,22 @@ using namespace cgb;
 // pass).  Cutting the voxels into slabs of about kSlabTermBytes of FP64 terms and running
 // the fibre pass of each slab right after its voxel pass (overlapped, see slab_schedule)
 // keeps most gathers in L2.  fib_slab[s*nF + f] is the first entry of fibre f's
-// (ascending) position list that lies in slab s.
+// (ascending) position list that lies in slab s, for the fibre f = fib_order[fq] at pass
+// position fq (fib_slab[s*nF + fq]), so the passes read it, and their running sums in
+// fib_acc, in order.
 constexpr double kSlabTermBytes = 128.0 * (1 << 20);  // measured best band: 8-12 slabs at 1M streamlines
 
-__global__ void k_fib_slabs(const uint32_t *__restrict__ fib_ptr, const uint32_t *__restrict__ fib_perm, int nF,
-                            int S, const uint32_t *__restrict__ slab_pos, uint32_t *__restrict__ fib_slab) {
-    const int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (f >= nF) return;
+__global__ void k_fib_slabs(const uint32_t *__restrict__ fib_ptr, const uint32_t *__restrict__ fib_perm,
+                            const uint32_t *__restrict__ fib_order, int nF, int S,
+                            const uint32_t *__restrict__ slab_pos, uint32_t *__restrict__ fib_slab) {
+    const int64_t fq = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (fq >= nF) return;
+    const uint32_t f = fib_order[fq];
     uint32_t k = fib_ptr[f];
     const uint32_t end = fib_ptr[f + 1];
     for (int s = 0; s <= S; ++s) {
         while (k < end && fib_perm[k] < slab_pos[s]) ++k;
-        fib_slab[(size_t)s * nF + f] = k;
+        fib_slab[(size_t)s * nF + fq] = k;
     }
 }
 
@@ -217,6 +228,10 @@ static int build_slabs(cgb_op *op, int want = 0) {
     if (op->fib_slab) {
         cudaFree(op->fib_slab);
         op->fib_slab = nullptr;
+    }
+    if (op->fib_acc) {
+        cudaFree(op->fib_acc);
+        op->fib_acc = nullptr;
     }
     const double bytes = (double)op->n * (op->nIC > 0 ? op->nIC : 1) * sizeof(double);
     int S = want > 0 ? want : (int)(bytes / kSlabTermBytes + 0.5);
@@ -235,13 +250,18 @@ static int build_slabs(cgb_op *op, int want = 0) {
     uint32_t *dpos = nullptr;
     CGB_CUDA(cudaMalloc((void **)&dpos, pos.size() * sizeof(uint32_t)));
     CGB_CUDA(cudaMemcpy(dpos, pos.data(), pos.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
-    const cudaError_t e = cudaMalloc((void **)&op->fib_slab, (size_t)(S + 1) * op->nF * sizeof(uint32_t));
+    cudaError_t e = cudaMalloc((void **)&op->fib_slab, (size_t)(S + 1) * op->nF * sizeof(uint32_t));
+    if (e == cudaSuccess)
+        e = cudaMalloc((void **)&op->fib_acc, (size_t)op->nF * (op->nIC > 0 ? op->nIC : 1) * sizeof(double));
     if (e != cudaSuccess) {
         cudaFree(dpos);
+        cudaFree(op->fib_slab);
         op->fib_slab = nullptr;
+        op->fib_acc = nullptr;
         return cuda_fail(e, "cudaMalloc");
     }
-    k_fib_slabs<<<(op->nF + 255) / 256, 256>>>(op->fib_ptr, op->fib_perm, op->nF, S, dpos, op->fib_slab);
+    k_fib_slabs<<<(op->nF + 255) / 256, 256>>>(op->fib_ptr, op->fib_perm, op->fib_order, op->nF, S, dpos,
+                                                op->fib_slab);
     const cudaError_t e2 = cudaGetLastError();
     cudaDeviceSynchronize();
     cudaFree(dpos);
@@ -257,11 +277,11 @@ static void free_op(cgb_op *op) {
     if (!op) return;
     free_grad_state(op);
     void *ptrs[] = {op->lutIC, op->lutEC, op->lutISO, op->lutIC_p, op->lutEC_p, op->lutISO_p, op->lutIC_r, op->lutEC_r, op->lutISO_r, op->seg_l16, op->vox_ptr,
-                    op->seg_f, op->eval, op->fib_ptr, op->fib_perm, op->ec_ptr, op->ec_col, op->iso_ptr,
+                    op->seg_f, op->eval, op->fib_ptr, op->fib_perm, op->fib_order, op->ec_ptr, op->ec_col, op->iso_ptr,
                     op->iso_col, op->seg_o, op->ec_o, op->seg_l, op->scratch, op->scratch32, op->partials,
-                    op->dscal, op->d_in, op->d_out, op->d_x64, op->fib_slab, op->d_xmax,
+                    op->dscal, op->d_in, op->d_out, op->d_x64, op->fib_slab, op->fib_acc, op->d_xmax,
                     op->tc_ptr, op->tc_co, op->tc_l, op->tc_bimg, op->tc_xe, op->tc_err,
-                    op->tc_fptr, op->tc_fperm, op->tc_abimg, op->tc_terms, op->tc_ax};
+                    op->tc_fptr, op->tc_fperm, op->tc_abimg, op->tc_terms, op->tc_ax, op->tc_ec16, op->tc_iso16, op->tc_ford};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (op->h_scal) cudaFreeHost(op->h_scal);
@@ -425,6 +445,15 @@ static int create_impl(int device, int nS, int ndirs, int nF, int64_t n, int nE,
     } else {
         CGB_CUDA(cudaMemset(op->fib_ptr, 0, ((size_t)nF + 1) * sizeof(uint32_t)));
     }
+    // the fibres in the order of their first segment's voxel-order position: threads of the
+    // fibre passes that are neighbours gather terms that are neighbours
+    CGB_TRY(dalloc(op, &op->fib_order, (size_t)nF));
+    if (nF > 0) {
+        uint32_t *fkey;
+        CGB_TRY(tmp.alloc(&fkey, (size_t)nF));
+        k_fib_first<<<grid_for(nF), 256>>>(op->fib_ptr, op->fib_perm, nF, (uint32_t)n, fkey);
+        CGB_TRY(sort_perm(fkey, nF, bits_for((uint64_t)n + 1), op->fib_order, tmp));
+    }
 
     // EC / ISO voxel CSR with original column indices
     CGB_TRY(dalloc(op, &op->ec_ptr, (size_t)nV + 1));
@@ -570,7 +599,9 @@ int cgb_op_set_slabs(cgb_op *op, int nslab, int *out) {
         delete[] op->slab_v;
         op->slab_v = new int[2]{0, op->nV};
         if (op->fib_slab) cudaFree(op->fib_slab);
+        if (op->fib_acc) cudaFree(op->fib_acc);
         op->fib_slab = nullptr;
+        op->fib_acc = nullptr;
         op->nslab = 1;
     }
     if (op->partials) cudaFree(op->partials);

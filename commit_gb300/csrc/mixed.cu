@@ -75,11 +75,12 @@ __global__ void k_fibre_sum32(const OpDev P, const float *__restrict__ scr, doub
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
          q += (int64_t)gridDim.x * blockDim.x) {
         const int i = (int)(q / P.nF);
-        const uint32_t f = (uint32_t)(q - (int64_t)i * P.nF);
+        const uint32_t f = P.fib_order[q - (int64_t)i * P.nF];
         const float *S = scr + (size_t)i * P.n;
         double s = 0.0;
         for (uint32_t k = P.fib_ptr[f]; k < P.fib_ptr[f + 1]; ++k) s += (double)S[P.fib_perm[k]];
-        xout[q] = s * (double)P.eval[q];
+        const int64_t c = (int64_t)i * P.nF + f;
+        xout[c] = s * (double)P.eval[c];
     }
 }
 
@@ -104,18 +105,23 @@ int fibre_sum32(cgb_op *op, double *xout, cudaStream_t st) {
 }  // namespace
 
 __global__ void k_fibre_sum32_slab(const OpDev P, const float *__restrict__ scr, double *__restrict__ xout,
-                                   const uint32_t *__restrict__ fib_slab, int s, int S) {
+                                   const uint32_t *__restrict__ fib_slab, double *__restrict__ accb, int s, int S) {
     const int64_t total = (int64_t)P.nF * P.nIC;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
          q += (int64_t)gridDim.x * blockDim.x) {
         const int i = (int)(q / P.nF);
-        const uint32_t f = (uint32_t)(q - (int64_t)i * P.nF);
-        const uint32_t beg = fib_slab[(size_t)s * P.nF + f], end = fib_slab[(size_t)(s + 1) * P.nF + f];
+        const int64_t fq = q - (int64_t)i * P.nF;
+        const uint32_t beg = fib_slab[(size_t)s * P.nF + fq], end = fib_slab[(size_t)(s + 1) * P.nF + fq];
         if (s > 0 && s < S - 1 && beg == end) continue;
         const float *T = scr + (size_t)i * P.n;
-        double acc = s == 0 ? 0.0 : xout[q];
+        double acc = s == 0 ? 0.0 : accb[q];
         for (uint32_t k = beg; k < end; ++k) acc += (double)T[P.fib_perm[k]];
-        xout[q] = s == S - 1 ? acc * (double)P.eval[q] : acc;
+        if (s == S - 1) {
+            const int64_t c = (int64_t)i * P.nF + P.fib_order[fq];
+            xout[c] = acc * (double)P.eval[c];
+        } else {
+            accb[q] = acc;
+        }
     }
 }
 
@@ -124,7 +130,7 @@ int fibre_sum32_slab(cgb_op *op, const float *scr, double *xout, int s, cudaStre
         const int64_t total = (int64_t)op->nF * op->nIC;
         int gb = (int)((total + 255) / 256);
         if (gb > op->nsm * 16) gb = op->nsm * 16;
-        k_fibre_sum32_slab<<<gb, 256, 0, st>>>(op->dev(), scr, xout, op->fib_slab, s, op->nslab);
+        k_fibre_sum32_slab<<<gb, 256, 0, st>>>(op->dev(), scr, xout, op->fib_slab, op->fib_acc, s, op->nslab);
         CGB_CUDA(cudaGetLastError());
     }
     return CGB_OK;

@@ -24,18 +24,20 @@ int adjoint_ff(cgb_op *op, const double *yin, int in_mode, const double *x, cons
                double *partials, cudaStream_t st, int *grid);
 
 namespace detail {
-// second A' pass: per-fibre sums of the voxel-ordered segment terms
+// second A' pass: per-fibre sums of the voxel-ordered segment terms, fibres in the order
+// of their first segment (fib_order)
 __global__ void k_fibre_sum(const OpDev P, const double *__restrict__ scratch, double *__restrict__ xout) {
     const int64_t total = (int64_t)P.nF * P.nIC;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
          q += (int64_t)gridDim.x * blockDim.x) {
         const int i = (int)(q / P.nF);
-        const uint32_t f = (uint32_t)(q - (int64_t)i * P.nF);
+        const uint32_t f = P.fib_order[q - (int64_t)i * P.nF];
         const uint32_t beg = P.fib_ptr[f], end = P.fib_ptr[f + 1];
         const double *S = scratch + (size_t)i * P.n;
         double s = 0.0;
         for (uint32_t k = beg; k < end; ++k) s += S[P.fib_perm[k]];
-        xout[q] = s * (double)P.eval[q];
+        const int64_t c = (int64_t)i * P.nF + f;
+        xout[c] = s * (double)P.eval[c];
     }
 }
 
@@ -108,22 +110,27 @@ __global__ void k_adjoint_nolut(const OpDev P, const double *__restrict__ yin, i
     if (partials) block_sum_store(nrm, partials + (size_t)blockIdx.x * kRedSlots);
 }
 
-// fibre pass of slab s: the running sums of the fibres continue from xout (slab 0 starts
-// at 0), terms in the fibre's position order, so the sums are those of k_fibre_sum; the
-// last slab applies eval
+// fibre pass of slab s, fibres in pass order (fib_order): the running sums continue from
+// acc (slab 0 starts at 0), terms in the fibre's position order, so the sums are those of
+// k_fibre_sum; the last slab applies eval and writes the fibre's column
 __global__ void k_fibre_sum_slab(const OpDev P, const double *__restrict__ scratch, double *__restrict__ xout,
-                                 const uint32_t *__restrict__ fib_slab, int s, int S) {
+                                 const uint32_t *__restrict__ fib_slab, double *__restrict__ accb, int s, int S) {
     const int64_t total = (int64_t)P.nF * P.nIC;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
          q += (int64_t)gridDim.x * blockDim.x) {
         const int i = (int)(q / P.nF);
-        const uint32_t f = (uint32_t)(q - (int64_t)i * P.nF);
-        const uint32_t beg = fib_slab[(size_t)s * P.nF + f], end = fib_slab[(size_t)(s + 1) * P.nF + f];
+        const int64_t fq = q - (int64_t)i * P.nF;
+        const uint32_t beg = fib_slab[(size_t)s * P.nF + fq], end = fib_slab[(size_t)(s + 1) * P.nF + fq];
         if (s > 0 && s < S - 1 && beg == end) continue;
         const double *T = scratch + (size_t)i * P.n;
-        double acc = s == 0 ? 0.0 : xout[q];
+        double acc = s == 0 ? 0.0 : accb[q];
         for (uint32_t k = beg; k < end; ++k) acc += T[P.fib_perm[k]];
-        xout[q] = s == S - 1 ? acc * (double)P.eval[q] : acc;
+        if (s == S - 1) {
+            const int64_t c = (int64_t)i * P.nF + P.fib_order[fq];
+            xout[c] = acc * (double)P.eval[c];
+        } else {
+            accb[q] = acc;
+        }
     }
 }
 
@@ -205,7 +212,7 @@ int fibre_sum_slab(cgb_op *op, double *xout, int s, cudaStream_t st) {
         const int64_t total = (int64_t)op->nF * op->nIC;
         int gb = (int)((total + 255) / 256);
         if (gb > op->nsm * 16) gb = op->nsm * 16;
-        k_fibre_sum_slab<<<gb, 256, 0, st>>>(P, op->scratch, xout, op->fib_slab, s, op->nslab);
+        k_fibre_sum_slab<<<gb, 256, 0, st>>>(P, op->scratch, xout, op->fib_slab, op->fib_acc, s, op->nslab);
         CGB_CUDA(cudaGetLastError());
     }
     return CGB_OK;

@@ -2,22 +2,25 @@
 // accumulation), followed by the per-fibre FP64 sums.
 //
 // The voxel pass of A' needs, for every item of voxel v, the dot product of its LUT row k
-// with the voxel's input row z (setup_operator.py:591-710 forms one per segment).  Over a
-// tile of 128 voxels these are the entries of the dense product G = Z * L^T (128 x every
-// LUT row): the kernel loads the tile's rows of z (y, or the weighted residual of the FISTA
-// gradient) once, splits them into BF16 high and low parts in shared memory (K-major, 64
-// samples per K-block), and multiplies them with the BF16 LUT rows, 256 rows per round,
-// into one half of tensor memory while the previous round's half is read back: for each
-// item of the round's rows the drain warps form l * G[v, k] and write it -- IC items to a
-// term array in entry order (the tile-ordered entry stream of tc_forward.cu), EC / ISO
-// items straight to their column of x.  The IC columns are then the sums of their terms,
-// gathered per fibre in entry order through an entry-order fibre index (deterministic,
-// FP64 sums, as the CUDA-core path).
+// with the voxel's input row z (setup_operator.py:591-710 forms one per segment).  For the
+// IC compartment these are, over a tile of 128 voxels, the entries of the dense product
+// G = Z * L^T (128 x every IC LUT row): the kernel loads the tile's rows of z (y, or the
+// weighted residual of the FISTA gradient) once, splits them into BF16 high and low parts
+// in shared memory (K-major, 64 samples per K-block), and multiplies them with the BF16
+// LUT rows, 256 rows per round, into one half of tensor memory while the previous round's
+// half is read back: for each IC item of the round's rows the drain warps form l * G[v, k]
+// and write it to a term array in entry order (the tile-ordered entry stream of
+// tc_forward.cu).  The IC columns are then the sums of their terms, gathered per fibre in
+// entry order through an entry-order fibre index (deterministic, FP64 sums, as the
+// CUDA-core path).  The EC and ISO items (one or two per voxel) are dot products of the
+// same BF16 rows of z with their BF16 LUT rows on the CUDA cores, written straight to
+// their column of x.
 //
 // Warp roles (256 threads, one CTA per SM): all threads load and split Z; warp 4's first
 // lane fetches the LUT row images (bulk copies, 2 stages) and issues the MMAs; warps 0-3
-// (one per TMEM lane quarter) drain the accumulators, 64 LUT rows (one K-block) at a time.
-// Every wait is bounded (tc_ptx.cuh).
+// (one per TMEM lane quarter) drain the accumulators, 64 LUT rows (one K-block) at a time;
+// warps 5-7 compute the EC / ISO dot products meanwhile.  Every wait is bounded
+// (tc_ptx.cuh).
 #include <cub/cub.cuh>
 
 #include "operator_launch.cuh"
@@ -36,7 +39,13 @@ constexpr int kADrainStride = 65;   // floats per drain staging row (64 columns 
 constexpr uint32_t kAColBits = 26;
 
 struct TcAdjArgs {
-    int nV, nS, KBS, R, NKB, kb_ec, ntiles;
+    int nV, nS, KBS, R, NKB, ntiles, Np;
+    // EC / ISO items (voxel-ordered arrays of the handle) and their BF16 LUT rows (stride Np)
+    int nE, nEC, nISOv, nISO, ndirs;
+    int64_t ec_base, iso_base;
+    const uint32_t *ec_ptr, *ec_col, *iso_ptr, *iso_col;
+    const uint16_t *ec_o;
+    const __nv_bfloat16 *lut_ec, *lut_iso;
     const uint32_t *ent_ptr, *ent_co;
     const __half *ent_l;
     float l_scale;
@@ -63,6 +72,35 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
         v[i] = a[i];
         v[16 + i] = b[i];
     }
+}
+
+// dot product of row m of the tile's z (BF16 hi + lo, K-major swizzled in shared memory)
+// with a BF16 LUT row of stride Np, FP32, samples in order
+__device__ __forceinline__ float z_dot_row(const uint8_t *a_hi, const uint8_t *a_lo, int m, int KBS, int Np,
+                                           const __nv_bfloat16 *row) {
+    float acc = 0.f;
+    const uint32_t rbase = (uint32_t)(m >> 3) * 1024u + (uint32_t)(m & 7) * 128u;
+    for (int kb = 0; kb < KBS; ++kb) {
+#pragma unroll 4
+        for (int p = 0; p < 8; ++p) {
+            const int s0 = kb * 64 + p * 8;
+            if (s0 >= Np) break;
+            const uint32_t off = (uint32_t)kb * 16384u + rbase + (uint32_t)((p ^ (m & 7)) * 16);
+            const uint4 h = *reinterpret_cast<const uint4 *>(a_hi + off);
+            const uint4 l = *reinterpret_cast<const uint4 *>(a_lo + off);
+            const uint4 w = __ldg(reinterpret_cast<const uint4 *>(row + s0));
+            const uint32_t hw[4] = {h.x, h.y, h.z, h.w}, lw[4] = {l.x, l.y, l.z, l.w}, ww[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const float w0 = __uint_as_float(ww[e] << 16), w1 = __uint_as_float(ww[e] & 0xffff0000u);
+                acc = fmaf(__uint_as_float(hw[e] << 16), w0, acc);
+                acc = fmaf(__uint_as_float(lw[e] << 16), w0, acc);
+                acc = fmaf(__uint_as_float(hw[e] & 0xffff0000u), w1, acc);
+                acc = fmaf(__uint_as_float(lw[e] & 0xffff0000u), w1, acc);
+            }
+        }
+    }
+    return acc;
 }
 
 __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) {
@@ -221,9 +259,9 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
                     const size_t pb = ((size_t)tile * A.NKB + kbf) * kATile + vloc;
                     uint32_t j = A.ent_ptr[pb];
                     const uint32_t p1 = A.ent_ptr[pb + 1];
-                    const float lsc = kbf < A.kb_ec ? A.l_scale : 1.f;
+                    const float lsc = A.l_scale;
                     // the K-block's 64 columns of this voxel into its private row; the items
-                    // of the K-block may come in any row order (EC items keep their file order)
+                    // of the K-block come in segment order, not row order
                     __syncwarp();
 #pragma unroll
                     for (int c = 0; c < 2; ++c) {
@@ -237,15 +275,36 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
                         const uint32_t co = A.ent_co[j];
                         const uint32_t o = co >> kAColBits;
                         if (o >= 64u) continue;  // not produced by the layout; never indexes outside the row
-                        const float t = row[o] * (__half2float(A.ent_l[j]) * lsc);
-                        if (kbf < A.kb_ec) A.terms[j] = t;
-                        else A.xout[co & ((1u << kAColBits) - 1u)] = (double)t;
+                        A.terms[j] = row[o] * (__half2float(A.ent_l[j]) * lsc);
                     }
                 }
                 tc::tc_fence_before();
                 tc::mbar_arrive(&drained[rg & 1u]);
             }
             rgd += (uint32_t)A.R;
+        } else if (warp > 4) {
+            // (4) EC / ISO items of the tile's voxels: dot products with the rows of z
+            for (int m = tid - 5 * 32; m < kATile; m += kAThreads - 5 * 32) {
+                const int v = tile * kATile + m;
+                if (v >= A.nV) break;
+                if (A.ec_ptr) {
+                    for (uint32_t e = A.ec_ptr[v]; e < A.ec_ptr[v + 1]; ++e) {
+                        const int64_t cb = A.ec_base + A.ec_col[e];
+                        const size_t ro = (size_t)A.ec_o[e];
+                        for (int i = 0; i < A.nEC; ++i)
+                            A.xout[cb + (int64_t)i * A.nE] = (double)z_dot_row(
+                                a_hi, a_lo, m, A.KBS, A.Np, A.lut_ec + ((size_t)i * A.ndirs + ro) * A.Np);
+                    }
+                }
+                if (A.iso_ptr) {
+                    for (uint32_t e = A.iso_ptr[v]; e < A.iso_ptr[v + 1]; ++e) {
+                        const int64_t cb = A.iso_base + A.iso_col[e];
+                        for (int i = 0; i < A.nISO; ++i)
+                            A.xout[cb + (int64_t)i * A.nISOv] =
+                                (double)z_dot_row(a_hi, a_lo, m, A.KBS, A.Np, A.lut_iso + (size_t)i * A.Np);
+                    }
+                }
+            }
         }
         if (__syncthreads_or(bad)) break;
     }
@@ -263,15 +322,17 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
     if (warp == 0) tc::tmem_dealloc(tmem, 512);
 }
 
-// x[q] = eval[q] * sum of the IC column's terms, gathered in entry order (FP64 sums)
+// x[c] = eval[c] * sum of IC column c's terms, gathered in entry order (FP64 sums); the
+// columns in the order of their first entry (ford)
 __global__ void k_fibre_sum_entries(const uint32_t *__restrict__ fptr, const uint32_t *__restrict__ fperm,
-                                    const float *__restrict__ terms, const uint32_t *__restrict__ eval, int64_t ncols,
-                                    double *__restrict__ xout) {
+                                    const uint32_t *__restrict__ ford, const float *__restrict__ terms,
+                                    const uint32_t *__restrict__ eval, int64_t ncols, double *__restrict__ xout) {
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < ncols;
          q += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t c = ford[q];
         double s = 0.0;
-        for (uint32_t k = fptr[q]; k < fptr[q + 1]; ++k) s += (double)terms[fperm[k]];
-        xout[q] = s * (double)eval[q];
+        for (uint32_t k = fptr[c]; k < fptr[c + 1]; ++k) s += (double)terms[fperm[k]];
+        xout[c] = s * (double)eval[c];
     }
 }
 
@@ -297,8 +358,24 @@ int adjoint_tc(cgb_op *op, int mode, const float *yin, const float *axa, const f
     A.KBS = op->tc_kbs;
     A.R = op->tc_rounds;
     A.NKB = op->tc_nkb;
-    A.kb_ec = op->tc_kb_ec;
     A.ntiles = op->tc_ntiles;
+    A.Np = op->tc_np;
+    const bool ec = op->nE > 0 && op->nEC > 0, iso = op->nISOv > 0 && op->nISO > 0;
+    const OpDev P = op->dev();
+    A.nE = op->nE;
+    A.nEC = ec ? op->nEC : 0;
+    A.nISOv = op->nISOv;
+    A.nISO = iso ? op->nISO : 0;
+    A.ndirs = op->ndirs;
+    A.ec_base = P.ec_base;
+    A.iso_base = P.iso_base;
+    A.ec_ptr = ec ? op->ec_ptr : nullptr;
+    A.ec_col = op->ec_col;
+    A.ec_o = op->ec_o;
+    A.iso_ptr = iso ? op->iso_ptr : nullptr;
+    A.iso_col = op->iso_col;
+    A.lut_ec = op->tc_ec16;
+    A.lut_iso = op->tc_iso16;
     A.ent_ptr = op->tc_ptr;
     A.ent_co = op->tc_co;
     A.ent_l = op->tc_l;
@@ -324,7 +401,8 @@ int adjoint_tc(cgb_op *op, int mode, const float *yin, const float *axa, const f
     if (nic > 0) {
         int64_t gb = (nic + 255) / 256;
         if (gb > (int64_t)op->nsm * 16) gb = (int64_t)op->nsm * 16;
-        k_fibre_sum_entries<<<(int)gb, 256, 0, st>>>(op->tc_fptr, op->tc_fperm, op->tc_terms, op->eval, nic, xout);
+        k_fibre_sum_entries<<<(int)gb, 256, 0, st>>>(op->tc_fptr, op->tc_fperm, op->tc_ford, op->tc_terms, op->eval,
+                                                      nic, xout);
         CGB_CUDA(cudaGetLastError());
     }
     if (grid) *grid = g;

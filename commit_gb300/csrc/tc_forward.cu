@@ -1,31 +1,35 @@
 // Reduced-precision A*x on the tensor cores (tcgen05, BF16 operands, FP32 accumulation).
 //
 // A*x is, voxel by voxel, y[v, :] = sum_k C[v, k] * L[k, :] where k runs over the LUT rows
-// of every compartment (IC response i and orientation o, EC response i and orientation o,
-// ISO response i) and C[v, k] is the sum of l * x * eval over the voxel's items that use
-// row k (setup_operator.py:50-218 computes the same sums item by item).  Over a tile of 128
-// voxels this is a dense product C[128 x K] * L[K x nS]: the kernel builds C in shared
+// of every compartment and C[v, k] is the sum of l * x * eval over the voxel's items that
+// use row k (setup_operator.py:50-218 computes the same sums item by item).  For the IC
+// compartment (many segments per voxel, spread over every orientation) this is, over a
+// tile of 128 voxels, a dense product C[128 x K] * L[K x nS]: the kernel builds C in shared
 // memory 64 LUT rows at a time, splits it into BF16 high and low parts (C = hi + lo to
 // about 16 bits), and multiplies both with the BF16 LUT on the tensor cores into one FP32
-// accumulator of 128 x nS in tensor memory.  The LUT is the only reduced-precision
-// operand, as in the CUDA-core BF16 path (operator_mixed.cuh).
+// accumulator of 128 x nS in tensor memory.  The EC and ISO compartments have one or two
+// items per voxel, which would leave their K-blocks nearly empty; the epilogue adds them
+// on the CUDA cores (x * BF16 LUT row, FP32 FMAs in item order) to the accumulator rows it
+// reads back.  The LUT is the only reduced-precision operand, as in the CUDA-core BF16
+// path (operator_mixed.cuh).
 //
 // Data (built once per handle, ensure_tc):
-//  - entries: every (item, response) pair of the operator, ordered by (tile of 128
-//    voxels, K-block of 64 LUT rows, voxel, LUT row) -- ent_co = column of x | row in the
-//    K-block << 26, ent_l = FP16 length * 2^k (1 for EC / ISO) -- and ent_ptr, the
-//    first entry of each (tile, K-block, voxel), so a voxel's entries of one K-block are
-//    contiguous;
+//  - IC entries: every (segment, response) pair, ordered by (tile of 128 voxels, K-block
+//    of 64 LUT rows, voxel) -- ent_co = column of x | row in the K-block << 26, ent_l =
+//    FP16 length * 2^k -- and ent_ptr, the first entry of each (tile, K-block, voxel), so a
+//    voxel's entries of one K-block are contiguous;
 //  - B images: per K-block the LUT rows transposed to [Np samples x 64 rows] BF16 in the
-//    K-major 128-byte-swizzled layout of tc_ptx.cuh, fetched whole by one bulk copy.
+//    K-major 128-byte-swizzled layout of tc_ptx.cuh, fetched whole by one bulk copy;
+//  - the EC and ISO LUT rows as BF16 with row stride Np (read by the epilogue).
 //
 // Kernel: one CTA of 256 threads per SM (persistent over tiles), 2-stage pipeline over the
 // K-blocks of a tile: while the tensor cores multiply K-block b, the threads build the C
 // tile of block b+1 (two threads per voxel walk its entries into FP32 rows in shared
-// memory, in order, so results are deterministic) and one thread fetches its B image.
-// The 128 x Np accumulator (two MMAs of N = Np/2 per 16-row K step) is read back by the
-// 8 warps (lane quarter = warp % 4, column half = warp / 4) into y, with the residual-norm
-// epilogue of the CUDA-core kernel.
+// memory, in order, so results are deterministic; the entry offsets of the next K-block
+// are loaded one K-block ahead) and one thread fetches its B image.  The 128 x Np
+// accumulator (two MMAs of N = Np/2 per 16-row K step) is read back by the 8 warps (lane
+// quarter = warp % 4, column half = warp / 4), completed with the EC / ISO items and
+// written to y, with the residual-norm epilogue of the CUDA-core kernel.
 #include <cub/cub.cuh>
 
 #include "operator_launch.cuh"
@@ -44,7 +48,12 @@ constexpr int kTcMaxNp = 320;          // padded samples the shared-memory budge
 
 struct TcFwdArgs {
     int nV, nS, Np, NKB, ntiles;
-    int kb_ec;  // first K-block of EC / ISO rows (lengths 1, no 2^-k scale)
+    // EC / ISO items (voxel-ordered arrays of the handle) and their BF16 LUT rows
+    int nE, nEC, nISOv, nISO, ndirs;
+    int64_t ec_base, iso_base;
+    const uint32_t *ec_ptr, *ec_col, *iso_ptr, *iso_col;
+    const uint16_t *ec_o;
+    const __nv_bfloat16 *lut_ec, *lut_iso;
     const uint32_t *ent_ptr;
     const uint32_t *ent_co;
     const __half *ent_l;
@@ -60,6 +69,34 @@ struct TcFwdArgs {
 __host__ __device__ constexpr size_t tc_smem_bytes(int Np) {
     return 1024 /* alignment slack */ + 4 * 16384 /* A hi / lo x 2 stages */ + 2 * (size_t)Np * 128 /* B x 2 */ +
            2 * kTcTile * kStageStride * 4 /* FP32 staging, 2 parts */ + 128 /* barriers, TMEM slot, flags */;
+}
+
+// r[0..15] += xv * the 16 BF16 LUT values at row (16 consecutive samples, 32-byte aligned)
+__device__ __forceinline__ void fma_row16(float (&r)[16], float xv, const __nv_bfloat16 *row) {
+    const uint4 a = __ldg(reinterpret_cast<const uint4 *>(row)), b = __ldg(reinterpret_cast<const uint4 *>(row) + 1);
+    const uint32_t w[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        r[2 * i] = fmaf(xv, __uint_as_float(w[i] << 16), r[2 * i]);
+        r[2 * i + 1] = fmaf(xv, __uint_as_float(w[i] & 0xffff0000u), r[2 * i + 1]);
+    }
+}
+
+// the EC and ISO items of one voxel ([e0, e1) and [i0, i1) of the voxel-ordered arrays)
+// added to its samples [c0, c0 + 16)
+__device__ __forceinline__ void add_ec_iso(const TcFwdArgs &A, uint32_t e0, uint32_t e1, uint32_t i0, uint32_t i1,
+                                           int c0, float (&r)[16]) {
+    for (uint32_t e = e0; e < e1; ++e) {
+        const int64_t cb = A.ec_base + A.ec_col[e];
+        const size_t ro = (size_t)A.ec_o[e];
+        for (int i = 0; i < A.nEC; ++i)
+            fma_row16(r, A.xe[cb + (int64_t)i * A.nE], A.lut_ec + ((size_t)i * A.ndirs + ro) * A.Np + c0);
+    }
+    for (uint32_t e = i0; e < i1; ++e) {
+        const int64_t cb = A.iso_base + A.iso_col[e];
+        for (int i = 0; i < A.nISO; ++i)
+            fma_row16(r, A.xe[cb + (int64_t)i * A.nISOv], A.lut_iso + (size_t)i * A.Np + c0);
+    }
 }
 
 __global__ void __launch_bounds__(kTcThreads, 1) k_forward_tc(const TcFwdArgs A) {
@@ -109,6 +146,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_forward_tc(const TcFwdArgs A)
     bool stop = false;
 
     for (int tile = blockIdx.x; tile < A.ntiles && !stop; tile += gridDim.x) {
+        // the epilogue's voxel: its EC / ISO item ranges, loaded ahead of the K-blocks
+        const int ve = tile * kTcTile + (warp & 3) * 32 + lane;
+        uint32_t e0 = 0, e1 = 0, i0 = 0, i1 = 0;
+        if (ve < A.nV) {
+            if (A.ec_ptr) {
+                e0 = A.ec_ptr[ve];
+                e1 = A.ec_ptr[ve + 1];
+            }
+            if (A.iso_ptr) {
+                i0 = A.iso_ptr[ve];
+                i1 = A.iso_ptr[ve + 1];
+            }
+        }
+        // entry offsets of this thread's voxel, one K-block ahead
+        size_t pb = (size_t)tile * A.NKB * kTcTile + vloc;
+        uint32_t p0n = A.ent_ptr[pb], p1n = A.ent_ptr[pb + 1];
         for (int kb = 0; kb < A.NKB; ++kb, ++it) {
             const uint32_t s = it & 1u;
             // stage s is free once the MMAs of its previous use (two K-blocks ago) completed
@@ -122,8 +175,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_forward_tc(const TcFwdArgs A)
                 last_b[s] = it;
             }
             // C rows of this K-block: two threads per voxel, each over half of its entries
-            const size_t pb = ((size_t)tile * A.NKB + kb) * kTcTile + vloc;
-            const uint32_t p0 = A.ent_ptr[pb], p1 = A.ent_ptr[pb + 1];
+            const uint32_t p0 = p0n, p1 = p1n;
+            if (kb + 1 < A.NKB) {
+                pb += kTcTile;
+                p0n = A.ent_ptr[pb];
+                p1n = A.ent_ptr[pb + 1];
+            }
             const uint32_t hcount = (p1 - p0 + 1) >> 1;
             const uint32_t j0 = part ? p0 + hcount : p0, j1 = part ? p1 : p0 + hcount;
             for (uint32_t j = j0; j < j1; j += 8) {
@@ -148,7 +205,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_forward_tc(const TcFwdArgs A)
             __syncthreads();
             // FP32 rows -> BF16 hi / lo in the swizzled layout; staging back to zero
             uint8_t *ah = a_hi + s * 16384, *al = a_lo + s * 16384;
-            const float lsc = kb < A.kb_ec ? A.l_scale : 1.f;
+            const float lsc = A.l_scale;
 #pragma unroll
             for (int q = tid; q < kTcTile * 8; q += kTcThreads) {
                 const int m = q >> 3, p = q & 7, cl = p ^ (m & 7);
@@ -215,11 +272,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_forward_tc(const TcFwdArgs A)
         tc::tc_fence_after();
         if (__syncthreads_or(bad)) break;
         const int q = warp & 3, colh = warp >> 2;
-        const int v = tile * kTcTile + q * 32 + lane;
+        const int v = ve;
         float vn = 0.f;
         for (int c0 = colh * half; c0 < (colh + 1) * half; c0 += 16) {
             float r[16];
             tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, r);
+            add_ec_iso(A, e0, e1, i0, i1, c0, r);
             if (v < A.nV && vec4 && c0 + 16 <= A.nS && !A.partials) {
                 const size_t idx = (size_t)v * A.nS + c0;
 #pragma unroll
@@ -279,52 +337,26 @@ __device__ __forceinline__ int owner_of(const uint32_t *ptr, int nV, uint32_t j)
 
 struct TcLayoutArgs {
     const OpDev P;
-    int NKB, nkbd, kb_ec, kb_iso;
-    __half one;  // the length of an EC / ISO item (1; IC lengths are scaled by 2^k)
+    int NKB, nkbd;
 };
 
+// IC entries: key (tile, K-block, voxel in tile), value column | row << 26 | FP16 length << 32
 __global__ void k_tc_entries(const TcLayoutArgs L, const __half *__restrict__ l16, uint32_t *__restrict__ key,
                              unsigned long long *__restrict__ val) {
     const OpDev &P = L.P;
-    const int64_t nic = P.n * P.nIC, nec = (int64_t)P.nE * P.nEC, niso = (int64_t)P.nISOv * P.nISO;
-    const int64_t total = nic + nec + niso;
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
+    const int64_t nic = P.n * P.nIC;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nic;
          q += (int64_t)gridDim.x * blockDim.x) {
-        int v, kb;
-        uint32_t col, row;
-        __half l;
-        if (q < nic) {
-            const int i = (int)(q / P.n);
-            const uint32_t j = (uint32_t)(q - (int64_t)i * P.n);
-            v = owner_of(P.vox_ptr, P.nV, j);
-            const uint32_t o = P.seg_o[j];
-            kb = i * L.nkbd + (int)(o >> 6);
-            row = o & 63u;
-            col = (uint32_t)i * (uint32_t)P.nF + P.seg_f[j];
-            l = l16[j];
-        } else if (q < nic + nec) {
-            const int64_t r = q - nic;
-            const int i = (int)(r / P.nE);
-            const uint32_t e = (uint32_t)(r - (int64_t)i * P.nE);
-            v = owner_of(P.ec_ptr, P.nV, e);
-            const uint32_t o = P.ec_o[e];
-            kb = L.kb_ec + i * L.nkbd + (int)(o >> 6);
-            row = o & 63u;
-            col = (uint32_t)(P.ec_base + (int64_t)i * P.nE + P.ec_col[e]);
-            l = L.one;
-        } else {
-            const int64_t r = q - nic - nec;
-            const int i = (int)(r / P.nISOv);
-            const uint32_t e = (uint32_t)(r - (int64_t)i * P.nISOv);
-            v = owner_of(P.iso_ptr, P.nV, e);
-            kb = L.kb_iso;
-            row = (uint32_t)i;
-            col = (uint32_t)(P.iso_base + (int64_t)i * P.nISOv + P.iso_col[e]);
-            l = L.one;
-        }
+        const int i = (int)(q / P.n);
+        const uint32_t j = (uint32_t)(q - (int64_t)i * P.n);
+        const int v = owner_of(P.vox_ptr, P.nV, j);
+        const uint32_t o = P.seg_o[j];
+        const int kb = i * L.nkbd + (int)(o >> 6);
+        const uint32_t row = o & 63u;
+        const uint32_t col = (uint32_t)i * (uint32_t)P.nF + P.seg_f[j];
         key[q] = ((uint32_t)(v >> 7) * (uint32_t)L.NKB + (uint32_t)kb) * (uint32_t)kTcTile + (uint32_t)(v & 127);
         val[q] = (unsigned long long)(col | (row << kColBits)) |
-                 ((unsigned long long)__half_as_ushort(l) << 32);
+                 ((unsigned long long)__half_as_ushort(l16[j]) << 32);
     }
 }
 
@@ -338,41 +370,48 @@ __global__ void k_tc_split(const unsigned long long *__restrict__ val, int64_t n
     }
 }
 
-// LUT rows of every K-block as [Np samples x 64 rows] BF16, K-major, 128-byte swizzle
-__global__ void k_tc_bimg(const OpDev P, int Np, int NKB, int nkbd, int kb_ec, int kb_iso,
-                          __nv_bfloat16 *__restrict__ img) {
+// IC LUT rows of every K-block as [Np samples x 64 rows] BF16, K-major, 128-byte swizzle
+__global__ void k_tc_bimg(const OpDev P, int Np, int NKB, int nkbd, __nv_bfloat16 *__restrict__ img) {
     const int64_t total = (int64_t)NKB * Np * kTcKB;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
          q += (int64_t)gridDim.x * blockDim.x) {
         const int kb = (int)(q / ((int64_t)Np * kTcKB));
         const int r = (int)(q - (int64_t)kb * Np * kTcKB);
         const int s = r / kTcKB, k = r - s * kTcKB;
-        float v = 0.f;
-        if (s < P.nS) {
-            if (kb < kb_ec) {
-                const int i = kb / nkbd, o = (kb - i * nkbd) * kTcKB + k;
-                if (o < P.ndirs) v = P.lutIC[((size_t)i * P.ndirs + o) * P.nS + s];
-            } else if (kb < kb_iso) {
-                const int i = (kb - kb_ec) / nkbd, o = (kb - kb_ec - i * nkbd) * kTcKB + k;
-                if (o < P.ndirs) v = P.lutEC[((size_t)i * P.ndirs + o) * P.nS + s];
-            } else if (k < P.nISO) {
-                v = P.lutISO[(size_t)k * P.nS + s];
-            }
-        }
+        const int i = kb / nkbd, o = (kb - i * nkbd) * kTcKB + k;
+        const float v = (s < P.nS && o < P.ndirs) ? P.lutIC[((size_t)i * P.ndirs + o) * P.nS + s] : 0.f;
         img[(size_t)kb * Np * kTcKB + tc::sw128_offset((uint32_t)s, (uint32_t)k) / 2] = __float2bfloat16_rn(v);
     }
 }
 
-// IC entries (K-blocks before kb_ec) keyed by their column, for the entry-order fibre index
-__global__ void k_tc_fib_keys(const uint32_t *__restrict__ key, const uint32_t *__restrict__ co, int64_t n, int NKB,
-                              int kb_ec, uint32_t *__restrict__ ckey, uint32_t *__restrict__ pos,
-                              unsigned long long *__restrict__ nic) {
+// EC / ISO LUT rows as BF16 with row stride Np (zero padded)
+__global__ void k_tc_rows16(const float *__restrict__ lut, int rows, int nS, int Np, __nv_bfloat16 *__restrict__ out) {
+    const int64_t total = (int64_t)rows * Np;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = q / Np;
+        const int s = (int)(q - r * Np);
+        out[q] = __float2bfloat16_rn(s < nS ? lut[r * nS + s] : 0.f);
+    }
+}
+
+// IC entries keyed by their column, for the entry-order fibre index
+__global__ void k_tc_fib_keys(const uint32_t *__restrict__ co, int64_t n, uint32_t *__restrict__ ckey,
+                              uint32_t *__restrict__ pos) {
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-        const int kb = (int)((key[q] / (uint32_t)kTcTile) % (uint32_t)NKB);
-        const bool ic = kb < kb_ec;
-        ckey[q] = ic ? (co[q] & ((1u << kColBits) - 1u)) : 0xffffffffu;
+        ckey[q] = co[q] & ((1u << kColBits) - 1u);
         pos[q] = (uint32_t)q;
-        if (ic) atomicAdd(nic, 1ull);
+    }
+}
+
+// IC columns keyed by the entry position of their first term (nent without terms), for the
+// fibre pass order
+__global__ void k_tc_first(const uint32_t *__restrict__ fptr, const uint32_t *__restrict__ fperm, int64_t ncols,
+                           uint32_t nent, uint32_t *__restrict__ key, uint32_t *__restrict__ col) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < ncols;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        key[q] = fptr[q] < fptr[q + 1] ? fperm[fptr[q]] : nent;
+        col[q] = (uint32_t)q;
     }
 }
 
@@ -381,10 +420,10 @@ __global__ void k_tc_count(const uint32_t *__restrict__ ckey, int64_t n, uint32_
         atomicAdd(count + ckey[q], 1u);
 }
 
-// LUT rows as the B operand of the adjoint: per round of 256 rows, sample K-block and half,
-// [128 rows x 64 samples] BF16, K-major, 128-byte swizzle; row g is the forward's K index g
-__global__ void k_tca_bimg(const OpDev P, int R, int KBS, int NKB, int nkbd, int kb_ec, int kb_iso,
-                           __nv_bfloat16 *__restrict__ img) {
+// IC LUT rows as the B operand of the adjoint: per round of 256 rows, sample K-block and
+// half, [128 rows x 64 samples] BF16, K-major, 128-byte swizzle; row g is the forward's K
+// index g
+__global__ void k_tca_bimg(const OpDev P, int R, int KBS, int NKB, int nkbd, __nv_bfloat16 *__restrict__ img) {
     const int64_t total = (int64_t)R * KBS * 2 * 128 * 64;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
          q += (int64_t)gridDim.x * blockDim.x) {
@@ -395,15 +434,8 @@ __global__ void k_tca_bimg(const OpDev P, int R, int KBS, int NKB, int nkbd, int
         const int kbf = g / kTcKB, kk = g - kbf * kTcKB;
         float v = 0.f;
         if (s < P.nS && kbf < NKB) {
-            if (kbf < kb_ec) {
-                const int i = kbf / nkbd, o = (kbf - i * nkbd) * kTcKB + kk;
-                if (o < P.ndirs) v = P.lutIC[((size_t)i * P.ndirs + o) * P.nS + s];
-            } else if (kbf < kb_iso) {
-                const int i = (kbf - kb_ec) / nkbd, o = (kbf - kb_ec - i * nkbd) * kTcKB + kk;
-                if (o < P.ndirs) v = P.lutEC[((size_t)i * P.ndirs + o) * P.nS + s];
-            } else if (kk < P.nISO) {
-                v = P.lutISO[(size_t)kk * P.nS + s];
-            }
+            const int i = kbf / nkbd, o = (kbf - i * nkbd) * kTcKB + kk;
+            if (o < P.ndirs) v = P.lutIC[((size_t)i * P.ndirs + o) * P.nS + s];
         }
         img[item * 128 * 64 + tc::sw128_offset((uint32_t)row, (uint32_t)k) / 2] = __float2bfloat16_rn(v);
     }
@@ -430,35 +462,35 @@ int grid_of(int64_t n, int nsm) {
 
 using namespace detail;
 
-// Whether the tensor-core forward handles this operator: padded samples within the
-// shared-memory budget, columns within ent_co's 26 bits, at most 64 ISO responses.
+// Whether the tensor-core kernels handle this operator: an IC compartment with segments,
+// padded samples within the shared-memory budget, columns within ent_co's 26 bits.
 bool tc_supported(const cgb_op *op) {
     const int Np = (op->nS + 31) / 32 * 32;
-    const int64_t nent = op->n * op->nIC + (int64_t)op->nE * op->nEC + (int64_t)op->nISOv * op->nISO;
-    return !op->nolut && op->nV > 0 && Np <= kTcMaxNp && op->ncols < ((int64_t)1 << kColBits) && op->nISO <= 64 &&
-           nent > 0 && nent < ((int64_t)1 << 32);
+    const int64_t nent = op->n * op->nIC;
+    return !op->nolut && op->nV > 0 && Np <= kTcMaxNp && op->ncols < ((int64_t)1 << kColBits) && nent > 0 &&
+           nent < ((int64_t)1 << 32);
 }
 
 bool tc_forward_enabled(const cgb_op *op) { return op->tc_mode != 1 && tc_supported(op); }
 
-// entries, their per-(tile, K-block, voxel) offsets and the B images; needs the FP16
-// lengths of ensure_reduced
+// IC entries, their per-(tile, K-block, voxel) offsets, the B images and the BF16 EC / ISO
+// rows; needs the FP16 lengths of ensure_reduced
 int ensure_tc(cgb_op *op) {
     if (op->tc_ready) return CGB_OK;
     if (!tc_supported(op)) return fail(CGB_ERR_UNSUPPORTED, "tensor-core forward: operator shape not supported");
     const OpDev P = op->dev();
     const int nkbd = (op->ndirs + kTcKB - 1) / kTcKB;
-    const int kb_ec = op->nIC * nkbd;
-    const int kb_iso = kb_ec + ((op->nE > 0 && op->nEC > 0) ? op->nEC * nkbd : 0);
-    const int NKB = kb_iso + ((op->nISOv > 0 && op->nISO > 0) ? 1 : 0);
+    const int NKB = op->nIC * nkbd;
     const int Np = (op->nS + 31) / 32 * 32;
     const int ntiles = (op->nV + kTcTile - 1) / kTcTile;
-    const int64_t nent = op->n * op->nIC + (int64_t)op->nE * op->nEC + (int64_t)op->nISOv * op->nISO;
+    const int64_t nent = op->n * op->nIC;
+    const int64_t nec_rows = (op->nE > 0 && op->nEC > 0) ? (int64_t)op->nEC * op->ndirs : 0;
+    const int64_t niso_rows = (op->nISOv > 0 && op->nISO > 0) ? op->nISO : 0;
     const int64_t nkeys = (int64_t)ntiles * NKB * kTcTile;
     if (nkeys >= ((int64_t)1 << 32) - 1) return fail(CGB_ERR_UNSUPPORTED, "tensor-core forward: too many tiles");
     const int64_t ncount = nkeys + 1 > (int64_t)op->nF * op->nIC + 1 ? nkeys + 1 : (int64_t)op->nF * op->nIC + 1;
     const float lscale = op->len16_inv_scale > 0.f ? op->len16_inv_scale : 1.f;
-    TcLayoutArgs L{P, NKB, nkbd, kb_ec, kb_iso, __float2half_rn(1.f)};
+    TcLayoutArgs L{P, NKB, nkbd};
 
     uint32_t *key = nullptr, *key2 = nullptr, *count = nullptr;
     unsigned long long *val = nullptr, *val2 = nullptr;
@@ -478,6 +510,10 @@ int ensure_tc(cgb_op *op) {
        "cudaMalloc");
     cu(cudaMalloc((void **)&op->tc_xe, (size_t)(op->ncols > 0 ? op->ncols : 1) * sizeof(float)), "cudaMalloc");
     cu(cudaMalloc((void **)&op->tc_err, sizeof(int)), "cudaMalloc");
+    cu(cudaMalloc((void **)&op->tc_ec16, (size_t)(nec_rows > 0 ? nec_rows : 1) * Np * sizeof(__nv_bfloat16)),
+       "cudaMalloc");
+    cu(cudaMalloc((void **)&op->tc_iso16, (size_t)(niso_rows > 0 ? niso_rows : 1) * Np * sizeof(__nv_bfloat16)),
+       "cudaMalloc");
     cu(cudaMalloc((void **)&key, nent * sizeof(uint32_t)), "cudaMalloc");
     cu(cudaMalloc((void **)&key2, nent * sizeof(uint32_t)), "cudaMalloc");
     cu(cudaMalloc((void **)&val, nent * sizeof(unsigned long long)), "cudaMalloc");
@@ -500,8 +536,17 @@ int ensure_tc(cgb_op *op) {
         cu(cudaGetLastError(), "k_tc_split");
         cu(cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, count, op->tc_ptr, nkeys + 1), "cub scan");
         const int64_t nimg = (int64_t)NKB * Np * kTcKB;
-        k_tc_bimg<<<grid_of(nimg, op->nsm), 256>>>(P, Np, NKB, nkbd, kb_ec, kb_iso, op->tc_bimg);
+        k_tc_bimg<<<grid_of(nimg, op->nsm), 256>>>(P, Np, NKB, nkbd, op->tc_bimg);
         cu(cudaGetLastError(), "k_tc_bimg");
+        if (nec_rows > 0) {
+            k_tc_rows16<<<grid_of(nec_rows * Np, op->nsm), 256>>>(op->lutEC, (int)nec_rows, op->nS, Np, op->tc_ec16);
+            cu(cudaGetLastError(), "k_tc_rows16");
+        }
+        if (niso_rows > 0) {
+            k_tc_rows16<<<grid_of(niso_rows * Np, op->nsm), 256>>>(op->lutISO, (int)niso_rows, op->nS, Np,
+                                                                   op->tc_iso16);
+            cu(cudaGetLastError(), "k_tc_rows16");
+        }
         cu(cudaFuncSetAttribute(k_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes(Np)),
            "cudaFuncSetAttribute");
     }
@@ -511,28 +556,22 @@ int ensure_tc(cgb_op *op) {
     const int R = (NKB * kTcKB + 255) / 256;
     const int64_t nic_cols = (int64_t)op->nF * op->nIC;
     if (rc == CGB_OK) {
-        unsigned long long *dnic = nullptr;
-        cu(cudaMalloc((void **)&dnic, sizeof(unsigned long long)), "cudaMalloc");
-        cu(cudaMemset(dnic, 0, sizeof(unsigned long long)), "cudaMemset");
         // key / val buffers are reused: key <- column keys, (uint32 view of val) <- positions
         uint32_t *pos = reinterpret_cast<uint32_t *>(val), *pos2 = reinterpret_cast<uint32_t *>(val2);
-        k_tc_fib_keys<<<grid_of(nent, op->nsm), 256>>>(key2, op->tc_co, nent, NKB, kb_ec, key, pos, dnic);
+        k_tc_fib_keys<<<grid_of(nent, op->nsm), 256>>>(op->tc_co, nent, key, pos);
         cu(cudaGetLastError(), "k_tc_fib_keys");
-        unsigned long long hnic = 0;
-        cu(cudaMemcpy(&hnic, dnic, sizeof(hnic), cudaMemcpyDeviceToHost), "cudaMemcpy");
-        cudaFree(dnic);
+        const uint64_t hnic = (uint64_t)nent;
         int cbits = 1;
         while (cbits < 32 && (((uint64_t)nic_cols) >> cbits) != 0) ++cbits;
-        // non-IC entries carry key 0xffffffff: sort all 32 bits so they go last
         size_t need = 0;
-        cu(cub::DeviceRadixSort::SortPairs(nullptr, need, key, key2, pos, pos2, nent, 0, 32), "cub sort");
+        cu(cub::DeviceRadixSort::SortPairs(nullptr, need, key, key2, pos, pos2, nent, 0, cbits), "cub sort");
         if (need > tmp_bytes) {
             cudaFree(tmp);
             tmp = nullptr;
             tmp_bytes = need;
             cu(cudaMalloc(&tmp, tmp_bytes), "cudaMalloc");
         }
-        cu(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, key, key2, pos, pos2, nent, 0, 32), "cub sort");
+        cu(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, key, key2, pos, pos2, nent, 0, cbits), "cub sort");
         cu(cudaMalloc((void **)&op->tc_fperm, (hnic > 0 ? hnic : 1) * sizeof(uint32_t)), "cudaMalloc");
         cu(cudaMalloc((void **)&op->tc_fptr, (nic_cols + 1) * sizeof(uint32_t)), "cudaMalloc");
         if (rc == CGB_OK && hnic > 0)
@@ -551,9 +590,36 @@ int ensure_tc(cgb_op *op) {
             cu(cudaMalloc(&tmp, tmp_bytes), "cudaMalloc");
         }
         cu(cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, count, op->tc_fptr, nic_cols + 1), "cub scan");
+        // columns in the order of their first entry: neighbouring threads of the fibre pass
+        // gather neighbouring terms
+        uint32_t *fk = nullptr, *fk2 = nullptr, *fc = nullptr;
+        cu(cudaMalloc((void **)&fk, nic_cols * 2 * sizeof(uint32_t)), "cudaMalloc");
+        cu(cudaMalloc((void **)&fc, nic_cols * sizeof(uint32_t)), "cudaMalloc");
+        cu(cudaMalloc((void **)&op->tc_ford, nic_cols * sizeof(uint32_t)), "cudaMalloc");
+        if (rc == CGB_OK) {
+            fk2 = fk + nic_cols;
+            k_tc_first<<<grid_of(nic_cols, op->nsm), 256>>>(op->tc_fptr, op->tc_fperm, nic_cols, (uint32_t)nent, fk, fc);
+            cu(cudaGetLastError(), "k_tc_first");
+            int ebits = 1;
+            while (ebits < 32 && (((uint64_t)nent) >> ebits) != 0) ++ebits;
+            size_t fneed = 0;
+            cu(cub::DeviceRadixSort::SortPairs(nullptr, fneed, fk, fk2, fc, op->tc_ford, nic_cols, 0, ebits),
+               "cub sort");
+            if (fneed > tmp_bytes) {
+                cudaFree(tmp);
+                tmp = nullptr;
+                tmp_bytes = fneed;
+                cu(cudaMalloc(&tmp, tmp_bytes), "cudaMalloc");
+            }
+            cu(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, fk, fk2, fc, op->tc_ford, nic_cols, 0, ebits),
+               "cub sort");
+        }
+        cu(cudaDeviceSynchronize(), "tensor-core layout");
+        cudaFree(fk);
+        cudaFree(fc);
         cu(cudaMalloc((void **)&op->tc_abimg, (size_t)R * KBS * 2 * 128 * 64 * sizeof(__nv_bfloat16)), "cudaMalloc");
         if (rc == CGB_OK) {
-            k_tca_bimg<<<grid_of((int64_t)R * KBS * 2 * 128 * 64, op->nsm), 256>>>(P, R, KBS, NKB, nkbd, kb_ec, kb_iso,
+            k_tca_bimg<<<grid_of((int64_t)R * KBS * 2 * 128 * 64, op->nsm), 256>>>(P, R, KBS, NKB, nkbd,
                                                                                    op->tc_abimg);
             cu(cudaGetLastError(), "k_tca_bimg");
         }
@@ -569,14 +635,14 @@ int ensure_tc(cgb_op *op) {
     if (rc != CGB_OK) return rc;
     op->tc_np = Np;
     op->tc_nkb = NKB;
-    op->tc_kb_ec = kb_ec;
     op->tc_ntiles = ntiles;
     op->tc_lscale = lscale;
     op->tc_kbs = KBS;
     op->tc_rounds = R;
     op->tc_nent = nent;
     op->bytes += nent * 6 + (nkeys + 1) * 4 + (size_t)NKB * Np * kTcKB * 2 + (size_t)op->ncols * 4 + nent * 8 +
-                 (size_t)(nic_cols + 1) * 4 + (size_t)R * KBS * 2 * 128 * 64 * 2;
+                 (size_t)(nic_cols + 1) * 4 + (size_t)nic_cols * 4 + (size_t)R * KBS * 2 * 128 * 64 * 2 +
+                 (size_t)(nec_rows + niso_rows) * Np * 2;
     op->tc_ready = 1;
     return CGB_OK;
 }
@@ -595,8 +661,23 @@ int forward_tc(cgb_op *op, const double *x, float *y, float *ax, const float *yo
     A.nS = op->nS;
     A.Np = op->tc_np;
     A.NKB = op->tc_nkb;
-    A.kb_ec = op->tc_kb_ec;
     A.ntiles = op->tc_ntiles;
+    const bool ec = op->nE > 0 && op->nEC > 0, iso = op->nISOv > 0 && op->nISO > 0;
+    A.nE = op->nE;
+    A.nEC = ec ? op->nEC : 0;
+    A.nISOv = op->nISOv;
+    A.nISO = iso ? op->nISO : 0;
+    A.ndirs = op->ndirs;
+    const OpDev P = op->dev();
+    A.ec_base = P.ec_base;
+    A.iso_base = P.iso_base;
+    A.ec_ptr = ec ? op->ec_ptr : nullptr;
+    A.ec_col = op->ec_col;
+    A.ec_o = op->ec_o;
+    A.iso_ptr = iso ? op->iso_ptr : nullptr;
+    A.iso_col = op->iso_col;
+    A.lut_ec = op->tc_ec16;
+    A.lut_iso = op->tc_iso16;
     A.ent_ptr = op->tc_ptr;
     A.ent_co = op->tc_co;
     A.ent_l = op->tc_l;

@@ -425,15 +425,17 @@ def solve_batch(y, A, regularisations, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, 
     return out
 
 
-def solve_batches(jobs, n_streams: int = 4, **kw):
+def solve_batches(jobs, n_streams: int = 8, **kw):
     """Regularisation paths on several operators (e.g. tractograms of uneven size) at once.
 
-    jobs: list of (y, A, regularisations).  Each job runs ``solve_batch`` on its own CUDA
-    stream from its own host thread (the library releases the GIL and allocates
-    stream-ordered), up to n_streams at a time, so the device overlaps one job's host
-    decisions and small passes with another job's work.  Returns one list of (x, details)
-    per job, in order."""
-    from concurrent.futures import ThreadPoolExecutor
+    jobs: list of (y, A, regularisations).  Each job runs ``solve_batch`` on a CUDA stream
+    from a host thread (the library releases the GIL and allocates stream-ordered), up to
+    n_streams at a time, so the device overlaps one job's host decisions and small passes
+    with another job's work.  Jobs are taken largest first (segments x problems) from one
+    queue by whichever stream is free, so the last jobs to finish are the small ones.
+    Returns one list of (x, details) per job, in order."""
+    import queue
+    import threading
     if not jobs:
         return []
     n_streams = max(1, min(int(n_streams), len(jobs)))
@@ -441,22 +443,36 @@ def solve_batches(jobs, n_streams: int = 4, **kw):
     streams = [torch.cuda.Stream(device=devs[0]) for _ in range(n_streams)]
     for s in streams:
         s.wait_stream(torch.cuda.current_stream(devs[0]))
+    order = sorted(range(len(jobs)), key=lambda k: -(jobs[k][1].ICn * jobs[k][1].ICnRF * max(1, len(jobs[k][2]))))
+    todo = queue.Queue()
+    for k in order:
+        todo.put(k)
+    res, errors = {}, []
 
-    def run(k):
-        y, A, regs = jobs[k]
-        s = streams[k % n_streams]
-        with torch.cuda.device(devs[k]), torch.cuda.stream(s):
-            out = solve_batch(y, A, regs, **kw)
-        s.synchronize()
-        return out
+    def worker(w):
+        s = streams[w]
+        while True:
+            try:
+                k = todo.get_nowait()
+            except queue.Empty:
+                return
+            try:
+                y, A, regs = jobs[k]
+                with torch.cuda.device(devs[k]), torch.cuda.stream(s):
+                    res[k] = solve_batch(y, A, regs, **kw)
+                s.synchronize()
+            except BaseException as e:  # noqa: BLE001 - re-raised on the calling thread
+                errors.append(e)
+                return
 
     if n_streams == 1:
-        return [run(k) for k in range(len(jobs))]
-    # job k uses stream k % n_streams: a worker per stream keeps each stream's jobs in order
-    with ThreadPoolExecutor(max_workers=n_streams) as ex:
-        futs = [ex.submit(lambda w=w: [(k, run(k)) for k in range(w, len(jobs), n_streams)])
-                for w in range(n_streams)]
-        res = {}
-        for f in futs:
-            res.update(dict(f.result()))
+        worker(0)
+    else:
+        threads = [threading.Thread(target=worker, args=(w,)) for w in range(n_streams)]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+    if errors:
+        raise errors[0]
     return [res[k] for k in range(len(jobs))]
