@@ -262,6 +262,7 @@ struct GState {
     int bt_iter, max_bt;  // backtracks of the current iteration and their cap
     int reuse;            // A x_hat of the gradient pass comes from the stored rows
     int anchored;         // this iteration's qfval was evaluated again directly
+    int anchor_req;       // the next backtracking evaluation starts with that evaluation
     int anchors;          // such evaluations over the solve
 };
 
@@ -280,6 +281,11 @@ __global__ void k_ctl_begin(GState *S, const double *h) {
     S->anchored = 0;
 }
 
+// whether this backtracking evaluation starts with a direct evaluation of f(x_hat)
+__global__ void k_ctl_anchor_decide(const GState *S, cudaGraphConditionalHandle anchor) {
+    cudaGraphSetConditional(anchor, S->anchor_req);
+}
+
 // qfval from a direct evaluation of x_hat (slot 0 of h), replacing the stored-row one
 __global__ void k_ctl_anchor(GState *S, const double *h) {
     const double r = __dsqrt_rn(h[0]);
@@ -292,9 +298,8 @@ __global__ void k_ctl_anchor(GState *S, const double *h) {
 // from the stored rows is rounded differently from the evaluation of x, so near convergence
 // the test can fail at the rounding level for every step; its first failure in an iteration
 // asks instead for f(x_hat) evaluated directly, as the reference computes it, and the same
-// step is judged again (`anchor`)
-__global__ void k_ctl_judge(GState *S, const double *h, cudaGraphConditionalHandle bt,
-                            cudaGraphConditionalHandle anchor) {
+// step is judged again (anchor_req)
+__global__ void k_ctl_judge(GState *S, const double *h, cudaGraphConditionalHandle bt) {
     const double reg = g_omega(*S, h);
     const double d2 = __dsqrt_rn(h[2]);
     const double q = __dadd_rn(__dadd_rn(__dadd_rn(S->qfval, h[1]), __dmul_rn(__ddiv_rn(0.5, S->step), __dmul_rn(d2, d2))),
@@ -304,24 +309,21 @@ __global__ void k_ctl_judge(GState *S, const double *h, cudaGraphConditionalHand
     S->reg_x = reg;
     S->res_norm = rn;
     S->curr_obj = cur;
+    int an = 0, more = 0;
     if (cur > q && S->reuse && S->it > 1 && !S->anchored) {
         S->anchored = 1;
-        cudaGraphSetConditional(anchor, 1);
-        cudaGraphSetConditional(bt, 1);
+        an = 1;
+        more = 1;
     } else if (cur > q && S->bt_iter >= S->max_bt) {
         S->crit = -1;  // cap reached: leave the backtracking loop, k_ctl_stop ends the solve
-        cudaGraphSetConditional(anchor, 0);
-        cudaGraphSetConditional(bt, 0);
     } else if (cur > q) {
         S->step = __dmul_rn(0.9, S->step);
         S->backtracks += 1;
         S->bt_iter += 1;
-        cudaGraphSetConditional(anchor, 0);
-        cudaGraphSetConditional(bt, 1);
-    } else {
-        cudaGraphSetConditional(anchor, 0);
-        cudaGraphSetConditional(bt, 0);
+        more = 1;
     }
+    S->anchor_req = an;
+    cudaGraphSetConditional(bt, more);
 }
 
 // stopping tests (solvers.py:335-357) and the FISTA coefficients (solvers.py:359-368)
@@ -1068,20 +1070,27 @@ struct Solver {
             CGB_CUDA(cudaStreamCreateWithFlags(&s3, cudaStreamNonBlocking));
             CGB_CUDA(cudaStreamCreateWithFlags(&s4, cudaStreamNonBlocking));
             CGB_CUDA(cudaGraphCreate(&graph, 0));
-            cudaGraphConditionalHandle hmain, hbt, hcont, hbt2, hcont2, hq, hq2;
-            CGB_CUDA(cudaGraphConditionalHandleCreate(&hq, graph, 0, cudaGraphCondAssignDefault));
-            CGB_CUDA(cudaGraphConditionalHandleCreate(&hq2, graph, 0, cudaGraphCondAssignDefault));
+            // every handle belongs to exactly one conditional node: the anchors' IF nodes
+            // exist only with momentum reuse, and so do their handles
+            cudaGraphConditionalHandle hmain, hbt, hcont, hbt2 = 0, hcont2 = 0, hq = 0, hq2 = 0;
+            if (reuse) {
+                CGB_CUDA(cudaGraphConditionalHandleCreate(&hq, graph, 0, cudaGraphCondAssignDefault));
+                CGB_CUDA(cudaGraphConditionalHandleCreate(&hq2, graph, 0, cudaGraphCondAssignDefault));
+            }
             CGB_CUDA(cudaGraphConditionalHandleCreate(&hmain, graph, 1, cudaGraphCondAssignDefault));
             CGB_CUDA(cudaGraphConditionalHandleCreate(&hbt, graph, 0, cudaGraphCondAssignDefault));
             CGB_CUDA(cudaGraphConditionalHandleCreate(&hcont, graph, 0, cudaGraphCondAssignDefault));
-            CGB_CUDA(cudaGraphConditionalHandleCreate(&hbt2, graph, 0, cudaGraphCondAssignDefault));
-            CGB_CUDA(cudaGraphConditionalHandleCreate(&hcont2, graph, 0, cudaGraphCondAssignDefault));
+            if (reuse) {
+                CGB_CUDA(cudaGraphConditionalHandleCreate(&hbt2, graph, 0, cudaGraphCondAssignDefault));
+                CGB_CUDA(cudaGraphConditionalHandleCreate(&hcont2, graph, 0, cudaGraphCondAssignDefault));
+            }
             const int64_t nr = op->nrows;
             // one iteration captured on `cap`: evaluation into stored row `slot` (-1: none),
             // backtracking (WHILE(bt) { IF(anchor) { f(x_hat) directly }; eval; judge }),
             // stopping test, and for a continuing iteration the momentum, the gradient at
-            // x_hat and then `more`.  The anchor's body is captured on `sif`, which is free
-            // until the backtracking node is complete.
+            // x_hat and then `more`.  The anchor's IF node and the kernel that sets its handle
+            // sit in the backtracking body; its body is captured on `sif`, which is free until
+            // the backtracking node is complete.
             std::function<int(cudaStream_t, cudaStream_t, cudaStream_t, cudaGraphConditionalHandle,
                               cudaGraphConditionalHandle, cudaGraphConditionalHandle, int, std::function<int()>)>
                 iteration = [&](cudaStream_t cap, cudaStream_t sbt, cudaStream_t sif, cudaGraphConditionalHandle hb,
@@ -1090,10 +1099,12 @@ struct Solver {
                 k_ctl_begin<<<1, 1, 0, cap>>>(gs, d);
                 CGB_CUDA(cudaGetLastError());
                 CGB_TRY(eval_dev(x, slot));
-                k_ctl_judge<<<1, 1, 0, cap>>>(gs, d, hb, ha);
+                k_ctl_judge<<<1, 1, 0, cap>>>(gs, d, hb);
                 CGB_CUDA(cudaGetLastError());
                 CGB_TRY(conditional(cap, sbt, hb, cudaGraphCondTypeWhile, [&]() -> int {
                     if (reuse) {
+                        k_ctl_anchor_decide<<<1, 1, 0, st>>>(gs, ha);
+                        CGB_CUDA(cudaGetLastError());
                         CGB_TRY(conditional(st, sif, ha, cudaGraphCondTypeIf, [&]() -> int {
                             CGB_TRY(objective(ws.xhat, -1));
                             k_ctl_anchor<<<1, 1, 0, st>>>(gs, d);
@@ -1102,7 +1113,7 @@ struct Solver {
                         }));
                     }
                     CGB_TRY(eval_dev(x, slot));
-                    k_ctl_judge<<<1, 1, 0, st>>>(gs, d, hb, ha);
+                    k_ctl_judge<<<1, 1, 0, st>>>(gs, d, hb);
                     CGB_CUDA(cudaGetLastError());
                     return CGB_OK;
                 }));

@@ -271,11 +271,25 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
 #pragma unroll
                         for (int i = 0; i < 32; ++i) row[c * 32 + i] = g[i];
                     }
-                    for (; j < p1; ++j) {
-                        const uint32_t co = A.ent_co[j];
-                        const uint32_t o = co >> kAColBits;
-                        if (o >= 64u) continue;  // not produced by the layout; never indexes outside the row
-                        A.terms[j] = row[o] * (__half2float(A.ent_l[j]) * lsc);
+                    // four entries per step, their loads issued together
+                    for (; j < p1; j += 4) {
+                        uint32_t co[4];
+                        float l[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            co[u] = 0xffffffffu;
+                            l[u] = 0.f;
+                            if (j + u < p1) {
+                                co[u] = A.ent_co[j + u];
+                                l[u] = __half2float(A.ent_l[j + u]);
+                            }
+                        }
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const uint32_t o = co[u] >> kAColBits;
+                            // o < 64 always holds for the layout's entries; never indexes outside the row
+                            if (j + u < p1 && o < 64u) A.terms[j + u] = row[o] * (l[u] * lsc);
+                        }
                     }
                 }
                 tc::tc_fence_before();
