@@ -145,6 +145,33 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_forward_tc(const TcFwdArgs A)
     int bad = 0;
     bool stop = false;
 
+    // this thread's half of its voxel's entries of the next K-block to walk: [cj0, cj1), the
+    // first 8 of them (column | row, length) already in registers
+    uint32_t cj0 = 0, cj1 = 0;
+    uint32_t pco[8];
+    float pc[8];
+    auto half_range = [&](uint32_t p0, uint32_t p1, uint32_t &j0, uint32_t &j1) {
+        const uint32_t hcount = (p1 - p0 + 1) >> 1;
+        j0 = part ? p0 + hcount : p0;
+        j1 = part ? p1 : p0 + hcount;
+    };
+    auto load8 = [&](uint32_t j0, uint32_t j1) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            pco[u] = 0;
+            pc[u] = 0.f;
+            if (j0 + u < j1) {
+                pco[u] = __ldg(A.ent_co + j0 + u);
+                pc[u] = __half2float(A.ent_l[j0 + u]);
+            }
+        }
+    };
+    if ((int)blockIdx.x < A.ntiles) {
+        const size_t pb = (size_t)blockIdx.x * A.NKB * kTcTile + vloc;
+        half_range(A.ent_ptr[pb], A.ent_ptr[pb + 1], cj0, cj1);
+        load8(cj0, cj1);
+    }
+
     for (int tile = blockIdx.x; tile < A.ntiles && !stop; tile += gridDim.x) {
         // the epilogue's voxel: its EC / ISO item ranges, loaded ahead of the K-blocks
         const int ve = tile * kTcTile + (warp & 3) * 32 + lane;
@@ -159,9 +186,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_forward_tc(const TcFwdArgs A)
                 i1 = A.iso_ptr[ve + 1];
             }
         }
-        // entry offsets of this thread's voxel, one K-block ahead
-        size_t pb = (size_t)tile * A.NKB * kTcTile + vloc;
-        uint32_t p0n = A.ent_ptr[pb], p1n = A.ent_ptr[pb + 1];
         for (int kb = 0; kb < A.NKB; ++kb, ++it) {
             const uint32_t s = it & 1u;
             // stage s is free once the MMAs of its previous use (two K-blocks ago) completed
@@ -174,33 +198,44 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_forward_tc(const TcFwdArgs A)
                 tc::bulk_g2s(b_img + s * bbytes, A.bimg + (size_t)kb * A.Np * kTcKB, bbytes, &bfull[s]);
                 last_b[s] = it;
             }
-            // C rows of this K-block: two threads per voxel, each over half of its entries
-            const uint32_t p0 = p0n, p1 = p1n;
-            if (kb + 1 < A.NKB) {
-                pb += kTcTile;
-                p0n = A.ent_ptr[pb];
-                p1n = A.ent_ptr[pb + 1];
+            // the K-block after this one (this tile's next, or the next tile's first): its
+            // entry offsets load during this block's walk, its first entries after it
+            int nt = tile, nk = kb + 1;
+            if (nk == A.NKB) {
+                nt += gridDim.x;
+                nk = 0;
             }
-            const uint32_t hcount = (p1 - p0 + 1) >> 1;
-            const uint32_t j0 = part ? p0 + hcount : p0, j1 = part ? p1 : p0 + hcount;
-            for (uint32_t j = j0; j < j1; j += 8) {
-                uint32_t co[8];
-                float c[8];
+            const bool has_next = nt < A.ntiles;
+            uint32_t n0 = 0, n1 = 0;
+            if (has_next) {
+                const size_t pb = ((size_t)nt * A.NKB + nk) * kTcTile + vloc;
+                n0 = A.ent_ptr[pb];
+                n1 = A.ent_ptr[pb + 1];
+            }
+            // C rows of this K-block: two threads per voxel, each over half of its entries;
+            // the first 8 were loaded during the previous K-block
+            for (uint32_t j = cj0; j < cj1; j += 8) {
+                if (j != cj0) {
 #pragma unroll
-                for (int u = 0; u < 8; ++u) {
-                    co[u] = 0;
-                    c[u] = 0.f;
-                    if (j + u < j1) {
-                        co[u] = __ldg(A.ent_co + j + u);
-                        c[u] = __half2float(A.ent_l[j + u]);
+                    for (int u = 0; u < 8; ++u) {
+                        pco[u] = 0;
+                        pc[u] = 0.f;
+                        if (j + u < cj1) {
+                            pco[u] = __ldg(A.ent_co + j + u);
+                            pc[u] = __half2float(A.ent_l[j + u]);
+                        }
                     }
                 }
 #pragma unroll
                 for (int u = 0; u < 8; ++u)
-                    if (j + u < j1) c[u] *= __ldg(A.xe + (co[u] & ((1u << kColBits) - 1u)));
+                    if (j + u < cj1) pc[u] *= __ldg(A.xe + (pco[u] & ((1u << kColBits) - 1u)));
 #pragma unroll
                 for (int u = 0; u < 8; ++u)
-                    if (j + u < j1) myrow[co[u] >> kColBits] += c[u];
+                    if (j + u < cj1) myrow[pco[u] >> kColBits] += pc[u];
+            }
+            if (has_next) {
+                half_range(n0, n1, cj0, cj1);
+                load8(cj0, cj1);
             }
             __syncthreads();
             // FP32 rows -> BF16 hi / lo in the swizzled layout; staging back to zero
