@@ -161,7 +161,7 @@ struct cgb_op {
     __nv_bfloat16 *tc_abimg;        // adjoint LUT images
     float *tc_terms;                // adjoint IC terms in entry order
     float *tc_ax;                   // A x rows for the gradient (FISTA), on demand
-    __nv_bfloat16 *tc_ec16, *tc_iso16;  // EC / ISO LUT rows as BF16, row stride tc_np
+    __nv_bfloat16 *tc_rows16;       // EC rows (nEC * ndirs) then ISO rows (nISO) as BF16, stride tc_np
     size_t bytes;
     int nsm;
     cgb::OpDev dev() const;

@@ -112,7 +112,9 @@ int adjoint_ff(cgb_op *op, const double *yin, int in_mode, const double *x, cons
                const double *ax_a, const double *ax_b, double ca, double cb, double *xout, double *partials,
                cudaStream_t st, int *grid) {
     AdjPair L{op, yin, in_mode, x, yobs, sqw, ax_a, ax_b, ca, cb, xout, partials, st, grid};
-    if (in_mode == 1) return dispatch_pair_shape(op->ff_shape[1] == 2 ? wide_pair_shape(op->nS) : pick_pair_shape(op->nS), L);
+    // the first A' call of any input mode chooses the shape, so a solve whose first A' is the
+    // fused gradient does not change shape (and summation order) at its second
+    if (in_mode == 1) return shaped(op, 1, kOccAdjFFFused, kOccAdjFFWideFused, st, L);
     return shaped(op, 1, kOccAdjFF, kOccAdjFFWide, st, L);
 }
 

@@ -45,7 +45,7 @@ struct TcAdjArgs {
     int64_t ec_base, iso_base;
     const uint32_t *ec_ptr, *ec_col, *iso_ptr, *iso_col;
     const uint16_t *ec_o;
-    const __nv_bfloat16 *lut_ec, *lut_iso;
+    const __nv_bfloat16 *rows16;  // EC rows (nEC * ndirs) then ISO rows (nISO), BF16, stride Np
     const uint32_t *ent_ptr, *ent_co;
     const __half *ent_l;
     float l_scale;
@@ -307,15 +307,15 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
                         const size_t ro = (size_t)A.ec_o[e];
                         for (int i = 0; i < A.nEC; ++i)
                             A.xout[cb + (int64_t)i * A.nE] = (double)z_dot_row(
-                                a_hi, a_lo, m, A.KBS, A.Np, A.lut_ec + ((size_t)i * A.ndirs + ro) * A.Np);
+                                a_hi, a_lo, m, A.KBS, A.Np, A.rows16 + ((size_t)i * A.ndirs + ro) * A.Np);
                     }
                 }
                 if (A.iso_ptr) {
                     for (uint32_t e = A.iso_ptr[v]; e < A.iso_ptr[v + 1]; ++e) {
                         const int64_t cb = A.iso_base + A.iso_col[e];
                         for (int i = 0; i < A.nISO; ++i)
-                            A.xout[cb + (int64_t)i * A.nISOv] =
-                                (double)z_dot_row(a_hi, a_lo, m, A.KBS, A.Np, A.lut_iso + (size_t)i * A.Np);
+                            A.xout[cb + (int64_t)i * A.nISOv] = (double)z_dot_row(
+                                a_hi, a_lo, m, A.KBS, A.Np, A.rows16 + ((size_t)A.nEC * A.ndirs + i) * A.Np);
                     }
                 }
             }
@@ -388,8 +388,7 @@ int adjoint_tc(cgb_op *op, int mode, const float *yin, const float *axa, const f
     A.ec_o = op->ec_o;
     A.iso_ptr = iso ? op->iso_ptr : nullptr;
     A.iso_col = op->iso_col;
-    A.lut_ec = op->tc_ec16;
-    A.lut_iso = op->tc_iso16;
+    A.rows16 = op->tc_rows16;
     A.ent_ptr = op->tc_ptr;
     A.ent_co = op->tc_co;
     A.ent_l = op->tc_l;

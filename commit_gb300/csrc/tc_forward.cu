@@ -20,7 +20,7 @@
 //    voxel's entries of one K-block are contiguous;
 //  - B images: per K-block the LUT rows transposed to [Np samples x 64 rows] BF16 in the
 //    K-major 128-byte-swizzled layout of tc_ptx.cuh, fetched whole by one bulk copy;
-//  - the EC and ISO LUT rows as BF16 with row stride Np (read by the epilogue).
+//  - the EC and ISO LUT rows as BF16 with row stride Np, EC first (read by the epilogue).
 //
 // Kernel: one CTA of 256 threads per SM (persistent over tiles), 2-stage pipeline over the
 // K-blocks of a tile: while the tensor cores multiply K-block b, the threads build the C
@@ -53,7 +53,7 @@ struct TcFwdArgs {
     int64_t ec_base, iso_base;
     const uint32_t *ec_ptr, *ec_col, *iso_ptr, *iso_col;
     const uint16_t *ec_o;
-    const __nv_bfloat16 *lut_ec, *lut_iso;
+    const __nv_bfloat16 *rows16;  // EC rows (nEC * ndirs) then ISO rows (nISO), BF16, stride Np
     const uint32_t *ent_ptr;
     const uint32_t *ent_co;
     const __half *ent_l;
@@ -71,9 +71,10 @@ __host__ __device__ constexpr size_t tc_smem_bytes(int Np) {
            2 * kTcTile * kStageStride * 4 /* FP32 staging, 2 parts */ + 128 /* barriers, TMEM slot, flags */;
 }
 
-// r[0..15] += xv * the 16 BF16 LUT values at row (16 consecutive samples, 32-byte aligned)
-__device__ __forceinline__ void fma_row16(float (&r)[16], float xv, const __nv_bfloat16 *row) {
-    const uint4 a = __ldg(reinterpret_cast<const uint4 *>(row)), b = __ldg(reinterpret_cast<const uint4 *>(row) + 1);
+constexpr int kTcItems = 8;  // EC / ISO items of a voxel held in registers (more take a loop)
+
+// r[0..15] += xv * the 16 BF16 values of w (two 16-byte words)
+__device__ __forceinline__ void fma16(float (&r)[16], float xv, const uint4 &a, const uint4 &b) {
     const uint32_t w[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
@@ -82,22 +83,30 @@ __device__ __forceinline__ void fma_row16(float (&r)[16], float xv, const __nv_b
     }
 }
 
-// the EC and ISO items of one voxel ([e0, e1) and [i0, i1) of the voxel-ordered arrays)
-// added to its samples [c0, c0 + 16)
-__device__ __forceinline__ void add_ec_iso(const TcFwdArgs &A, uint32_t e0, uint32_t e1, uint32_t i0, uint32_t i1,
-                                           int c0, float (&r)[16]) {
-    for (uint32_t e = e0; e < e1; ++e) {
-        const int64_t cb = A.ec_base + A.ec_col[e];
-        const size_t ro = (size_t)A.ec_o[e];
-        for (int i = 0; i < A.nEC; ++i)
-            fma_row16(r, A.xe[cb + (int64_t)i * A.nE], A.lut_ec + ((size_t)i * A.ndirs + ro) * A.Np + c0);
+// The EC and ISO items of one voxel, in order (EC entries [e0, e1) x responses, then ISO
+// entries [i0, i1) x responses): item k has BF16 row rows16[row(k)] and coefficient x(k).
+struct VoxItems {
+    uint32_t e0, e1, i0, i1;
+    int n;  // items
+    __device__ __forceinline__ int count(const TcFwdArgs &A) const {
+        return (int)(e1 - e0) * A.nEC + (int)(i1 - i0) * A.nISO;
     }
-    for (uint32_t e = i0; e < i1; ++e) {
-        const int64_t cb = A.iso_base + A.iso_col[e];
-        for (int i = 0; i < A.nISO; ++i)
-            fma_row16(r, A.xe[cb + (int64_t)i * A.nISOv], A.lut_iso + (size_t)i * A.Np + c0);
+    __device__ __forceinline__ void item(const TcFwdArgs &A, int k, uint32_t &row, float &xv) const {
+        const int nec = (int)(e1 - e0) * A.nEC;
+        if (k < nec) {
+            const uint32_t e = e0 + (uint32_t)(k / A.nEC);
+            const int i = k - (int)(e - e0) * A.nEC;
+            row = (uint32_t)i * (uint32_t)A.ndirs + A.ec_o[e];
+            xv = A.xe[A.ec_base + A.ec_col[e] + (int64_t)i * A.nE];
+        } else {
+            const int kk = k - nec;
+            const uint32_t e = i0 + (uint32_t)(kk / A.nISO);
+            const int i = kk - (int)(e - i0) * A.nISO;
+            row = (uint32_t)(A.nEC * A.ndirs + i);
+            xv = A.xe[A.iso_base + A.iso_col[e] + (int64_t)i * A.nISOv];
+        }
     }
-}
+};
 
 __global__ void __launch_bounds__(kTcThreads, 1) k_forward_tc(const TcFwdArgs A) {
     extern __shared__ uint8_t smem_raw[];
@@ -145,46 +154,81 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_forward_tc(const TcFwdArgs A)
     int bad = 0;
     bool stop = false;
 
-    // this thread's half of its voxel's entries of the next K-block to walk: [cj0, cj1), the
-    // first 8 of them (column | row, length) already in registers
-    uint32_t cj0 = 0, cj1 = 0;
-    uint32_t pco[8];
-    float pc[8];
+    // Entry pipeline of this thread (its half of its voxel's entries, per K-block in the
+    // CTA's order of (tile, K-block)): for the block being walked, [cj0, cj1) with the first 8
+    // entries (column | row, length) and their x values in registers; for the block after it,
+    // [nj0, nj1) with its first 8 entries loading; for the block after that, its offsets
+    // loading.  So the gathers of x and of the entries run one and two K-blocks ahead.
+    uint32_t cj0 = 0, cj1 = 0, nj0 = 0, nj1 = 0;
+    uint32_t cco[8], nco[8];
+    float cl[8], nl[8], cx[8];
+    const uint32_t kColMask = (1u << kColBits) - 1u;
     auto half_range = [&](uint32_t p0, uint32_t p1, uint32_t &j0, uint32_t &j1) {
         const uint32_t hcount = (p1 - p0 + 1) >> 1;
         j0 = part ? p0 + hcount : p0;
         j1 = part ? p1 : p0 + hcount;
     };
-    auto load8 = [&](uint32_t j0, uint32_t j1) {
+    // (tile, K-block) `ahead` blocks after (t, k) in this CTA's order; false past the end
+    auto step = [&](int t, int k, int ahead, int &t2, int &k2) {
+        k2 = k + ahead;
+        t2 = t;
+        while (k2 >= A.NKB) {
+            k2 -= A.NKB;
+            t2 += gridDim.x;
+        }
+        return t2 < A.ntiles;
+    };
+    auto ptr_of = [&](int t, int k) { return ((size_t)t * A.NKB + k) * kTcTile + vloc; };
+    if ((int)blockIdx.x < A.ntiles) {
+        int t1, k1;
+        size_t pb = ptr_of(blockIdx.x, 0);
+        half_range(A.ent_ptr[pb], A.ent_ptr[pb + 1], cj0, cj1);
+        if (step(blockIdx.x, 0, 1, t1, k1)) {
+            pb = ptr_of(t1, k1);
+            half_range(A.ent_ptr[pb], A.ent_ptr[pb + 1], nj0, nj1);
+        }
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
-            pco[u] = 0;
-            pc[u] = 0.f;
-            if (j0 + u < j1) {
-                pco[u] = __ldg(A.ent_co + j0 + u);
-                pc[u] = __half2float(A.ent_l[j0 + u]);
+            cco[u] = 0;
+            cl[u] = 0.f;
+            nco[u] = 0;
+            nl[u] = 0.f;
+            if (cj0 + u < cj1) {
+                cco[u] = __ldg(A.ent_co + cj0 + u);
+                cl[u] = __half2float(A.ent_l[cj0 + u]);
+            }
+            if (nj0 + u < nj1) {
+                nco[u] = __ldg(A.ent_co + nj0 + u);
+                nl[u] = __half2float(A.ent_l[nj0 + u]);
             }
         }
-    };
-    if ((int)blockIdx.x < A.ntiles) {
-        const size_t pb = (size_t)blockIdx.x * A.NKB * kTcTile + vloc;
-        half_range(A.ent_ptr[pb], A.ent_ptr[pb + 1], cj0, cj1);
-        load8(cj0, cj1);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) cx[u] = cj0 + u < cj1 ? __ldg(A.xe + (cco[u] & kColMask)) : 0.f;
     }
 
     for (int tile = blockIdx.x; tile < A.ntiles && !stop; tile += gridDim.x) {
-        // the epilogue's voxel: its EC / ISO item ranges, loaded ahead of the K-blocks
+        // the epilogue's voxel: its EC / ISO items, the first kTcItems (row, x) loaded ahead
+        // of the K-blocks
         const int ve = tile * kTcTile + (warp & 3) * 32 + lane;
-        uint32_t e0 = 0, e1 = 0, i0 = 0, i1 = 0;
+        VoxItems V{0, 0, 0, 0, 0};
         if (ve < A.nV) {
             if (A.ec_ptr) {
-                e0 = A.ec_ptr[ve];
-                e1 = A.ec_ptr[ve + 1];
+                V.e0 = A.ec_ptr[ve];
+                V.e1 = A.ec_ptr[ve + 1];
             }
             if (A.iso_ptr) {
-                i0 = A.iso_ptr[ve];
-                i1 = A.iso_ptr[ve + 1];
+                V.i0 = A.iso_ptr[ve];
+                V.i1 = A.iso_ptr[ve + 1];
             }
+        }
+        V.n = V.count(A);
+        uint32_t irow[kTcItems];
+        float ix[kTcItems];
+#pragma unroll
+        for (int k = 0; k < kTcItems; ++k) {
+            irow[k] = 0;
+            ix[k] = 0.f;
+            if (k < V.n) V.item(A, k, irow[k], ix[k]);
         }
         for (int kb = 0; kb < A.NKB; ++kb, ++it) {
             const uint32_t s = it & 1u;
@@ -198,44 +242,55 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_forward_tc(const TcFwdArgs A)
                 tc::bulk_g2s(b_img + s * bbytes, A.bimg + (size_t)kb * A.Np * kTcKB, bbytes, &bfull[s]);
                 last_b[s] = it;
             }
-            // the K-block after this one (this tile's next, or the next tile's first): its
-            // entry offsets load during this block's walk, its first entries after it
-            int nt = tile, nk = kb + 1;
-            if (nk == A.NKB) {
-                nt += gridDim.x;
-                nk = 0;
+            // offsets of the block two ahead, loading during this block's walk
+            int t2, k2;
+            const bool has2 = step(tile, kb, 2, t2, k2);
+            uint32_t q0 = 0, q1 = 0;
+            if (has2) {
+                const size_t pb = ptr_of(t2, k2);
+                q0 = A.ent_ptr[pb];
+                q1 = A.ent_ptr[pb + 1];
             }
-            const bool has_next = nt < A.ntiles;
-            uint32_t n0 = 0, n1 = 0;
-            if (has_next) {
-                const size_t pb = ((size_t)nt * A.NKB + nk) * kTcTile + vloc;
-                n0 = A.ent_ptr[pb];
-                n1 = A.ent_ptr[pb + 1];
-            }
-            // C rows of this K-block: two threads per voxel, each over half of its entries;
-            // the first 8 were loaded during the previous K-block
+            // C rows of this K-block: two threads per voxel, each over half of its entries
             for (uint32_t j = cj0; j < cj1; j += 8) {
                 if (j != cj0) {
 #pragma unroll
                     for (int u = 0; u < 8; ++u) {
-                        pco[u] = 0;
-                        pc[u] = 0.f;
+                        cco[u] = 0;
+                        cl[u] = 0.f;
                         if (j + u < cj1) {
-                            pco[u] = __ldg(A.ent_co + j + u);
-                            pc[u] = __half2float(A.ent_l[j + u]);
+                            cco[u] = __ldg(A.ent_co + j + u);
+                            cl[u] = __half2float(A.ent_l[j + u]);
                         }
                     }
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) cx[u] = j + u < cj1 ? __ldg(A.xe + (cco[u] & kColMask)) : 0.f;
                 }
 #pragma unroll
                 for (int u = 0; u < 8; ++u)
-                    if (j + u < cj1) pc[u] *= __ldg(A.xe + (pco[u] & ((1u << kColBits) - 1u)));
-#pragma unroll
-                for (int u = 0; u < 8; ++u)
-                    if (j + u < cj1) myrow[pco[u] >> kColBits] += pc[u];
+                    if (j + u < cj1) myrow[cco[u] >> kColBits] += cl[u] * cx[u];
             }
-            if (has_next) {
-                half_range(n0, n1, cj0, cj1);
-                load8(cj0, cj1);
+            // shift the pipeline: the next block's entries (loaded a block ago) become
+            // current and their x values start loading; the block two ahead starts loading
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                cco[u] = nco[u];
+                cl[u] = nl[u];
+            }
+            cj0 = nj0;
+            cj1 = nj1;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) cx[u] = cj0 + u < cj1 ? __ldg(A.xe + (cco[u] & kColMask)) : 0.f;
+            nj0 = nj1 = 0;
+            if (has2) half_range(q0, q1, nj0, nj1);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                nco[u] = 0;
+                nl[u] = 0.f;
+                if (nj0 + u < nj1) {
+                    nco[u] = __ldg(A.ent_co + nj0 + u);
+                    nl[u] = __half2float(A.ent_l[nj0 + u]);
+                }
             }
             __syncthreads();
             // FP32 rows -> BF16 hi / lo in the swizzled layout; staging back to zero
@@ -312,7 +367,28 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_forward_tc(const TcFwdArgs A)
         for (int c0 = colh * half; c0 < (colh + 1) * half; c0 += 16) {
             float r[16];
             tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, r);
-            add_ec_iso(A, e0, e1, i0, i1, c0, r);
+            // the voxel's EC / ISO items: all row loads of the chunk issued together
+            {
+                uint4 wa[kTcItems], wb[kTcItems];
+#pragma unroll
+                for (int k = 0; k < kTcItems; ++k) {
+                    if (k < V.n) {
+                        const uint4 *rp = reinterpret_cast<const uint4 *>(A.rows16 + (size_t)irow[k] * A.Np + c0);
+                        wa[k] = __ldg(rp);
+                        wb[k] = __ldg(rp + 1);
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < kTcItems; ++k)
+                    if (k < V.n) fma16(r, ix[k], wa[k], wb[k]);
+                for (int k = kTcItems; k < V.n; ++k) {
+                    uint32_t row;
+                    float xv;
+                    V.item(A, k, row, xv);
+                    const uint4 *rp = reinterpret_cast<const uint4 *>(A.rows16 + (size_t)row * A.Np + c0);
+                    fma16(r, xv, __ldg(rp), __ldg(rp + 1));
+                }
+            }
             if (v < A.nV && vec4 && c0 + 16 <= A.nS && !A.partials) {
                 const size_t idx = (size_t)v * A.nS + c0;
 #pragma unroll
@@ -545,9 +621,8 @@ int ensure_tc(cgb_op *op) {
        "cudaMalloc");
     cu(cudaMalloc((void **)&op->tc_xe, (size_t)(op->ncols > 0 ? op->ncols : 1) * sizeof(float)), "cudaMalloc");
     cu(cudaMalloc((void **)&op->tc_err, sizeof(int)), "cudaMalloc");
-    cu(cudaMalloc((void **)&op->tc_ec16, (size_t)(nec_rows > 0 ? nec_rows : 1) * Np * sizeof(__nv_bfloat16)),
-       "cudaMalloc");
-    cu(cudaMalloc((void **)&op->tc_iso16, (size_t)(niso_rows > 0 ? niso_rows : 1) * Np * sizeof(__nv_bfloat16)),
+    cu(cudaMalloc((void **)&op->tc_rows16, (size_t)(nec_rows + niso_rows > 0 ? nec_rows + niso_rows : 1) * Np *
+                                               sizeof(__nv_bfloat16)),
        "cudaMalloc");
     cu(cudaMalloc((void **)&key, nent * sizeof(uint32_t)), "cudaMalloc");
     cu(cudaMalloc((void **)&key2, nent * sizeof(uint32_t)), "cudaMalloc");
@@ -573,13 +648,14 @@ int ensure_tc(cgb_op *op) {
         const int64_t nimg = (int64_t)NKB * Np * kTcKB;
         k_tc_bimg<<<grid_of(nimg, op->nsm), 256>>>(P, Np, NKB, nkbd, op->tc_bimg);
         cu(cudaGetLastError(), "k_tc_bimg");
+        // EC rows (response, orientation) first, then the ISO rows
         if (nec_rows > 0) {
-            k_tc_rows16<<<grid_of(nec_rows * Np, op->nsm), 256>>>(op->lutEC, (int)nec_rows, op->nS, Np, op->tc_ec16);
+            k_tc_rows16<<<grid_of(nec_rows * Np, op->nsm), 256>>>(op->lutEC, (int)nec_rows, op->nS, Np, op->tc_rows16);
             cu(cudaGetLastError(), "k_tc_rows16");
         }
         if (niso_rows > 0) {
             k_tc_rows16<<<grid_of(niso_rows * Np, op->nsm), 256>>>(op->lutISO, (int)niso_rows, op->nS, Np,
-                                                                   op->tc_iso16);
+                                                                   op->tc_rows16 + (size_t)nec_rows * Np);
             cu(cudaGetLastError(), "k_tc_rows16");
         }
         cu(cudaFuncSetAttribute(k_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes(Np)),
@@ -711,8 +787,7 @@ int forward_tc(cgb_op *op, const double *x, float *y, float *ax, const float *yo
     A.ec_o = op->ec_o;
     A.iso_ptr = iso ? op->iso_ptr : nullptr;
     A.iso_col = op->iso_col;
-    A.lut_ec = op->tc_ec16;
-    A.lut_iso = op->tc_iso16;
+    A.rows16 = op->tc_rows16;
     A.ent_ptr = op->tc_ptr;
     A.ent_co = op->tc_co;
     A.ent_l = op->tc_l;

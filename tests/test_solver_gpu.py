@@ -174,12 +174,14 @@ def test_backtracking_cap_ends_the_solve():
 
 @pytest.mark.parametrize('name', ['szb', 'multi_rf'])
 def test_solve_far_past_convergence(name):
-    """Tolerances off, 4000 nnls iterations: near the minimum the sufficient-decrease test is
-    decided at the rounding level.  With momentum reuse qfval comes from the stored rows and
-    rounds differently from the evaluation of x; the solver then evaluates f(x_hat) directly
-    (an anchor) instead of shrinking the step without end.  Host loop (with and without
-    restart) and graph finish every iteration, the graph with the host loop's iterates bit
-    for bit, and all reach the no-reuse solution."""
+    """Tolerances off, up to 4000 nnls iterations: near the minimum the sufficient-decrease
+    test is decided at the rounding level.  With momentum reuse qfval comes from the stored
+    rows and rounds differently from the evaluation of x; on a failed test the solver then
+    evaluates f(x_hat) directly (an anchor) instead of shrinking the step without end.  The
+    host loop (with and without restart) and the graph end without error, on the iteration
+    cap or on the reference's absolute tests (|f_k - f_k-1| or |x_k - x_k-1| below eps),
+    the graph with the host loop's iterates, backtracks and anchors bit for bit, and all
+    reach the no-reuse solution."""
     from commit_gb300 import solvers
     from commit_gb300.operator import LinearOperator
     c = G.load_case(name)
@@ -192,10 +194,12 @@ def test_solve_far_past_convergence(name):
     xg, dg = solvers.solve(c['y_obs'], A, A.T, regularisation=reg(), graph=True, **kw)
     xr, dr = solvers.solve(c['y_obs'], A, A.T, regularisation=reg(), restart=True, **kw)
     assert d0['anchors'] == 0
-    for d in (dh, dg, dr):
-        assert d['iterations'] == 4000
-    assert dh['anchors'] > 0 and dg['anchors'] == dh['anchors']
+    ends = ('Maximum number of iterations', 'Absolute tolerance on the objective',
+            'Absolute tolerance on the unknowns')
+    for d in (d0, dh, dg, dr):
+        assert d['stopping_criterion'] in ends
+    for k in ('iterations', 'backtracks', 'anchors', 'cost_function'):
+        assert dg[k] == dh[k], k
     assert np.array_equal(xg, xh)
     for x in (xh, xr):
         assert G.rel(x, x0) <= 1e-8
-    assert dh['cost_function'] <= d0['cost_function'] * (1 + 1e-12)
