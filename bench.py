@@ -55,11 +55,11 @@ def parse():
     p.add_argument('--slabs', type=int, default=-1,
                    help='adjoint slab count (0 automatic, 1 off; default: the handle\'s own choice)')
     p.add_argument('--fista', action='store_true', help='FISTA time-to-tolerance, plain vs mixed + refinement')
-    p.add_argument('--fista-iters', type=int, default=8000, help='iterations of the plain arm')
+    p.add_argument('--fista-iters', type=int, default=8000, help='iterations of each plain arm')
     p.add_argument('--mixed-iters', type=int, default=4000, help='reduced-precision iterations of a mixed arm')
-    p.add_argument('--refine-iters', type=int, default=4000, help='FP64 refinement iterations of a mixed arm')
+    p.add_argument('--refine-iters', type=int, default=6000, help='FP64 refinement iterations of a mixed arm')
     p.add_argument('--xstar-iters', type=int, default=20000, help='cap on the iterations computing x*')
-    p.add_argument('--xstar-chunk', type=int, default=1000, help='iterations per warm-started chunk of x*')
+    p.add_argument('--xstar-chunk', type=int, default=1000, help='iterations run from x* to measure its drift')
     p.add_argument('--demo', action='store_true',
                    help='demo-scale case (5k streamlines, nS=66): A*x, A\'y and 200 FISTA nnls iterations, '
                         'host-driven loop vs graph-captured loop, next to the reference CPU operator')
@@ -76,7 +76,7 @@ def parse():
                         'iterations): batched BF16 solves polished by a per-problem FP64 solve, against '
                         'sequential plain solves to the same tolerance')
     p.add_argument('--batch-max', type=int, default=1000, help='iteration cap per solve with --batch-tol')
-    p.add_argument('--batch-streams', type=int, default=8, help='tractograms solved concurrently (streams)')
+    p.add_argument('--batch-streams', type=int, default=4, help='tractograms solved concurrently (streams)')
     p.add_argument('--sample-frac', type=float, default=0.25, help='CPU sample: fraction of the segments')
     p.add_argument('--no-e2e', action='store_true')
     p.add_argument('--no-cpu', action='store_true')
@@ -506,19 +506,17 @@ def run_ours(args):
 def run_fista(args, spec, D, K, dev):
     """FISTA time-to-tolerance at the 1M-streamline workload (nnls on all compartments).
 
-    x*: the FP64-accurate (float-float) solver with function-value momentum restart, run in
-    warm-started chunks until a chunk ends on tol_fun 1e-12 or --xstar-iters iterations are
-    spent; the change over its last chunk is reported as x*'s own accuracy.  The chunk ends
-    are kept, so the restarted FP64 solver's own distance to x* after each chunk is an arm
-    ('plain_restart', momentum reset at every chunk start).  Other arms, each traced per
-    accepted iteration (seconds since its start, |x_k - x*| / |x*|, cost): the plain
-    FP64-accurate solver as the reference runs it (no restart), and reduced precision + FP64
-    refinement with restart: BF16 LUT on the tensor cores and FP32 LUT on the CUDA cores.
-    Times to 1e-2 / 1e-3 / 1e-4 in x and to a relative cost gap of 1e-6 / 1e-8 / 1e-10, and
-    the errors of the reduced-precision phase's y = A x*, x and cost against FP64.  Prints
-    one JSON line."""
+    x*: the FP64-accurate (float-float) solver with function-value momentum restart, run to
+    tol_fun 1e-12 or --xstar-iters iterations; --xstar-chunk more iterations from it measure
+    how far x* itself still moves (the better of the two points is kept).  Arms, each traced
+    per accepted iteration (seconds since its start, |x_k - x*| / |x*|, cost): the plain
+    FP64-accurate solver as the reference runs it (no restart), the same with restart, and
+    reduced precision + FP64 refinement with restart: BF16 LUT on the tensor cores and FP32
+    LUT on the CUDA cores.  Times to 1e-2 / 1e-3 / 1e-4 in x and to a relative cost gap of
+    1e-6 / 1e-8 / 1e-10, and the errors of the reduced-precision phase's y = A x*, x and
+    cost against FP64.  Prints one JSON line."""
     import torch
-    from commit_gb300 import _lib, solvers, synth
+    from commit_gb300 import solvers, synth
     from commit_gb300.operator import LinearOperator
     A = LinearOperator(D, K, None, arith='ff', device=dev.index)
     x_true = synth.make_x(A.nCOLS, spec.seed + 1)
@@ -530,40 +528,38 @@ def run_fista(args, spec, D, K, dev):
           'dictIC_params': None, 'dictEC_params': None, 'dictISO_params': None}
     reg = lambda: solvers.init_regularisation(dict(rp))  # noqa: E731
     rel = lambda a, b: float(torch.linalg.norm(a - b) / torch.linalg.norm(b))  # noqa: E731
-    # ---- x*: restarted FP64-accurate FISTA in warm-started chunks, chunk ends kept
-    x = torch.zeros(A.nCOLS, dtype=torch.float64, device=dev)
-    chunks, snaps, done, change, elapsed = [], [], 0, None, 0.0
-    while done < args.xstar_iters:
-        t0 = time.perf_counter()
-        try:
-            xn, d = solvers.solve(y, A, A.T, tol_fun=1e-12, tol_x=0.0, max_iter=min(args.xstar_chunk,
-                                  args.xstar_iters - done), verbose=0, x0=x, regularisation=reg(), restart=True)
-        except _lib.CgbError as e:  # a stall of the line search: keep the last complete chunk
-            chunks.append({'iterations': done, 'stalled': str(e)})
-            break
-        torch.cuda.synchronize()
-        elapsed += time.perf_counter() - t0
-        change = rel(xn, x) if done else 1.0
-        x = xn
-        done += d['iterations']
-        snaps.append((elapsed, done, x.clone(), d['cost_function']))
-        chunks.append({'iterations': done, 'seconds': elapsed, 'change': change, 'cost': d['cost_function'],
-                       'criterion': d['stopping_criterion'], 'anchors': d['anchors']})
-        print(json.dumps({'xstar_chunk': chunks[-1]}), file=sys.stderr, flush=True)
-        if d['stopping_criterion'] != 'Maximum number of iterations':
-            break
-    x_star = x
-    cost_star = snaps[-1][3]
+    # ---- x*: one restarted FP64-accurate solve to tol_fun 1e-12 (or --xstar-iters), then
+    # --xstar-chunk more iterations from it to measure how far x* itself still moves
+    x0 = torch.zeros(A.nCOLS, dtype=torch.float64, device=dev)
+    t0 = time.perf_counter()
+    x_star, d = solvers.solve(y, A, A.T, tol_fun=1e-12, tol_x=0.0, max_iter=args.xstar_iters, verbose=0, x0=x0,
+                              regularisation=reg(), restart=True)
+    torch.cuda.synchronize()
+    xs_info = {'method': 'float-float FISTA with function-value restart, tol_fun 1e-12',
+               'iterations': d['iterations'], 'seconds': time.perf_counter() - t0, 'criterion': d['stopping_criterion'],
+               'cost': d['cost_function'], 'backtracks': d['backtracks'], 'anchors': d['anchors']}
+    cost_star = d['cost_function']
+    print(json.dumps({'x_star': xs_info}), file=sys.stderr, flush=True)
+    xn, d = solvers.solve(y, A, A.T, tol_fun=0.0, tol_x=0.0, max_iter=args.xstar_chunk, verbose=0, x0=x_star,
+                          regularisation=reg(), restart=True)
+    xs_info['drift'] = {'iterations': d['iterations'], 'rel_change': rel(xn, x_star),
+                        'cost_change': (d['cost_function'] - cost_star) / cost_star}
+    if d['cost_function'] < cost_star:  # the later point is the better minimiser
+        x_star, cost_star = xn, d['cost_function']
+    del xn
     x_tols, c_tols = (1e-2, 1e-3, 1e-4), (1e-6, 1e-8, 1e-10)
 
     def first_below(t, v, tol):
         idx = np.flatnonzero(v <= tol)
         return {'seconds': float(t[idx[0]]), 'iteration': int(idx[0]) + 1} if idx.size else None
 
-    def summary(t, xd, cost, extra=None):
+    def summary(det, extra=None):
+        tr = det['trace']
+        t, xd, cost = tr[:, 0], tr[:, 1], tr[:, 2]
         gap = (cost - cost_star) / cost_star
         out = {'iterations': int(len(t)), 'seconds': float(t[-1]), 'final_rel': float(xd[-1]),
-               'final_cost_gap': float(gap[-1]),
+               'final_cost_gap': float(gap[-1]), 'backtracks': det.get('backtracks'), 'anchors': det.get('anchors'),
+               'stopping_criterion': det.get('stopping_criterion'),
                'time_to_x': {f'{tol:g}': first_below(t, xd, tol) for tol in x_tols},
                'time_to_cost_gap': {f'{tol:g}': first_below(t, gap, tol) for tol in c_tols}}
         out['ms_per_iteration'] = 1000.0 * out['seconds'] / len(t)
@@ -572,18 +568,12 @@ def run_fista(args, spec, D, K, dev):
         return out
 
     arms = {}
-    # the restarted FP64 solver at its chunk ends (all but the last, which is x* itself)
-    st = np.array([s[0] for s in snaps[:-1]] or [np.nan])
-    sx = np.array([rel(s[2], x_star) for s in snaps[:-1]] or [np.nan])
-    sc = np.array([s[3] for s in snaps[:-1]] or [np.nan])
-    arms['plain_restart'] = summary(st, sx, sc, {'granularity': f'chunk ends, every {args.xstar_chunk} iterations'})
-    arms['plain_restart']['iterations'] = int(snaps[-2][1]) if len(snaps) > 1 else 0
-    arms['plain_restart']['ms_per_iteration'] = 1000.0 * elapsed / max(done, 1)
-    del snaps
     n = args.fista_iters
+    _, d = solvers.solve(y, A, A.T, tol_fun=0.0, tol_x=0.0, max_iter=n, verbose=0, regularisation=reg(), x_ref=x_star,
+                         restart=True)
+    arms['plain_restart'] = summary(d)
     _, d = solvers.solve(y, A, A.T, tol_fun=0.0, tol_x=0.0, max_iter=n, verbose=0, regularisation=reg(), x_ref=x_star)
-    tr = d['trace']
-    arms['plain'] = summary(tr[:, 0], tr[:, 1], tr[:, 2], {'anchors': d['anchors']})
+    arms['plain'] = summary(d)
     n1, n2 = args.mixed_iters, args.refine_iters
     errors = {}
     yf = A.dot(x_star)
@@ -593,12 +583,13 @@ def run_fista(args, spec, D, K, dev):
         A.tensor_cores(tcm)
         xm, dm = solvers.solve_mixed(y, A, tol_fun=0.0, tol_x=0.0, max_iter=n1, verbose=0, regularisation=reg(),
                                      arith=ar, refine_max_iter=n2, x_ref=x_star, restart=True)
-        tr, mix = dm['trace'], dm['mixed']['trace']
+        mix = dm['mixed']['trace']
         errors[name] = {'y': rel(A.dot(x_star.float(), arith=ar).double(), yf),
                         'x_after_reduced_phase': float(mix[-1, 1]),
                         'cost_after_reduced_phase': float((mix[-1, 2] - cost_star) / cost_star)}
-        arms[name + '_refined'] = summary(tr[:, 0], tr[:, 1], tr[:, 2], {
-            'reduced_iterations': n1, 'refine_iterations': n2,
+        arms[name + '_refined'] = summary(dm, {
+            'reduced_iterations': int(len(mix)), 'refine_iterations': int(dm['refine']['iterations']),
+            'refine_stopping_criterion': dm['refine']['stopping_criterion'],
             'ms_per_reduced_iteration': 1000.0 * float(mix[-1, 0]) / len(mix)})
     A.tensor_cores(1)
     for v in arms.values():
@@ -611,9 +602,7 @@ def run_fista(args, spec, D, K, dev):
     out = {'metric': 'FISTA time-to-tolerance |x_k - x*|/|x*| (1M-streamline workload, nnls)',
            'unit': 's', 'higher_is_better': False, 'data': 'synthetic',
            'config': workload_config(spec, D, K, args) | {'regulariser': 'nnls (all compartments)'},
-           'x_star': {'method': 'float-float FISTA with function-value restart, warm-started chunks, tol_fun 1e-12',
-                      'iterations': done, 'seconds': elapsed, 'last_chunk_change': change, 'cost': cost_star,
-                      'chunks': chunks},
+           'x_star': xs_info,
            'arms': arms, 'reduced_precision_errors_vs_fp64': errors}
     if not args.no_cpu:
         out['cpu_baseline'] = cpu_reference_fista(D, K, args.sample_frac, 5)

@@ -425,7 +425,7 @@ def solve_batch(y, A, regularisations, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, 
     return out
 
 
-def solve_batches(jobs, n_streams: int = 8, **kw):
+def solve_batches(jobs, n_streams: int = 4, **kw):
     """Regularisation paths on several operators (e.g. tractograms of uneven size) at once.
 
     jobs: list of (y, A, regularisations).  Each job runs ``solve_batch`` on a CUDA stream
