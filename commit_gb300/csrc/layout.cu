@@ -509,7 +509,7 @@ int cgb_op_create(int device, int nS, int ndirs, int nF, int64_t n, int nE, int 
     DeviceGuard g(device);
     cgb_op *op = new cgb_op();
     memset((void *)op, 0, sizeof(cgb_op));
-    op->tc_mode = 1;  // tensor-core forward off until asked for (cgb_op_tensor_cores)
+    op->tc_mode = 0;  // tensor cores when dense enough (tc_forward_enabled)
     int rc = create_impl(device, nS, ndirs, nF, n, nE, nV, nISOv, ICf, ICeval, ICv, ICo, ICl, ECv, ECo, ISOv, lutIC,
                          lutEC, lutISO, nIC, nEC, nISO, nolut, arith, op);
     if (rc != CGB_OK) {

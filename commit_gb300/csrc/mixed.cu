@@ -331,7 +331,7 @@ int launch_adjoint_mix(cgb_op *op, const float *yin, double *xout, cudaStream_t 
     }
     if (arith == CGB_ARITH_BF16 && tc_forward_enabled(op))
         return adjoint_tc(op, 0, yin, nullptr, nullptr, 0.f, 0.f, nullptr, nullptr, xout, nullptr, st, nullptr);
-return adj_mix_slabs(op, arith, yin, 0, nullptr, nullptr, nullptr, nullptr, nullptr, 0.f, 0.f, xout, nullptr, st,
+    return adj_mix_slabs(op, arith, yin, 0, nullptr, nullptr, nullptr, nullptr, nullptr, 0.f, 0.f, xout, nullptr, st,
                          nullptr);
 }
 

@@ -582,7 +582,14 @@ bool tc_supported(const cgb_op *op) {
            nent < ((int64_t)1 << 32);
 }
 
-bool tc_forward_enabled(const cgb_op *op) { return op->tc_mode != 1 && tc_supported(op); }
+// IC segments per voxel from which mode 0 takes the tensor cores: the dense product costs
+// per (tile, K-block) whatever the segments, so sparse operators stay on the CUDA cores
+constexpr int64_t kTcMinSegmentsPerVoxel = 64;
+
+bool tc_forward_enabled(const cgb_op *op) {
+    if (op->tc_mode == 1 || !tc_supported(op)) return false;
+    return op->tc_mode == 2 || op->n * op->nIC >= kTcMinSegmentsPerVoxel * (int64_t)op->nV;
+}
 
 // IC entries, their per-(tile, K-block, voxel) offsets, the B images and the BF16 EC / ISO
 // rows; needs the FP16 lengths of ensure_reduced

@@ -211,15 +211,19 @@ int cgb_op_adjoint_noalloc(int nS, int ndirs, int nF, int64_t n, int nE, int nV,
                            void *stream);
 
 /*
- * Reduced-precision A*x with a BF16 LUT on the tensor cores (tcgen05): per tile of 128
- * voxels the voxel-by-LUT-row coefficient matrix is built in shared memory, split into
- * BF16 high and low parts and multiplied with the BF16 LUT into an FP32 accumulator in
- * tensor memory.  mode 0 uses it whenever the operator's shape allows (nS <= 320, fewer
- * than 2^26 columns), 1 keeps the CUDA-core kernels, 2 requires it (CGB_ERR_UNSUPPORTED
- * when the shape does not allow it); a negative mode only reads.  *out (may be NULL)
- * receives 1 when the tensor-core forward is in use.  The first use on a handle builds its
- * tile-ordered entry stream and LUT images (about 6 bytes per item).  No counterpart in
- * the reference (setup_operator.py:50-218 is its CPU A).
+ * Reduced-precision A*x and A'*y with a BF16 LUT on the tensor cores (tcgen05): per tile
+ * of 128 voxels the IC part is a dense product of the voxel-by-LUT-row coefficients (A) or
+ * of the input rows (A') with the BF16 LUT, FP32 accumulation in tensor memory; the EC and
+ * ISO items run on the CUDA cores in the same kernels.  mode 0 (the default) uses it when
+ * the shape allows it (an IC compartment, nS <= 320, fewer than 2^26 columns) and the IC
+ * segments are dense enough for the dense product to pay, at least 64 per voxel on
+ * average (measured on GB300: at 212 per voxel it is 1.65x faster than the CUDA-core
+ * kernels, at 21 per voxel slower); 1 keeps the CUDA-core kernels; 2 requires it
+ * (CGB_ERR_UNSUPPORTED when the shape does not allow it); a negative mode only reads.
+ * *out (may be NULL) receives 1 when the tensor-core kernels are in use.  The first use on
+ * a handle builds its tile-ordered entry stream and LUT images (about 6 bytes per
+ * segment).  No counterpart in the reference (setup_operator.py:50-218 and 591-710 are its
+ * CPU A and A').
  */
 int cgb_op_tensor_cores(cgb_op *op, int mode, int *out);
 
