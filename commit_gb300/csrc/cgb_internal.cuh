@@ -140,7 +140,8 @@ struct cgb_op {
     int *slab_v;                    // host [nslab+1] voxel boundaries
     uint32_t *fib_slab;             // device [(nslab+1) * nF]: where slab s starts in the position list of
                                     // the fibre at pass position fq (fib_order[fq])
-    double *fib_acc;                // device [nF * nIC]: running fibre sums between slabs, pass order
+    double *fib_acc;                // device [fib_acc_slots * nF * nIC]: running fibre sums between slabs,
+    int fib_acc_slots;              // pass order, one accumulator per vector of a pass
     cudaStream_t slab_st[3];        // slab schedule streams (created on first use)
     cudaEvent_t slab_ev[68];
     cudaEvent_t pipe_ev[8];
@@ -214,8 +215,11 @@ int forward_tc(cgb_op *op, const double *x, float *y, float *ax, const float *yo
 int fibre_sum(cgb_op *op, double *xout, cudaStream_t st);
 // fibre pass of one adjoint slab (sums continue across slabs in fibre order; the last slab
 // applies eval), FP64 / FP32 terms
+// fibre pass of slab s; the running sums between slabs live in accumulator `slot` of
+// op->fib_acc (one per vector of a multi-vector pass: ensure_fib_acc)
 int fibre_sum_slab(cgb_op *op, double *xout, int s, cudaStream_t st);
-int fibre_sum32_slab(cgb_op *op, const float *scr, double *xout, int s, cudaStream_t st);
+int fibre_sum32_slab(cgb_op *op, const float *scr, double *xout, int s, cudaStream_t st, int slot = 0);
+int ensure_fib_acc(cgb_op *op, int slots);
 // blocks of partial sums an adjoint may write (one grid per slab)
 int partial_blocks(const cgb_op *op);
 

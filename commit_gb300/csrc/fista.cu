@@ -1382,7 +1382,9 @@ struct BatchSolver {
                     if (r < take) M.off[r] = 16 * p + 12;
                 }
                 if (op->nslab > 1) {
-                    // slab by slab, the fibre passes right after each voxel pass (terms in L2)
+                    // slab by slab, the fibre passes right after each voxel pass (terms in L2),
+                    // each vector's running fibre sums in its own accumulator
+                    CGB_TRY(ensure_fib_acc(op, take));
                     int g0 = 0;
                     CGB_TRY(slab_schedule(
                         op, st,
@@ -1396,7 +1398,7 @@ struct BatchSolver {
                         },
                         [&](int sl, cudaStream_t q) {
                             for (int r = 0; r < take; ++r)
-                                CGB_TRY(fibre_sum32_slab(op, scr[r], S[pp[r]].ws.grad, sl, q));
+                                CGB_TRY(fibre_sum32_slab(op, scr[r], S[pp[r]].ws.grad, sl, q, r));
                             return CGB_OK;
                         }));
                     g = g0 * op->nslab;

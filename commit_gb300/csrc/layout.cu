@@ -233,6 +233,7 @@ static int build_slabs(cgb_op *op, int want = 0) {
         cudaFree(op->fib_acc);
         op->fib_acc = nullptr;
     }
+    op->fib_acc_slots = 0;
     const double bytes = (double)op->n * (op->nIC > 0 ? op->nIC : 1) * sizeof(double);
     int S = want > 0 ? want : (int)(bytes / kSlabTermBytes + 0.5);
     if (S > 64) S = 64;
@@ -253,6 +254,7 @@ static int build_slabs(cgb_op *op, int want = 0) {
     cudaError_t e = cudaMalloc((void **)&op->fib_slab, (size_t)(S + 1) * op->nF * sizeof(uint32_t));
     if (e == cudaSuccess)
         e = cudaMalloc((void **)&op->fib_acc, (size_t)op->nF * (op->nIC > 0 ? op->nIC : 1) * sizeof(double));
+    op->fib_acc_slots = e == cudaSuccess ? 1 : 0;
     if (e != cudaSuccess) {
         cudaFree(dpos);
         cudaFree(op->fib_slab);
@@ -270,6 +272,19 @@ static int build_slabs(cgb_op *op, int want = 0) {
     op->slab_v = new int[S + 1];
     for (int s = 0; s <= S; ++s) op->slab_v[s] = sv[s];
     op->nslab = S;
+    return CGB_OK;
+}
+
+// room for `slots` running-sum accumulators of the slab fibre passes (one per vector of a
+// multi-vector pass); grows outside stream capture only
+int cgb::ensure_fib_acc(cgb_op *op, int slots) {
+    if (op->nslab <= 1 || slots <= op->fib_acc_slots) return CGB_OK;
+    CGB_CUDA(cudaDeviceSynchronize());
+    if (op->fib_acc) cudaFree(op->fib_acc);
+    op->fib_acc = nullptr;
+    op->fib_acc_slots = 0;
+    CGB_CUDA(cudaMalloc((void **)&op->fib_acc, (size_t)slots * op->nF * (op->nIC > 0 ? op->nIC : 1) * sizeof(double)));
+    op->fib_acc_slots = slots;
     return CGB_OK;
 }
 
@@ -602,6 +617,7 @@ int cgb_op_set_slabs(cgb_op *op, int nslab, int *out) {
         if (op->fib_acc) cudaFree(op->fib_acc);
         op->fib_slab = nullptr;
         op->fib_acc = nullptr;
+        op->fib_acc_slots = 0;
         op->nslab = 1;
     }
     if (op->partials) cudaFree(op->partials);

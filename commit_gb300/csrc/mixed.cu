@@ -125,12 +125,14 @@ __global__ void k_fibre_sum32_slab(const OpDev P, const float *__restrict__ scr,
     }
 }
 
-int fibre_sum32_slab(cgb_op *op, const float *scr, double *xout, int s, cudaStream_t st) {
+int fibre_sum32_slab(cgb_op *op, const float *scr, double *xout, int s, cudaStream_t st, int slot) {
     if (op->nIC > 0 && op->nF > 0) {
         const int64_t total = (int64_t)op->nF * op->nIC;
+        if (slot >= op->fib_acc_slots) return fail(CGB_ERR_INVALID, "fibre pass: no accumulator for this vector");
         int gb = (int)((total + 255) / 256);
         if (gb > op->nsm * 16) gb = op->nsm * 16;
-        k_fibre_sum32_slab<<<gb, 256, 0, st>>>(op->dev(), scr, xout, op->fib_slab, op->fib_acc, s, op->nslab);
+        k_fibre_sum32_slab<<<gb, 256, 0, st>>>(op->dev(), scr, xout, op->fib_slab, op->fib_acc + (size_t)slot * total,
+                                                s, op->nslab);
         CGB_CUDA(cudaGetLastError());
     }
     return CGB_OK;
