@@ -152,6 +152,7 @@ struct cgb_op {
     float tc_lscale;                // 2^-k of the FP16 lengths
     uint32_t *tc_ptr, *tc_co;       // entry offsets per (tile, K-block, voxel); column | row << 26
     __half *tc_l;                   // entry lengths (FP16, scaled by 2^k)
+    uint8_t *tc_vl;                 // entry voxel within its tile
     __nv_bfloat16 *tc_bimg;         // LUT K-block images (swizzled BF16)
     float *tc_xe;                   // x * eval as FP32, per forward
     int *tc_err;                    // device status word of the bounded waits

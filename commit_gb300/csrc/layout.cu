@@ -295,7 +295,7 @@ static void free_op(cgb_op *op) {
                     op->seg_f, op->eval, op->fib_ptr, op->fib_perm, op->fib_order, op->ec_ptr, op->ec_col, op->iso_ptr,
                     op->iso_col, op->seg_o, op->ec_o, op->seg_l, op->scratch, op->scratch32, op->partials,
                     op->dscal, op->d_in, op->d_out, op->d_x64, op->fib_slab, op->fib_acc, op->d_xmax,
-                    op->tc_ptr, op->tc_co, op->tc_l, op->tc_bimg, op->tc_xe, op->tc_err,
+                    op->tc_ptr, op->tc_co, op->tc_l, op->tc_vl, op->tc_bimg, op->tc_xe, op->tc_err,
                     op->tc_fptr, op->tc_fperm, op->tc_abimg, op->tc_terms, op->tc_ax, op->tc_rows16, op->tc_ford};
     for (void *p : ptrs)
         if (p) cudaFree(p);

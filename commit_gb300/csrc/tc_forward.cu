@@ -57,6 +57,7 @@ struct TcFwdArgs {
     const uint32_t *ent_ptr;
     const uint32_t *ent_co;
     const __half *ent_l;
+    const uint8_t *ent_vl;  // voxel of each entry within its tile
     float l_scale;
     const float *xe;
     const __nv_bfloat16 *bimg;
@@ -68,10 +69,34 @@ struct TcFwdArgs {
 
 __host__ __device__ constexpr size_t tc_smem_bytes(int Np) {
     return 1024 /* alignment slack */ + 4 * 16384 /* A hi / lo x 2 stages */ + 2 * (size_t)Np * 128 /* B x 2 */ +
-           2 * kTcTile * kStageStride * 4 /* FP32 staging, 2 parts */ + 128 /* barriers, TMEM slot, flags */;
+           kTcTile * kStageStride * 4 /* FP32 staging */ + 128 /* barriers, TMEM slot, flags */;
 }
 
 constexpr int kTcItems = 8;  // EC / ISO items of a voxel held in registers (more take a loop)
+constexpr int kSlice = 8;    // entries of a K-block per thread and pass (kTcThreads * kSlice per pass)
+constexpr int kWin = kSlice + 2;  // the entry before the slice, the slice, the entry after it
+
+// A thread's window of entries for one pass over a K-block's range [b0, b1): entry s0 - 1,
+// the slice [s0, s0 + kSlice) and entry s0 + kSlice; per entry its column | row (co) and
+// its FP16 length | voxel-in-tile << 16 (lv); 0xffffffff marks an entry outside the range.
+struct Window {
+    uint32_t co[kWin], lv[kWin];
+    __device__ __forceinline__ void load(const TcFwdArgs &A, uint32_t b0, uint32_t b1, uint32_t s0) {
+#pragma unroll
+        for (int i = 0; i < kWin; ++i) {
+            const uint32_t j = s0 + (uint32_t)i - 1u;
+            co[i] = 0xffffffffu;
+            lv[i] = 0xffffffffu;
+            if ((i > 0 || s0 > b0) && j < b1) {
+                co[i] = __ldg(A.ent_co + j);
+                lv[i] = (uint32_t)__half_as_ushort(A.ent_l[j]) | ((uint32_t)A.ent_vl[j] << 16);
+            }
+        }
+    }
+};
+
+// cell of an entry: voxel in tile * 64 + row in the K-block (the staging index before padding)
+__device__ __forceinline__ uint32_t cell_of(uint32_t co, uint32_t lv) { return ((lv >> 16) << 6) | (co >> kColBits); }
 
 // r[0..15] += xv * the 16 BF16 values of w (two 16-byte words)
 __device__ __forceinline__ void fma16(float (&r)[16], float xv, const uint4 &a, const uint4 &b) {
@@ -116,7 +141,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_forward_tc(const TcFwdArgs A)
     uint8_t *a_lo = sm + 2 * 16384;           // 2 x 16384
     uint8_t *b_img = sm + 4 * 16384;          // 2 x bbytes
     float *stage = reinterpret_cast<float *>(b_img + 2 * bbytes);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(stage + 2 * kTcTile * kStageStride);  // bfull[2], mdone[2]
+    uint64_t *bars = reinterpret_cast<uint64_t *>(stage + kTcTile * kStageStride);  // bfull[2], mdone[2]
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 4);
     uint64_t *bfull = bars, *mdone = bars + 2;
 
@@ -132,15 +157,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_forward_tc(const TcFwdArgs A)
         tc::tmem_alloc(tmem_slot, 512);
         tc::tmem_relinquish();
     }
-    for (int i = tid; i < 2 * kTcTile * kStageStride; i += kTcThreads) stage[i] = 0.f;
+    for (int i = tid; i < kTcTile * kStageStride; i += kTcThreads) stage[i] = 0.f;
     tc::tc_fence_before();
     __syncthreads();
     tc::tc_fence_after();
     const uint32_t tmem = *tmem_slot;
     const int half = A.Np / 2;
     const uint32_t idesc = tc::idesc_bf16(kTcTile, half);
-    const int vloc = tid & (kTcTile - 1), part = tid >> 7;
-    float *myrow = stage + (part * kTcTile + vloc) * kStageStride;
     uint32_t it = 0;  // K-blocks processed by this CTA (pipeline stage = it & 1)
     // thread 0: iteration of the last bulk copy issued / MMA group committed per stage, for
     // draining on an early exit (kNone: none)
@@ -154,20 +177,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_forward_tc(const TcFwdArgs A)
     int bad = 0;
     bool stop = false;
 
-    // Entry pipeline of this thread (its half of its voxel's entries, per K-block in the
-    // CTA's order of (tile, K-block)): for the block being walked, [cj0, cj1) with the first 8
-    // entries (column | row, length) and their x values in registers; for the block after it,
-    // [nj0, nj1) with its first 8 entries loading; for the block after that, its offsets
-    // loading.  So the gathers of x and of the entries run one and two K-blocks ahead.
-    uint32_t cj0 = 0, cj1 = 0, nj0 = 0, nj1 = 0;
-    uint32_t cco[8], nco[8];
-    float cl[8], nl[8], cx[8];
+    // Entry walk.  A K-block's entries (one tile) form the range [b0, b1), sorted by cell
+    // (voxel, LUT row), each cell's entries contiguous.  Each thread takes slices of
+    // kSlice entries (pass p: s0 = b0 + (p * kTcThreads + tid) * kSlice) and sums, in entry
+    // order, every cell whose first entry lies in its slice, reading past the slice to the
+    // end of its last cell; each cell is stored once, by one thread, so the result does not
+    // depend on the slicing.  Pipeline: while a K-block is walked, the x values of the next
+    // one's first window and the entries of the window after that are loading.
     const uint32_t kColMask = (1u << kColBits) - 1u;
-    auto half_range = [&](uint32_t p0, uint32_t p1, uint32_t &j0, uint32_t &j1) {
-        const uint32_t hcount = (p1 - p0 + 1) >> 1;
-        j0 = part ? p0 + hcount : p0;
-        j1 = part ? p1 : p0 + hcount;
-    };
     // (tile, K-block) `ahead` blocks after (t, k) in this CTA's order; false past the end
     auto step = [&](int t, int k, int ahead, int &t2, int &k2) {
         k2 = k + ahead;
@@ -178,33 +195,59 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_forward_tc(const TcFwdArgs A)
         }
         return t2 < A.ntiles;
     };
-    auto ptr_of = [&](int t, int k) { return ((size_t)t * A.NKB + k) * kTcTile + vloc; };
+    auto range_of = [&](int t, int k, uint32_t &b0, uint32_t &b1) {
+        const size_t pb = ((size_t)t * A.NKB + k) * kTcTile;
+        b0 = A.ent_ptr[pb];
+        b1 = A.ent_ptr[pb + kTcTile];
+    };
+    const uint32_t s_off = (uint32_t)tid * kSlice;
+    Window cw, nw;  // current K-block's first window, next K-block's
+    float cx[kWin];
+    uint32_t cb0 = 0, cb1 = 0, nb0 = 0, nb1 = 0;
+    auto load_x = [&](const Window &w, float (&x)[kWin]) {
+#pragma unroll
+        for (int i = 1; i < kWin; ++i) x[i] = w.co[i] != 0xffffffffu ? __ldg(A.xe + (w.co[i] & kColMask)) : 0.f;
+        x[0] = 0.f;
+    };
     if ((int)blockIdx.x < A.ntiles) {
         int t1, k1;
-        size_t pb = ptr_of(blockIdx.x, 0);
-        half_range(A.ent_ptr[pb], A.ent_ptr[pb + 1], cj0, cj1);
-        if (step(blockIdx.x, 0, 1, t1, k1)) {
-            pb = ptr_of(t1, k1);
-            half_range(A.ent_ptr[pb], A.ent_ptr[pb + 1], nj0, nj1);
-        }
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            cco[u] = 0;
-            cl[u] = 0.f;
-            nco[u] = 0;
-            nl[u] = 0.f;
-            if (cj0 + u < cj1) {
-                cco[u] = __ldg(A.ent_co + cj0 + u);
-                cl[u] = __half2float(A.ent_l[cj0 + u]);
-            }
-            if (nj0 + u < nj1) {
-                nco[u] = __ldg(A.ent_co + nj0 + u);
-                nl[u] = __half2float(A.ent_l[nj0 + u]);
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < 8; ++u) cx[u] = cj0 + u < cj1 ? __ldg(A.xe + (cco[u] & kColMask)) : 0.f;
+        range_of(blockIdx.x, 0, cb0, cb1);
+        if (step(blockIdx.x, 0, 1, t1, k1)) range_of(t1, k1, nb0, nb1);
+        cw.load(A, cb0, cb1, cb0 + s_off);
+        nw.load(A, nb0, nb1, nb0 + s_off);
+        load_x(cw, cx);
     }
+    // the runs of one window: cells whose first entry is in the slice; returns with the
+    // last one still open (cur, acc) when the slice ends inside it
+    auto walk_window = [&](const Window &w, const float (&x)[kWin], uint32_t s0, uint32_t b0, uint32_t b1) {
+        uint32_t cur = 0xffffffffu;
+        float acc = 0.f;
+        uint32_t prev = w.co[0] != 0xffffffffu ? cell_of(w.co[0], w.lv[0]) : 0xffffffffu;
+#pragma unroll
+        for (int i = 1; i <= kSlice; ++i) {
+            if (w.co[i] == 0xffffffffu) break;
+            const uint32_t c = cell_of(w.co[i], w.lv[i]);
+            if (c != prev) {  // first entry of a cell
+                if (cur != 0xffffffffu) stage[(cur >> 6) * kStageStride + (cur & 63u)] = acc;
+                cur = c;
+                acc = 0.f;
+            }
+            prev = c;
+            if (cur != 0xffffffffu) acc += __half2float(__ushort_as_half((unsigned short)(w.lv[i] & 0xffffu))) * x[i];
+        }
+        if (cur == 0xffffffffu) return;
+        // the open cell continues past the slice: the window's last entry, then loads
+        uint32_t j = s0 + kSlice;
+        if (w.co[kWin - 1] != 0xffffffffu && cell_of(w.co[kWin - 1], w.lv[kWin - 1]) == cur) {
+            acc += __half2float(__ushort_as_half((unsigned short)(w.lv[kWin - 1] & 0xffffu))) * x[kWin - 1];
+            for (j = s0 + kSlice + 1; j < b1; ++j) {
+                const uint32_t co = __ldg(A.ent_co + j);
+                if (cell_of(co, (uint32_t)A.ent_vl[j] << 16) != cur) break;
+                acc += __half2float(A.ent_l[j]) * __ldg(A.xe + (co & kColMask));
+            }
+        }
+        stage[(cur >> 6) * kStageStride + (cur & 63u)] = acc;
+    };
 
     for (int tile = blockIdx.x; tile < A.ntiles && !stop; tile += gridDim.x) {
         // the epilogue's voxel: its EC / ISO items, the first kTcItems (row, x) loaded ahead
@@ -242,56 +285,30 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_forward_tc(const TcFwdArgs A)
                 tc::bulk_g2s(b_img + s * bbytes, A.bimg + (size_t)kb * A.Np * kTcKB, bbytes, &bfull[s]);
                 last_b[s] = it;
             }
-            // offsets of the block two ahead, loading during this block's walk
+            // range of the block two ahead, loading during this block's walk
             int t2, k2;
             const bool has2 = step(tile, kb, 2, t2, k2);
-            uint32_t q0 = 0, q1 = 0;
-            if (has2) {
-                const size_t pb = ptr_of(t2, k2);
-                q0 = A.ent_ptr[pb];
-                q1 = A.ent_ptr[pb + 1];
+            uint32_t qb0 = 0, qb1 = 0;
+            if (has2) range_of(t2, k2, qb0, qb1);
+            // C rows of this K-block: first pass from the prefetched window, further passes
+            // (more than kTcThreads * kSlice entries) load their windows here
+            walk_window(cw, cx, cb0 + s_off, cb0, cb1);
+            for (uint32_t s0 = cb0 + s_off + kTcThreads * kSlice; s0 < cb1; s0 += kTcThreads * kSlice) {
+                Window w;
+                float x[kWin];
+                w.load(A, cb0, cb1, s0);
+                load_x(w, x);
+                walk_window(w, x, s0, cb0, cb1);
             }
-            // C rows of this K-block: two threads per voxel, each over half of its entries
-            for (uint32_t j = cj0; j < cj1; j += 8) {
-                if (j != cj0) {
-#pragma unroll
-                    for (int u = 0; u < 8; ++u) {
-                        cco[u] = 0;
-                        cl[u] = 0.f;
-                        if (j + u < cj1) {
-                            cco[u] = __ldg(A.ent_co + j + u);
-                            cl[u] = __half2float(A.ent_l[j + u]);
-                        }
-                    }
-#pragma unroll
-                    for (int u = 0; u < 8; ++u) cx[u] = j + u < cj1 ? __ldg(A.xe + (cco[u] & kColMask)) : 0.f;
-                }
-#pragma unroll
-                for (int u = 0; u < 8; ++u)
-                    if (j + u < cj1) myrow[cco[u] >> kColBits] += cl[u] * cx[u];
-            }
-            // shift the pipeline: the next block's entries (loaded a block ago) become
-            // current and their x values start loading; the block two ahead starts loading
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                cco[u] = nco[u];
-                cl[u] = nl[u];
-            }
-            cj0 = nj0;
-            cj1 = nj1;
-#pragma unroll
-            for (int u = 0; u < 8; ++u) cx[u] = cj0 + u < cj1 ? __ldg(A.xe + (cco[u] & kColMask)) : 0.f;
-            nj0 = nj1 = 0;
-            if (has2) half_range(q0, q1, nj0, nj1);
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                nco[u] = 0;
-                nl[u] = 0.f;
-                if (nj0 + u < nj1) {
-                    nco[u] = __ldg(A.ent_co + nj0 + u);
-                    nl[u] = __half2float(A.ent_l[nj0 + u]);
-                }
-            }
+            // shift the pipeline: the next block's window (loaded a block ago) becomes current
+            // and its x values start loading; the window of the block two ahead starts loading
+            cw = nw;
+            cb0 = nb0;
+            cb1 = nb1;
+            load_x(cw, cx);
+            nb0 = qb0;
+            nb1 = qb1;
+            nw.load(A, nb0, nb1, nb0 + s_off);
             __syncthreads();
             // FP32 rows -> BF16 hi / lo in the swizzled layout; staging back to zero
             uint8_t *ah = a_hi + s * 16384, *al = a_lo + s * 16384;
@@ -300,10 +317,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_forward_tc(const TcFwdArgs A)
             for (int q = tid; q < kTcTile * 8; q += kTcThreads) {
                 const int m = q >> 3, p = q & 7, cl = p ^ (m & 7);
                 float4 *r0 = reinterpret_cast<float4 *>(stage + m * kStageStride + cl * 8);
-                float4 *r1 = reinterpret_cast<float4 *>(stage + (kTcTile + m) * kStageStride + cl * 8);
-                const float4 x0 = r0[0], x1 = r0[1], y0 = r1[0], y1 = r1[1];
-                const float v[8] = {x0.x + y0.x, x0.y + y0.y, x0.z + y0.z, x0.w + y0.w,
-                                    x1.x + y1.x, x1.y + y1.y, x1.z + y1.z, x1.w + y1.w};
+                const float4 x0 = r0[0], x1 = r0[1];
+                const float v[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
                 uint32_t hw[4], lw[4];
 #pragma unroll
                 for (int e = 0; e < 4; ++e) {
@@ -320,8 +335,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_forward_tc(const TcFwdArgs A)
                 const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
                 r0[0] = z;
                 r0[1] = z;
-                r1[0] = z;
-                r1[1] = z;
             }
             tc::fence_async_smem();
             if (__syncthreads_or(bad)) {
@@ -472,11 +485,13 @@ __global__ void k_tc_entries(const TcLayoutArgs L, const __half *__restrict__ l1
 }
 
 __global__ void k_tc_split(const unsigned long long *__restrict__ val, int64_t n, uint32_t *__restrict__ co,
-                           __half *__restrict__ l, const uint32_t *__restrict__ key, uint32_t *__restrict__ count) {
+                           __half *__restrict__ l, uint8_t *__restrict__ vl, const uint32_t *__restrict__ key,
+                           uint32_t *__restrict__ count) {
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
         const unsigned long long w = val[q];
         co[q] = (uint32_t)w;
         l[q] = __ushort_as_half((unsigned short)(w >> 32));
+        vl[q] = (uint8_t)(key[q] & (uint32_t)(kTcTile - 1));
         atomicAdd(count + key[q], 1u);
     }
 }
@@ -623,6 +638,7 @@ int ensure_tc(cgb_op *op) {
     while (bits < 32 && (((uint64_t)nkeys) >> bits) != 0) ++bits;
     cu(cudaMalloc((void **)&op->tc_co, nent * sizeof(uint32_t)), "cudaMalloc");
     cu(cudaMalloc((void **)&op->tc_l, nent * sizeof(__half)), "cudaMalloc");
+    cu(cudaMalloc((void **)&op->tc_vl, nent * sizeof(uint8_t)), "cudaMalloc");
     cu(cudaMalloc((void **)&op->tc_ptr, (nkeys + 1) * sizeof(uint32_t)), "cudaMalloc");
     cu(cudaMalloc((void **)&op->tc_bimg, (size_t)(NKB > 0 ? NKB : 1) * Np * kTcKB * sizeof(__nv_bfloat16)),
        "cudaMalloc");
@@ -649,7 +665,7 @@ int ensure_tc(cgb_op *op) {
     }
     if (rc == CGB_OK) {
         cu(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, key, key2, val, val2, nent, 0, bits), "cub sort");
-        k_tc_split<<<grid_of(nent, op->nsm), 256>>>(val2, nent, op->tc_co, op->tc_l, key2, count);
+        k_tc_split<<<grid_of(nent, op->nsm), 256>>>(val2, nent, op->tc_co, op->tc_l, op->tc_vl, key2, count);
         cu(cudaGetLastError(), "k_tc_split");
         cu(cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, count, op->tc_ptr, nkeys + 1), "cub scan");
         const int64_t nimg = (int64_t)NKB * Np * kTcKB;
@@ -758,7 +774,7 @@ int ensure_tc(cgb_op *op) {
     op->tc_kbs = KBS;
     op->tc_rounds = R;
     op->tc_nent = nent;
-    op->bytes += nent * 6 + (nkeys + 1) * 4 + (size_t)NKB * Np * kTcKB * 2 + (size_t)op->ncols * 4 + nent * 8 +
+    op->bytes += nent * 7 + (nkeys + 1) * 4 + (size_t)NKB * Np * kTcKB * 2 + (size_t)op->ncols * 4 + nent * 8 +
                  (size_t)(nic_cols + 1) * 4 + (size_t)nic_cols * 4 + (size_t)R * KBS * 2 * 128 * 64 * 2 +
                  (size_t)(nec_rows + niso_rows) * Np * 2;
     op->tc_ready = 1;
@@ -798,6 +814,7 @@ int forward_tc(cgb_op *op, const double *x, float *y, float *ax, const float *yo
     A.ent_ptr = op->tc_ptr;
     A.ent_co = op->tc_co;
     A.ent_l = op->tc_l;
+    A.ent_vl = op->tc_vl;
     A.l_scale = op->tc_lscale;
     A.xe = op->tc_xe;
     A.bimg = op->tc_bimg;
