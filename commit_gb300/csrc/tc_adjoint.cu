@@ -75,38 +75,34 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 }
 
 // dot products of row m of the tile's z (BF16 hi + lo, K-major swizzled in shared memory)
-// with up to four BF16 LUT rows of stride Np (the first `cnt` of rp), FP32, samples in
-// order, hi then lo per sample
-__device__ __forceinline__ void z_dot_rows4(const uint8_t *a_hi, const uint8_t *a_lo, int m, int KBS, int Np,
-                                            const __nv_bfloat16 *const (&rp)[4], int cnt, float (&acc)[4]) {
+// with four BF16 LUT rows of stride Np (unused items point at a valid row and are ignored
+// by the caller), FP32, samples in order, hi then lo per sample.  The chunk loop has no
+// branches, so the row loads of the unrolled chunks are issued together.
+__device__ __forceinline__ void z_dot_rows4(const uint8_t *a_hi, const uint8_t *a_lo, int m, int Np,
+                                            const __nv_bfloat16 *const (&rp)[4], float (&acc)[4]) {
 #pragma unroll
     for (int u = 0; u < 4; ++u) acc[u] = 0.f;
-    const uint32_t rbase = (uint32_t)(m >> 3) * 1024u + (uint32_t)(m & 7) * 128u;
-    for (int kb = 0; kb < KBS; ++kb) {
+    const uint32_t rbase = (uint32_t)(m >> 3) * 1024u + (uint32_t)(m & 7) * 128u, sw = (uint32_t)(m & 7);
+    const int nch = Np >> 3;  // 8-sample chunks; Np is a multiple of 32
 #pragma unroll 4
-        for (int p = 0; p < 8; ++p) {
-            const int s0 = kb * 64 + p * 8;
-            if (s0 >= Np) break;
-            const uint32_t off = (uint32_t)kb * 16384u + rbase + (uint32_t)((p ^ (m & 7)) * 16);
-            const uint4 h = *reinterpret_cast<const uint4 *>(a_hi + off);
-            const uint4 l = *reinterpret_cast<const uint4 *>(a_lo + off);
-            const uint32_t hw[4] = {h.x, h.y, h.z, h.w}, lw[4] = {l.x, l.y, l.z, l.w};
-            uint4 w[4];
+    for (int c = 0; c < nch; ++c) {
+        const uint32_t off = (uint32_t)(c >> 3) * 16384u + rbase + (((uint32_t)(c & 7) ^ sw) << 4);
+        const uint4 h = *reinterpret_cast<const uint4 *>(a_hi + off);
+        const uint4 l = *reinterpret_cast<const uint4 *>(a_lo + off);
+        uint4 w[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u)
-                if (u < cnt) w[u] = __ldg(reinterpret_cast<const uint4 *>(rp[u] + s0));
+        for (int u = 0; u < 4; ++u) w[u] = __ldg(reinterpret_cast<const uint4 *>(rp[u] + c * 8));
+        const uint32_t hw[4] = {h.x, h.y, h.z, h.w}, lw[4] = {l.x, l.y, l.z, l.w};
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                if (u >= cnt) continue;
-                const uint32_t ww[4] = {w[u].x, w[u].y, w[u].z, w[u].w};
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t ww[4] = {w[u].x, w[u].y, w[u].z, w[u].w};
 #pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    const float w0 = __uint_as_float(ww[e] << 16), w1 = __uint_as_float(ww[e] & 0xffff0000u);
-                    acc[u] = fmaf(__uint_as_float(hw[e] << 16), w0, acc[u]);
-                    acc[u] = fmaf(__uint_as_float(lw[e] << 16), w0, acc[u]);
-                    acc[u] = fmaf(__uint_as_float(hw[e] & 0xffff0000u), w1, acc[u]);
-                    acc[u] = fmaf(__uint_as_float(lw[e] & 0xffff0000u), w1, acc[u]);
-                }
+            for (int e = 0; e < 4; ++e) {
+                const float w0 = __uint_as_float(ww[e] << 16), w1 = __uint_as_float(ww[e] & 0xffff0000u);
+                acc[u] = fmaf(__uint_as_float(hw[e] << 16), w0, acc[u]);
+                acc[u] = fmaf(__uint_as_float(lw[e] << 16), w0, acc[u]);
+                acc[u] = fmaf(__uint_as_float(hw[e] & 0xffff0000u), w1, acc[u]);
+                acc[u] = fmaf(__uint_as_float(lw[e] & 0xffff0000u), w1, acc[u]);
             }
         }
     }
@@ -147,8 +143,12 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
     // issuer state (warp 4, lane 0): items and rounds issued so far, last copy / commit per stage
     uint32_t gq = 0, rgi = 0;
     uint32_t last_b[2] = {kNone, kNone}, last_c[2] = {kNone, kNone};
-    // drain state (warps 0-3): rounds drained so far
+    // drain state (warps 0-3): rounds drained so far, entry pipeline (see (3))
     uint32_t rgd = 0;
+    uint32_t d_j0 = 0, d_j1 = 0, d_n0 = 0, d_n1 = 0;
+    uint32_t d_co[8];
+    float d_l[8];
+    bool d_primed = false;
     int bad = 0;
     double nrm = 0.0;
     // 8-sample items never straddle a row end and start 32-byte aligned when nS % 8 == 0
@@ -290,9 +290,46 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
                 rgi += (uint32_t)A.R;
             }
         } else if (warp < 4) {
-            // (3) drain: each thread is one voxel (TMEM lane); items of the round's LUT rows
+            // (3) drain: each thread is one voxel (TMEM lane); items of the round's LUT rows.
+            // Entry pipeline (carried across tiles): at the start of a K-block the first 8 of
+            // its entries are in registers, the next K-block's first 8 start loading and the
+            // offsets of the one after that too.
             const int vloc = warp * 32 + lane;
             float *row = dstage + (warp * 32 + lane) * kADrainStride;
+            auto range_of = [&](int t, int k, uint32_t &b0, uint32_t &b1) {
+                const size_t pb = ((size_t)t * A.NKB + k) * kATile + vloc;
+                b0 = A.ent_ptr[pb];
+                b1 = A.ent_ptr[pb + 1];
+            };
+            auto after = [&](int t, int k, int ahead, int &t2, int &k2) {
+                k2 = k + ahead;
+                t2 = t;
+                while (k2 >= A.NKB) {
+                    k2 -= A.NKB;
+                    t2 += gridDim.x;
+                }
+                return t2 < A.ntiles;
+            };
+            auto load8 = [&](uint32_t j0, uint32_t j1, uint32_t (&co)[8], float (&l)[8]) {
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    co[u] = 0xffffffffu;
+                    l[u] = 0.f;
+                    if (j0 + u < j1) {
+                        co[u] = __ldg(A.ent_co + j0 + u);
+                        l[u] = __half2float(A.ent_l[j0 + u]);
+                    }
+                }
+            };
+            if (!d_primed) {
+                int t1, k1;
+                range_of(tile, 0, d_j0, d_j1);
+                load8(d_j0, d_j1, d_co, d_l);
+                d_n0 = d_n1 = 0;
+                if (after(tile, 0, 1, t1, k1)) range_of(t1, k1, d_n0, d_n1);
+                d_primed = true;
+            }
+            const float lsc = A.l_scale;
             for (int r = 0; r < A.R; ++r) {
                 const uint32_t rg = rgd + (uint32_t)r;
                 if (!bad && !tc::mbar_wait(&gfull[rg & 1u], (rg >> 1) & 1u)) {
@@ -304,12 +341,14 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
                 for (int kbl = 0; kbl < kARows / 64; ++kbl) {
                     const int kbf = r * (kARows / 64) + kbl;
                     if (kbf >= A.NKB) break;
-                    const size_t pb = ((size_t)tile * A.NKB + kbf) * kATile + vloc;
-                    uint32_t j = A.ent_ptr[pb];
-                    const uint32_t p1 = A.ent_ptr[pb + 1];
-                    const float lsc = A.l_scale;
-                    // the K-block's 64 columns of this voxel into its private row; the items
-                    // of the K-block come in segment order, not row order
+                    // next K-block's first entries and the offsets of the one after it
+                    uint32_t nco[8];
+                    float nl[8];
+                    load8(d_n0, d_n1, nco, nl);
+                    int t2, k2;
+                    uint32_t q0 = 0, q1 = 0;
+                    if (after(tile, kbf, 2, t2, k2)) range_of(t2, k2, q0, q1);
+                    // the K-block's 64 columns of this voxel into its private row
                     __syncwarp();
 #pragma unroll
                     for (int c = 0; c < 2; ++c) {
@@ -319,26 +358,41 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
 #pragma unroll
                         for (int i = 0; i < 32; ++i) row[c * 32 + i] = g[i];
                     }
-                    // four entries per step, their loads issued together
-                    for (; j < p1; j += 4) {
+                    // the first 8 entries from registers, the rest four at a time
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const uint32_t o = d_co[u] >> kAColBits;
+                        // o < 64 always holds for the layout's entries; never indexes outside the row
+                        if (d_j0 + u < d_j1 && o < 64u) A.terms[d_j0 + u] = row[o] * (d_l[u] * lsc);
+                    }
+                    for (uint32_t j = d_j0 + 8; j < d_j1; j += 4) {
                         uint32_t co[4];
                         float l[4];
 #pragma unroll
                         for (int u = 0; u < 4; ++u) {
                             co[u] = 0xffffffffu;
                             l[u] = 0.f;
-                            if (j + u < p1) {
-                                co[u] = A.ent_co[j + u];
+                            if (j + u < d_j1) {
+                                co[u] = __ldg(A.ent_co + j + u);
                                 l[u] = __half2float(A.ent_l[j + u]);
                             }
                         }
 #pragma unroll
                         for (int u = 0; u < 4; ++u) {
                             const uint32_t o = co[u] >> kAColBits;
-                            // o < 64 always holds for the layout's entries; never indexes outside the row
-                            if (j + u < p1 && o < 64u) A.terms[j + u] = row[o] * (l[u] * lsc);
+                            if (j + u < d_j1 && o < 64u) A.terms[j + u] = row[o] * (l[u] * lsc);
                         }
                     }
+                    // shift the pipeline
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        d_co[u] = nco[u];
+                        d_l[u] = nl[u];
+                    }
+                    d_j0 = d_n0;
+                    d_j1 = d_n1;
+                    d_n0 = q0;
+                    d_n1 = q1;
                 }
                 tc::tc_fence_before();
                 tc::mbar_arrive(&drained[rg & 1u]);
@@ -379,7 +433,7 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
                         rp[u] = A.rows16 + (size_t)row * A.Np;
                     }
                     float acc[4];
-                    z_dot_rows4(a_hi, a_lo, m, A.KBS, A.Np, rp, n - k0, acc);
+                    z_dot_rows4(a_hi, a_lo, m, A.Np, rp, acc);
 #pragma unroll
                     for (int u = 0; u < 4; ++u)
                         if (k0 + u < n) A.xout[col[u]] = (double)acc[u];
