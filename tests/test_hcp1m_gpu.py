@@ -83,3 +83,22 @@ def test_reduced_precision_matches_reference(hcp, arith):
     assert G.rel(ax[r0:r1].double().cpu().numpy(), hcp['ax_ref']) <= REDUCED_TOL[arith]
     aty = A.T.dot(torch.from_numpy(hcp['ym']).cuda().float(), arith=arith)
     assert G.rel(aty.double().cpu().numpy(), hcp['aty_ref']) <= REDUCED_TOL[arith]
+
+
+def test_tensor_cores_at_full_workload(hcp):
+    """The tensor-core BF16 operator at 1M streamlines (the default there: 212 IC segments per
+    voxel; its adjoint runs in slabs of tiles whose fibre passes gather from L2) against the
+    CUDA-core BF16 kernels on the same BF16 LUT (1e-4), bitwise repeatable."""
+    from commit_gb300.operator import LinearOperator
+    A = LinearOperator(hcp['D'], hcp['K'], None)
+    x = torch.from_numpy(hcp['x']).cuda().float()
+    y = torch.from_numpy(hcp['ym']).cuda().float()
+    assert A.tensor_cores(None)  # chosen by density
+    ax1, ax2 = A.dot(x, arith='bf16'), A.dot(x, arith='bf16')
+    g1, g2 = A.T.dot(y, arith='bf16'), A.T.dot(y, arith='bf16')
+    A.device_status()
+    A.tensor_cores(1)
+    axc, gc = A.dot(x, arith='bf16'), A.T.dot(y, arith='bf16')
+    assert torch.equal(ax1, ax2) and torch.equal(g1, g2)
+    assert G.rel(ax1.double().cpu().numpy(), axc.double().cpu().numpy()) <= 1e-4
+    assert G.rel(g1.double().cpu().numpy(), gc.double().cpu().numpy()) <= 1e-4
