@@ -49,6 +49,26 @@ constexpr int kBlock = 256;          // threads per block of the voxel kernels
 constexpr int kRedSlots = 16;        // doubles reduced per block in the FISTA partial sums
 
 // ------------------------------------------------------------------ device view of a handle
+// a + sum of terms[perm[k]] for k in [beg, end), added in k order (the fibre passes' column
+// sums); eight gathers in flight per step
+template <class T>
+__device__ __forceinline__ double fibre_gather_sum(const uint32_t *__restrict__ perm, const T *__restrict__ terms,
+                                                   uint32_t beg, uint32_t end, double a) {
+    uint32_t k = beg;
+    for (; k + 8 <= end; k += 8) {
+        uint32_t i[8];
+        T t[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) i[u] = __ldg(perm + k + u);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) t[u] = __ldg(terms + i[u]);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) a += (double)t[u];
+    }
+    for (; k < end; ++k) a += (double)__ldg(terms + __ldg(perm + k));
+    return a;
+}
+
 struct OpDev {
     int nS, ndirs, nF, nE, nV, nISOv, nIC, nEC, nISO;
     int v0;                         // first voxel of the launch (voxels v0 .. nV-1; 0 for a full pass)

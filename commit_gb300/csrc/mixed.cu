@@ -76,9 +76,7 @@ __global__ void k_fibre_sum32(const OpDev P, const float *__restrict__ scr, doub
          q += (int64_t)gridDim.x * blockDim.x) {
         const int i = (int)(q / P.nF);
         const uint32_t f = P.fib_order[q - (int64_t)i * P.nF];
-        const float *S = scr + (size_t)i * P.n;
-        double s = 0.0;
-        for (uint32_t k = P.fib_ptr[f]; k < P.fib_ptr[f + 1]; ++k) s += (double)S[P.fib_perm[k]];
+        const double s = fibre_gather_sum(P.fib_perm, scr + (size_t)i * P.n, P.fib_ptr[f], P.fib_ptr[f + 1], 0.0);
         const int64_t c = (int64_t)i * P.nF + f;
         xout[c] = s * (double)P.eval[c];
     }
@@ -113,9 +111,7 @@ __global__ void k_fibre_sum32_slab(const OpDev P, const float *__restrict__ scr,
         const int64_t fq = q - (int64_t)i * P.nF;
         const uint32_t beg = fib_slab[(size_t)s * P.nF + fq], end = fib_slab[(size_t)(s + 1) * P.nF + fq];
         if (s > 0 && s < S - 1 && beg == end) continue;
-        const float *T = scr + (size_t)i * P.n;
-        double acc = s == 0 ? 0.0 : accb[q];
-        for (uint32_t k = beg; k < end; ++k) acc += (double)T[P.fib_perm[k]];
+        const double acc = fibre_gather_sum(P.fib_perm, scr + (size_t)i * P.n, beg, end, s == 0 ? 0.0 : accb[q]);
         if (s == S - 1) {
             const int64_t c = (int64_t)i * P.nF + P.fib_order[fq];
             xout[c] = acc * (double)P.eval[c];

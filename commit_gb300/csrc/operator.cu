@@ -33,9 +33,7 @@ __global__ void k_fibre_sum(const OpDev P, const double *__restrict__ scratch, d
         const int i = (int)(q / P.nF);
         const uint32_t f = P.fib_order[q - (int64_t)i * P.nF];
         const uint32_t beg = P.fib_ptr[f], end = P.fib_ptr[f + 1];
-        const double *S = scratch + (size_t)i * P.n;
-        double s = 0.0;
-        for (uint32_t k = beg; k < end; ++k) s += S[P.fib_perm[k]];
+        const double s = fibre_gather_sum(P.fib_perm, scratch + (size_t)i * P.n, beg, end, 0.0);
         const int64_t c = (int64_t)i * P.nF + f;
         xout[c] = s * (double)P.eval[c];
     }
@@ -122,9 +120,7 @@ __global__ void k_fibre_sum_slab(const OpDev P, const double *__restrict__ scrat
         const int64_t fq = q - (int64_t)i * P.nF;
         const uint32_t beg = fib_slab[(size_t)s * P.nF + fq], end = fib_slab[(size_t)(s + 1) * P.nF + fq];
         if (s > 0 && s < S - 1 && beg == end) continue;
-        const double *T = scratch + (size_t)i * P.n;
-        double acc = s == 0 ? 0.0 : accb[q];
-        for (uint32_t k = beg; k < end; ++k) acc += T[P.fib_perm[k]];
+        const double acc = fibre_gather_sum(P.fib_perm, scratch + (size_t)i * P.n, beg, end, s == 0 ? 0.0 : accb[q]);
         if (s == S - 1) {
             const int64_t c = (int64_t)i * P.nF + P.fib_order[fq];
             xout[c] = acc * (double)P.eval[c];

@@ -471,7 +471,7 @@ __global__ void k_fibre_sum_entries_slab(const uint32_t *__restrict__ fslab, con
         const uint32_t beg = fslab[(size_t)s * ncols + q], end = fslab[(size_t)(s + 1) * ncols + q];
         if (s > 0 && s < S - 1 && beg == end) continue;
         double a = s == 0 ? 0.0 : acc[q];
-        for (uint32_t k = beg; k < end; ++k) a += (double)terms[fperm[k]];
+        a = fibre_gather_sum(fperm, terms, beg, end, a);
         if (s == S - 1) {
             const uint32_t c = ford[q];
             xout[c] = a * (double)eval[c];
@@ -489,8 +489,7 @@ __global__ void k_fibre_sum_entries(const uint32_t *__restrict__ fptr, const uin
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < ncols;
          q += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t c = ford[q];
-        double s = 0.0;
-        for (uint32_t k = fptr[c]; k < fptr[c + 1]; ++k) s += (double)terms[fperm[k]];
+        const double s = fibre_gather_sum(fperm, terms, fptr[c], fptr[c + 1], 0.0);
         xout[c] = s * (double)eval[c];
     }
 }
