@@ -180,11 +180,6 @@ struct cgb_op {
     int64_t tc_nent;                // entries
     uint32_t *tc_fptr, *tc_fperm;   // adjoint: IC entry positions grouped by column, CSR offsets
     uint32_t *tc_ford;              // adjoint: IC columns by their first entry position (fibre-pass order)
-    int tc_nslab;                   // adjoint slabs of tiles (1: none)
-    int *tc_slab_t;                 // host [tc_nslab + 1]: first tile of each slab
-    uint32_t *tc_fslab;             // [(tc_nslab + 1) * nF * nIC]: where slab s starts in the entry list of the
-                                    // column at fibre-pass position q
-    double *tc_acc;                 // [nF * nIC]: running column sums between slabs, pass order
     __nv_bfloat16 *tc_abimg;        // adjoint LUT images
     float *tc_terms;                // adjoint IC terms in entry order
     float *tc_ax;                   // A x rows for the gradient (FISTA), on demand

@@ -40,7 +40,6 @@ constexpr uint32_t kAColBits = 26;
 
 struct TcAdjArgs {
     int nV, nS, KBS, R, NKB, ntiles, Np;
-    int t0, t1;  // tiles of this launch (a slab)
     // EC / ISO items (voxel-ordered arrays of the handle) and their BF16 LUT rows (stride Np)
     int nE, nEC, nISOv, nISO, ndirs;
     int64_t ec_base, iso_base;
@@ -156,8 +155,7 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
     auto al16 = [](const float *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
     const bool vec8 = (A.nS & 7) == 0 && al16(A.yin) && al16(A.axa) && al16(A.axb) && al16(A.yobs) && al16(A.sqw);
     auto load8 = [](const float *p, size_t idx, float (&o)[8]) {
-        // input rows are read once per product: streaming loads
-        const float4 a = __ldcs(reinterpret_cast<const float4 *>(p + idx)), b = __ldcs(reinterpret_cast<const float4 *>(p + idx) + 1);
+        const float4 a = __ldg(reinterpret_cast<const float4 *>(p + idx)), b = __ldg(reinterpret_cast<const float4 *>(p + idx) + 1);
         o[0] = a.x;
         o[1] = a.y;
         o[2] = a.z;
@@ -168,7 +166,7 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
         o[7] = b.w;
     };
 
-    for (int tile = A.t0 + blockIdx.x; tile < A.t1; tile += gridDim.x) {
+    for (int tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
         // (1) the tile's input rows -> BF16 hi / lo, K-major swizzled, one tile per K-block;
         // 8 samples per item, two 16-byte loads per input row when the rows allow it
         float vn = 0.f;
@@ -310,7 +308,7 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
                     k2 -= A.NKB;
                     t2 += gridDim.x;
                 }
-                return t2 < A.t1;
+                return t2 < A.ntiles;
             };
             auto load8 = [&](uint32_t j0, uint32_t j1, uint32_t (&co)[8], float (&l)[8]) {
 #pragma unroll
@@ -318,8 +316,8 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
                     co[u] = 0xffffffffu;
                     l[u] = 0.f;
                     if (j0 + u < j1) {
-                        co[u] = __ldcs(A.ent_co + j0 + u);
-                        l[u] = __half2float(__ldcs(A.ent_l + j0 + u));
+                        co[u] = __ldg(A.ent_co + j0 + u);
+                        l[u] = __half2float(A.ent_l[j0 + u]);
                     }
                 }
             };
@@ -375,8 +373,8 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
                             co[u] = 0xffffffffu;
                             l[u] = 0.f;
                             if (j + u < d_j1) {
-                                co[u] = __ldcs(A.ent_co + j + u);
-                                l[u] = __half2float(__ldcs(A.ent_l + j + u));
+                                co[u] = __ldg(A.ent_co + j + u);
+                                l[u] = __half2float(A.ent_l[j + u]);
                             }
                         }
 #pragma unroll
@@ -458,29 +456,6 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
     if (warp == 0) tc::tmem_dealloc(tmem, 512);
 }
 
-// fibre pass of slab s (tiles [t_s, t_s+1)): columns in the order of their first entry
-// (q -> c = ford[q]); the running sums continue from acc (slab 0 starts at 0) over the
-// column's terms of the slab, in entry order, so the sums are those of the one-pass
-// k_fibre_sum_entries; the last slab applies eval and writes x
-__global__ void k_fibre_sum_entries_slab(const uint32_t *__restrict__ fslab, const uint32_t *__restrict__ fperm,
-                                         const uint32_t *__restrict__ ford, const float *__restrict__ terms,
-                                         const uint32_t *__restrict__ eval, int64_t ncols, double *__restrict__ acc,
-                                         double *__restrict__ xout, int s, int S) {
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < ncols;
-         q += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t beg = fslab[(size_t)s * ncols + q], end = fslab[(size_t)(s + 1) * ncols + q];
-        if (s > 0 && s < S - 1 && beg == end) continue;
-        double a = s == 0 ? 0.0 : acc[q];
-        a = fibre_gather_sum(fperm, terms, beg, end, a);
-        if (s == S - 1) {
-            const uint32_t c = ford[q];
-            xout[c] = a * (double)eval[c];
-        } else {
-            acc[q] = a;
-        }
-    }
-}
-
 // x[c] = eval[c] * sum of IC column c's terms, gathered in entry order (FP64 sums); the
 // columns in the order of their first entry (ford)
 __global__ void k_fibre_sum_entries(const uint32_t *__restrict__ fptr, const uint32_t *__restrict__ fperm,
@@ -548,43 +523,21 @@ int adjoint_tc(cgb_op *op, int mode, const float *yin, const float *axa, const f
     A.cb = cb;
     A.terms = op->tc_terms;
     A.xout = xout;
+    A.partials = partials;
     A.err = op->tc_err;
+    int g = op->nsm < A.ntiles ? op->nsm : A.ntiles;
+    if (g > reduction_blocks(op)) g = reduction_blocks(op);
+    k_adjoint_tc<<<g, kAThreads, tca_smem_bytes(A.KBS), st>>>(A);
+    CGB_CUDA(cudaGetLastError());
     const int64_t nic = (int64_t)op->nF * op->nIC;
-    int64_t gb = (nic + 255) / 256;
-    if (gb > (int64_t)op->nsm * 16) gb = (int64_t)op->nsm * 16;
-    const int S = op->tc_nslab;
-    if (S <= 1) {
-        A.t0 = 0;
-        A.t1 = A.ntiles;
-        A.partials = partials;
-        int g = op->nsm < A.ntiles ? op->nsm : A.ntiles;
-        if (g > reduction_blocks(op)) g = reduction_blocks(op);
-        k_adjoint_tc<<<g, kAThreads, tca_smem_bytes(A.KBS), st>>>(A);
+    if (nic > 0) {
+        int64_t gb = (nic + 255) / 256;
+        if (gb > (int64_t)op->nsm * 16) gb = (int64_t)op->nsm * 16;
+        k_fibre_sum_entries<<<(int)gb, 256, 0, st>>>(op->tc_fptr, op->tc_fperm, op->tc_ford, op->tc_terms, op->eval,
+                                                      nic, xout);
         CGB_CUDA(cudaGetLastError());
-        if (nic > 0) {
-            k_fibre_sum_entries<<<(int)gb, 256, 0, st>>>(op->tc_fptr, op->tc_fperm, op->tc_ford, op->tc_terms, op->eval,
-                                                          nic, xout);
-            CGB_CUDA(cudaGetLastError());
-        }
-        if (grid) *grid = g;
-        return CGB_OK;
     }
-    // slabs of tiles: each slab's voxel pass, then its fibre pass while its terms are in L2;
-    // one partial-sum block range per slab (S * nsm <= partial_blocks, see ensure_tc)
-    const int g = op->nsm;
-    for (int sl = 0; sl < S; ++sl) {
-        A.t0 = op->tc_slab_t[sl];
-        A.t1 = op->tc_slab_t[sl + 1];
-        A.partials = partials ? partials + (size_t)sl * g * kRedSlots : nullptr;
-        k_adjoint_tc<<<g, kAThreads, tca_smem_bytes(A.KBS), st>>>(A);
-        CGB_CUDA(cudaGetLastError());
-        if (nic > 0) {
-            k_fibre_sum_entries_slab<<<(int)gb, 256, 0, st>>>(op->tc_fslab, op->tc_fperm, op->tc_ford, op->tc_terms,
-                                                               op->eval, nic, op->tc_acc, xout, sl, S);
-            CGB_CUDA(cudaGetLastError());
-        }
-    }
-    if (grid) *grid = g * S;
+    if (grid) *grid = g;
     return CGB_OK;
 }
 

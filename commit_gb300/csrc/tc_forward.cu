@@ -32,9 +32,6 @@
 // written to y, with the residual-norm epilogue of the CUDA-core kernel.
 #include <cub/cub.cuh>
 
-#include <algorithm>
-#include <vector>
-
 #include "operator_launch.cuh"
 #include "tc_ptx.cuh"
 
@@ -91,9 +88,8 @@ struct Window {
             co[i] = 0xffffffffu;
             lv[i] = 0xffffffffu;
             if ((i > 0 || s0 > b0) && j < b1) {
-                // the entry stream is read once: streaming loads keep x and the LUT images in L2
-                co[i] = __ldcs(A.ent_co + j);
-                lv[i] = (uint32_t)__half_as_ushort(__ldcs(A.ent_l + j)) | ((uint32_t)__ldcs(A.ent_vl + j) << 16);
+                co[i] = __ldg(A.ent_co + j);
+                lv[i] = (uint32_t)__half_as_ushort(A.ent_l[j]) | ((uint32_t)A.ent_vl[j] << 16);
             }
         }
     }
@@ -245,9 +241,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_forward_tc(const TcFwdArgs A)
         if (w.co[kWin - 1] != 0xffffffffu && cell_of(w.co[kWin - 1], w.lv[kWin - 1]) == cur) {
             acc += __half2float(__ushort_as_half((unsigned short)(w.lv[kWin - 1] & 0xffffu))) * x[kWin - 1];
             for (j = s0 + kSlice + 1; j < b1; ++j) {
-                const uint32_t co = __ldcs(A.ent_co + j);
-                if (cell_of(co, (uint32_t)__ldcs(A.ent_vl + j) << 16) != cur) break;
-                acc += __half2float(__ldcs(A.ent_l + j)) * __ldg(A.xe + (co & kColMask));
+                const uint32_t co = __ldg(A.ent_co + j);
+                if (cell_of(co, (uint32_t)A.ent_vl[j] << 16) != cur) break;
+                acc += __half2float(A.ent_l[j]) * __ldg(A.xe + (co & kColMask));
             }
         }
         stage[(cur >> 6) * kStageStride + (cur & 63u)] = acc;
@@ -411,9 +407,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_forward_tc(const TcFwdArgs A)
 #pragma unroll
                 for (int i = 0; i < 16; i += 4) {
                     const float4 w = make_float4(r[i], r[i + 1], r[i + 2], r[i + 3]);
-                    // rows are written once and not read back soon: streaming stores
-                    if (A.yout) __stcs(reinterpret_cast<float4 *>(A.yout + idx + i), w);
-                    if (A.axout) __stcs(reinterpret_cast<float4 *>(A.axout + idx + i), w);
+                    if (A.yout) *reinterpret_cast<float4 *>(A.yout + idx + i) = w;
+                    if (A.axout) *reinterpret_cast<float4 *>(A.axout + idx + i) = w;
                 }
             } else if (v < A.nV) {
 #pragma unroll
@@ -543,29 +538,6 @@ __global__ void k_tc_first(const uint32_t *__restrict__ fptr, const uint32_t *__
          q += (int64_t)gridDim.x * blockDim.x) {
         key[q] = fptr[q] < fptr[q + 1] ? fperm[fptr[q]] : nent;
         col[q] = (uint32_t)q;
-    }
-}
-
-// first entry of every tile (and the end of the last)
-__global__ void k_tc_tile_starts(const uint32_t *__restrict__ ptr, int NKB, int ntiles, uint32_t *__restrict__ out) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t <= ntiles) out[t] = ptr[(size_t)t * NKB * kTcTile];
-}
-
-// for the column at fibre-pass position q: where each adjoint slab (entries from pos[s])
-// starts in its ascending entry list
-__global__ void k_tc_fslabs(const uint32_t *__restrict__ fptr, const uint32_t *__restrict__ fperm,
-                            const uint32_t *__restrict__ ford, int64_t ncols, int S, const uint32_t *__restrict__ pos,
-                            uint32_t *__restrict__ fslab) {
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < ncols;
-         q += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t c = ford[q];
-        uint32_t k = fptr[c];
-        const uint32_t end = fptr[c + 1];
-        for (int sl = 0; sl <= S; ++sl) {
-            while (k < end && fperm[k] < pos[sl]) ++k;
-            fslab[(size_t)sl * ncols + q] = k;
-        }
     }
 }
 
@@ -779,53 +751,6 @@ int ensure_tc(cgb_op *op) {
         cu(cudaDeviceSynchronize(), "tensor-core layout");
         cudaFree(fk);
         cudaFree(fc);
-        // adjoint slabs of tiles with about equal entries, each slab's FP32 terms within 40 %
-        // of L2, so its fibre pass gathers from L2; at most 8 slabs, so S * nsm partial sums
-        // fit the reduction buffers (partial_blocks = 8 * nsm at least)
-        int l2 = 0;
-        cu(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, op->device), "cudaDeviceGetAttribute");
-        int S = l2 > 0 ? (int)((double)nent * sizeof(float) / (0.4 * l2) + 0.999) : 1;
-        if (S > 8) S = 8;
-        if (S < 2 || ntiles < 4 * S) S = 1;
-        if (rc == CGB_OK && S > 1) {
-            uint32_t *dts = nullptr, *dpos = nullptr;
-            cu(cudaMalloc((void **)&dts, (size_t)(ntiles + 1) * sizeof(uint32_t)), "cudaMalloc");
-            cu(cudaMalloc((void **)&dpos, (size_t)(S + 1) * sizeof(uint32_t)), "cudaMalloc");
-            std::vector<uint32_t> ts((size_t)ntiles + 1);
-            std::vector<uint32_t> pos((size_t)S + 1);
-            if (rc == CGB_OK) {
-                k_tc_tile_starts<<<(ntiles + 256) / 256, 256>>>(op->tc_ptr, NKB, ntiles, dts);
-                cu(cudaGetLastError(), "k_tc_tile_starts");
-                cu(cudaMemcpy(ts.data(), dts, ts.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost), "cudaMemcpy");
-            }
-            if (rc == CGB_OK) {
-                op->tc_slab_t = new int[S + 1];
-                for (int sl = 0; sl <= S; ++sl) {
-                    const uint64_t target = (uint64_t)nent * sl / S;
-                    int t = sl == S ? ntiles : (int)(std::lower_bound(ts.begin(), ts.end(), (uint32_t)target) - ts.begin());
-                    if (sl > 0 && t < op->tc_slab_t[sl - 1]) t = op->tc_slab_t[sl - 1];
-                    op->tc_slab_t[sl] = t;
-                    pos[sl] = ts[t];
-                }
-                cu(cudaMemcpy(dpos, pos.data(), pos.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "cudaMemcpy");
-                cu(cudaMalloc((void **)&op->tc_fslab, (size_t)(S + 1) * nic_cols * sizeof(uint32_t)), "cudaMalloc");
-                cu(cudaMalloc((void **)&op->tc_acc, (size_t)nic_cols * sizeof(double)), "cudaMalloc");
-            }
-            if (rc == CGB_OK) {
-                k_tc_fslabs<<<grid_of(nic_cols, op->nsm), 256>>>(op->tc_fptr, op->tc_fperm, op->tc_ford, nic_cols, S,
-                                                                 dpos, op->tc_fslab);
-                cu(cudaGetLastError(), "k_tc_fslabs");
-                cu(cudaDeviceSynchronize(), "tensor-core layout");
-            }
-            cudaFree(dts);
-            cudaFree(dpos);
-            if (rc == CGB_OK) {
-                op->tc_nslab = S;
-                op->bytes += (size_t)(S + 1) * nic_cols * 4 + (size_t)nic_cols * 8;
-            }
-        } else {
-            op->tc_nslab = 1;
-        }
         cu(cudaMalloc((void **)&op->tc_abimg, (size_t)R * KBS * 2 * 128 * 64 * sizeof(__nv_bfloat16)), "cudaMalloc");
         if (rc == CGB_OK) {
             k_tca_bimg<<<grid_of((int64_t)R * KBS * 2 * 128 * 64, op->nsm), 256>>>(P, R, KBS, NKB, nkbd,

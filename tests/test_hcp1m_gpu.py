@@ -87,8 +87,8 @@ def test_reduced_precision_matches_reference(hcp, arith):
 
 def test_tensor_cores_at_full_workload(hcp):
     """The tensor-core BF16 operator at 1M streamlines (the default there: 212 IC segments per
-    voxel; its adjoint runs in slabs of tiles whose fibre passes gather from L2) against the
-    CUDA-core BF16 kernels on the same BF16 LUT (1e-4), bitwise repeatable."""
+    voxel) against the CUDA-core BF16 kernels on the same BF16 LUT (1e-4), bitwise
+    repeatable."""
     from commit_gb300.operator import LinearOperator
     A = LinearOperator(hcp['D'], hcp['K'], None)
     x = torch.from_numpy(hcp['x']).cuda().float()
