@@ -48,7 +48,6 @@ struct TcAdjArgs {
     const __nv_bfloat16 *rows16;  // EC rows (nEC * ndirs) then ISO rows (nISO), BF16, stride Np
     const uint32_t *ent_ptr, *ent_co;
     const __half *ent_l;
-    const uint8_t *ent_vl;  // voxel of each entry within its tile
     float l_scale;
     const __nv_bfloat16 *bimg;  // [R][KBS][2][128 x 64] swizzled
     int mode;                   // 0: z = yin; 2: r = sqw*(ca*axa + cb*axb - yobs), z = sqw*r, |r|^2 partials
@@ -109,22 +108,6 @@ __device__ __forceinline__ void z_dot_rows4(const uint8_t *a_hi, const uint8_t *
     }
 }
 
-// named barrier 1 over the 128 threads of warps 0-3 (the drain); every drain thread calls
-// each of these the same number of times, in the same order
-__device__ __forceinline__ void drain_bar_sync() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
-__device__ __forceinline__ bool drain_bar_or(int v) {
-    uint32_t out;
-    asm volatile(
-        "{\n\t.reg .pred p, q;\n\t"
-        "setp.ne.s32 p, %1, 0;\n\t"
-        "bar.red.or.pred q, 1, 128, p;\n\t"
-        "selp.u32 %0, 1, 0, q;\n\t}"
-        : "=r"(out)
-        : "r"(v)
-        : "memory");
-    return out != 0;
-}
-
 __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
@@ -163,7 +146,8 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
     // drain state (warps 0-3): rounds drained so far, entry pipeline (see (3))
     uint32_t rgd = 0;
     uint32_t d_j0 = 0, d_j1 = 0, d_n0 = 0, d_n1 = 0;
-    uint32_t d_co[8], d_l[8];  // column | row, FP16 length | voxel << 16
+    uint32_t d_co[8];
+    float d_l[8];
     bool d_primed = false;
     int bad = 0;
     double nrm = 0.0;
@@ -306,19 +290,16 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
                 rgi += (uint32_t)A.R;
             }
         } else if (warp < 4) {
-            // (3) drain, warps 0-3 (128 threads): each thread copies a K-block's 64 columns of
-            // its voxel (its TMEM lane) into its shared-memory row; then the 128 threads share
-            // the K-block's entries of the tile (thread t: entries b0 + t + 128 i, so loads and
-            // term stores are coalesced and no voxel's count holds the others up), each entry
-            // reading its voxel's row.  Entry pipeline (carried across tiles): the K-block's
-            // first 8 entries per thread were loaded during the previous K-block, the next
-            // one's start loading now, with the offsets of the one after it.
-            const int dt = tid;  // 0..127
-            float *row = dstage + dt * kADrainStride;
+            // (3) drain: each thread is one voxel (TMEM lane); items of the round's LUT rows.
+            // Entry pipeline (carried across tiles): at the start of a K-block the first 8 of
+            // its entries are in registers, the next K-block's first 8 start loading and the
+            // offsets of the one after that too.
+            const int vloc = warp * 32 + lane;
+            float *row = dstage + (warp * 32 + lane) * kADrainStride;
             auto range_of = [&](int t, int k, uint32_t &b0, uint32_t &b1) {
-                const size_t pb = ((size_t)t * A.NKB + k) * kATile;
+                const size_t pb = ((size_t)t * A.NKB + k) * kATile + vloc;
                 b0 = A.ent_ptr[pb];
-                b1 = A.ent_ptr[pb + kATile];
+                b1 = A.ent_ptr[pb + 1];
             };
             auto after = [&](int t, int k, int ahead, int &t2, int &k2) {
                 k2 = k + ahead;
@@ -329,29 +310,15 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
                 }
                 return t2 < A.ntiles;
             };
-            auto load8 = [&](uint32_t base, uint32_t b1, uint32_t (&co)[8], uint32_t (&lv)[8]) {
+            auto load8 = [&](uint32_t j0, uint32_t j1, uint32_t (&co)[8], float (&l)[8]) {
 #pragma unroll
                 for (int u = 0; u < 8; ++u) {
-                    const uint32_t j = base + (uint32_t)dt + (uint32_t)(u * kATile);
                     co[u] = 0xffffffffu;
-                    lv[u] = 0u;
-                    if (j < b1) {
-                        co[u] = __ldg(A.ent_co + j);
-                        lv[u] = (uint32_t)__half_as_ushort(A.ent_l[j]) | ((uint32_t)A.ent_vl[j] << 16);
+                    l[u] = 0.f;
+                    if (j0 + u < j1) {
+                        co[u] = __ldg(A.ent_co + j0 + u);
+                        l[u] = __half2float(A.ent_l[j0 + u]);
                     }
-                }
-            };
-            const float lsc = A.l_scale;
-            // terms of 8 entries (base + dt + 128 u) from the rows
-            auto emit8 = [&](uint32_t base, uint32_t b1, const uint32_t (&co)[8], const uint32_t (&lv)[8]) {
-#pragma unroll
-                for (int u = 0; u < 8; ++u) {
-                    const uint32_t j = base + (uint32_t)dt + (uint32_t)(u * kATile);
-                    const uint32_t o = co[u] >> kAColBits, vl = lv[u] >> 16;
-                    // o < 64 and vl < 128 always hold for the layout's entries
-                    if (j < b1 && o < 64u && vl < (uint32_t)kATile)
-                        A.terms[j] = dstage[vl * kADrainStride + o] *
-                                     (__half2float(__ushort_as_half((unsigned short)(lv[u] & 0xffffu))) * lsc);
                 }
             };
             if (!d_primed) {
@@ -362,25 +329,26 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
                 if (after(tile, 0, 1, t1, k1)) range_of(t1, k1, d_n0, d_n1);
                 d_primed = true;
             }
+            const float lsc = A.l_scale;
             for (int r = 0; r < A.R; ++r) {
                 const uint32_t rg = rgd + (uint32_t)r;
                 if (!bad && !tc::mbar_wait(&gfull[rg & 1u], (rg >> 1) & 1u)) {
                     bad = 1;
                     atomicExch(A.err, 12);
                 }
-                // one decision for the 128 drain threads (they meet at named barriers below)
-                if (drain_bar_or(bad)) break;
+                if (__any_sync(0xffffffffu, bad)) break;
                 tc::tc_fence_after();
                 for (int kbl = 0; kbl < kARows / 64; ++kbl) {
                     const int kbf = r * (kARows / 64) + kbl;
                     if (kbf >= A.NKB) break;
                     // next K-block's first entries and the offsets of the one after it
-                    uint32_t nco[8], nlv[8];
-                    load8(d_n0, d_n1, nco, nlv);
+                    uint32_t nco[8];
+                    float nl[8];
+                    load8(d_n0, d_n1, nco, nl);
                     int t2, k2;
                     uint32_t q0 = 0, q1 = 0;
                     if (after(tile, kbf, 2, t2, k2)) range_of(t2, k2, q0, q1);
-                    // this voxel's 64 columns into its row, then all rows are complete
+                    // the K-block's 64 columns of this voxel into its private row
                     __syncwarp();
 #pragma unroll
                     for (int c = 0; c < 2; ++c) {
@@ -390,19 +358,36 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
 #pragma unroll
                         for (int i = 0; i < 32; ++i) row[c * 32 + i] = g[i];
                     }
-                    drain_bar_sync();
-                    emit8(d_j0, d_j1, d_co, d_l);
-                    for (uint32_t base = d_j0 + 8u * kATile; base < d_j1; base += 8u * kATile) {
-                        uint32_t co[8], lv[8];
-                        load8(base, d_j1, co, lv);
-                        emit8(base, d_j1, co, lv);
+                    // the first 8 entries from registers, the rest four at a time
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const uint32_t o = d_co[u] >> kAColBits;
+                        // o < 64 always holds for the layout's entries; never indexes outside the row
+                        if (d_j0 + u < d_j1 && o < 64u) A.terms[d_j0 + u] = row[o] * (d_l[u] * lsc);
                     }
-                    drain_bar_sync();  // the rows are read; the next K-block may overwrite them
+                    for (uint32_t j = d_j0 + 8; j < d_j1; j += 4) {
+                        uint32_t co[4];
+                        float l[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            co[u] = 0xffffffffu;
+                            l[u] = 0.f;
+                            if (j + u < d_j1) {
+                                co[u] = __ldg(A.ent_co + j + u);
+                                l[u] = __half2float(A.ent_l[j + u]);
+                            }
+                        }
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const uint32_t o = co[u] >> kAColBits;
+                            if (j + u < d_j1 && o < 64u) A.terms[j + u] = row[o] * (l[u] * lsc);
+                        }
+                    }
                     // shift the pipeline
 #pragma unroll
                     for (int u = 0; u < 8; ++u) {
                         d_co[u] = nco[u];
-                        d_l[u] = nlv[u];
+                        d_l[u] = nl[u];
                     }
                     d_j0 = d_n0;
                     d_j1 = d_n1;
@@ -526,7 +511,6 @@ int adjoint_tc(cgb_op *op, int mode, const float *yin, const float *axa, const f
     A.ent_ptr = op->tc_ptr;
     A.ent_co = op->tc_co;
     A.ent_l = op->tc_l;
-    A.ent_vl = op->tc_vl;
     A.l_scale = op->tc_lscale;
     A.bimg = op->tc_abimg;
     A.mode = mode;
