@@ -178,7 +178,9 @@ struct cgb_op {
     int *tc_err;                    // device status word of the bounded waits
     int tc_kbs, tc_rounds;          // adjoint: sample K-blocks of 64, rounds of 256 LUT rows
     int64_t tc_nent;                // entries
-    uint32_t *tc_fptr, *tc_fperm;   // adjoint: IC entry positions grouped by column, CSR offsets
+    uint32_t *tc_fptr, *tc_fperm;   // adjoint: CSR offsets per IC column; entry positions grouped by column
+                                    // (layout only)
+    uint32_t *tc_fpos;              // adjoint: column-sorted position of every IC entry (where its term goes)
     uint32_t *tc_ford;              // adjoint: IC columns by their first entry position (fibre-pass order)
     __nv_bfloat16 *tc_abimg;        // adjoint LUT images
     float *tc_terms;                // adjoint IC terms in entry order

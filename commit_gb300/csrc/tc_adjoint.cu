@@ -48,6 +48,7 @@ struct TcAdjArgs {
     const __nv_bfloat16 *rows16;  // EC rows (nEC * ndirs) then ISO rows (nISO), BF16, stride Np
     const uint32_t *ent_ptr, *ent_co;
     const __half *ent_l;
+    const uint32_t *ent_fpos;  // column-sorted position of each entry's term
     float l_scale;
     const __nv_bfloat16 *bimg;  // [R][KBS][2][128 x 64] swizzled
     int mode;                   // 0: z = yin; 2: r = sqw*(ca*axa + cb*axb - yobs), z = sqw*r, |r|^2 partials
@@ -146,7 +147,7 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
     // drain state (warps 0-3): rounds drained so far, entry pipeline (see (3))
     uint32_t rgd = 0;
     uint32_t d_j0 = 0, d_j1 = 0, d_n0 = 0, d_n1 = 0;
-    uint32_t d_co[8];
+    uint32_t d_co[8], d_fp[8];
     float d_l[8];
     bool d_primed = false;
     int bad = 0;
@@ -310,21 +311,23 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
                 }
                 return t2 < A.ntiles;
             };
-            auto load8 = [&](uint32_t j0, uint32_t j1, uint32_t (&co)[8], float (&l)[8]) {
+            auto load8 = [&](uint32_t j0, uint32_t j1, uint32_t (&co)[8], float (&l)[8], uint32_t (&fp)[8]) {
 #pragma unroll
                 for (int u = 0; u < 8; ++u) {
                     co[u] = 0xffffffffu;
                     l[u] = 0.f;
+                    fp[u] = 0u;
                     if (j0 + u < j1) {
                         co[u] = __ldg(A.ent_co + j0 + u);
                         l[u] = __half2float(A.ent_l[j0 + u]);
+                        fp[u] = __ldg(A.ent_fpos + j0 + u);
                     }
                 }
             };
             if (!d_primed) {
                 int t1, k1;
                 range_of(tile, 0, d_j0, d_j1);
-                load8(d_j0, d_j1, d_co, d_l);
+                load8(d_j0, d_j1, d_co, d_l, d_fp);
                 d_n0 = d_n1 = 0;
                 if (after(tile, 0, 1, t1, k1)) range_of(t1, k1, d_n0, d_n1);
                 d_primed = true;
@@ -342,9 +345,9 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
                     const int kbf = r * (kARows / 64) + kbl;
                     if (kbf >= A.NKB) break;
                     // next K-block's first entries and the offsets of the one after it
-                    uint32_t nco[8];
+                    uint32_t nco[8], nfp[8];
                     float nl[8];
-                    load8(d_n0, d_n1, nco, nl);
+                    load8(d_n0, d_n1, nco, nl, nfp);
                     int t2, k2;
                     uint32_t q0 = 0, q1 = 0;
                     if (after(tile, kbf, 2, t2, k2)) range_of(t2, k2, q0, q1);
@@ -363,24 +366,26 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
                     for (int u = 0; u < 8; ++u) {
                         const uint32_t o = d_co[u] >> kAColBits;
                         // o < 64 always holds for the layout's entries; never indexes outside the row
-                        if (d_j0 + u < d_j1 && o < 64u) A.terms[d_j0 + u] = row[o] * (d_l[u] * lsc);
+                        if (d_j0 + u < d_j1 && o < 64u) A.terms[d_fp[u]] = row[o] * (d_l[u] * lsc);
                     }
                     for (uint32_t j = d_j0 + 8; j < d_j1; j += 4) {
-                        uint32_t co[4];
+                        uint32_t co[4], fp[4];
                         float l[4];
 #pragma unroll
                         for (int u = 0; u < 4; ++u) {
                             co[u] = 0xffffffffu;
                             l[u] = 0.f;
+                            fp[u] = 0u;
                             if (j + u < d_j1) {
                                 co[u] = __ldg(A.ent_co + j + u);
                                 l[u] = __half2float(A.ent_l[j + u]);
+                                fp[u] = __ldg(A.ent_fpos + j + u);
                             }
                         }
 #pragma unroll
                         for (int u = 0; u < 4; ++u) {
                             const uint32_t o = co[u] >> kAColBits;
-                            if (j + u < d_j1 && o < 64u) A.terms[j + u] = row[o] * (l[u] * lsc);
+                            if (j + u < d_j1 && o < 64u) A.terms[fp[u]] = row[o] * (l[u] * lsc);
                         }
                     }
                     // shift the pipeline
@@ -388,6 +393,7 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
                     for (int u = 0; u < 8; ++u) {
                         d_co[u] = nco[u];
                         d_l[u] = nl[u];
+                        d_fp[u] = nfp[u];
                     }
                     d_j0 = d_n0;
                     d_j1 = d_n1;
@@ -456,15 +462,25 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
     if (warp == 0) tc::tmem_dealloc(tmem, 512);
 }
 
-// x[c] = eval[c] * sum of IC column c's terms, gathered in entry order (FP64 sums); the
-// columns in the order of their first entry (ford)
-__global__ void k_fibre_sum_entries(const uint32_t *__restrict__ fptr, const uint32_t *__restrict__ fperm,
-                                    const uint32_t *__restrict__ ford, const float *__restrict__ terms,
-                                    const uint32_t *__restrict__ eval, int64_t ncols, double *__restrict__ xout) {
+// x[c] = eval[c] * sum of IC column c's terms (stored contiguously, in entry order, at
+// [fptr[c], fptr[c + 1])), FP64 sums; the columns in the order of their first entry (ford)
+__global__ void k_fibre_sum_entries(const uint32_t *__restrict__ fptr, const uint32_t *__restrict__ ford,
+                                    const float *__restrict__ terms, const uint32_t *__restrict__ eval, int64_t ncols,
+                                    double *__restrict__ xout) {
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < ncols;
          q += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t c = ford[q];
-        const double s = fibre_gather_sum(fperm, terms, fptr[c], fptr[c + 1], 0.0);
+        const uint32_t e = fptr[c + 1];
+        uint32_t k = fptr[c];
+        double s = 0.0;
+        for (; k + 8 <= e; k += 8) {
+            float t[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) t[u] = __ldg(terms + k + u);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) s += (double)t[u];
+        }
+        for (; k < e; ++k) s += (double)__ldg(terms + k);
         xout[c] = s * (double)eval[c];
     }
 }
@@ -511,6 +527,7 @@ int adjoint_tc(cgb_op *op, int mode, const float *yin, const float *axa, const f
     A.ent_ptr = op->tc_ptr;
     A.ent_co = op->tc_co;
     A.ent_l = op->tc_l;
+    A.ent_fpos = op->tc_fpos;
     A.l_scale = op->tc_lscale;
     A.bimg = op->tc_abimg;
     A.mode = mode;
@@ -533,8 +550,7 @@ int adjoint_tc(cgb_op *op, int mode, const float *yin, const float *axa, const f
     if (nic > 0) {
         int64_t gb = (nic + 255) / 256;
         if (gb > (int64_t)op->nsm * 16) gb = (int64_t)op->nsm * 16;
-        k_fibre_sum_entries<<<(int)gb, 256, 0, st>>>(op->tc_fptr, op->tc_fperm, op->tc_ford, op->tc_terms, op->eval,
-                                                      nic, xout);
+        k_fibre_sum_entries<<<(int)gb, 256, 0, st>>>(op->tc_fptr, op->tc_ford, op->tc_terms, op->eval, nic, xout);
         CGB_CUDA(cudaGetLastError());
     }
     if (grid) *grid = g;

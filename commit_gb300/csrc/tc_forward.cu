@@ -541,6 +541,12 @@ __global__ void k_tc_first(const uint32_t *__restrict__ fptr, const uint32_t *__
     }
 }
 
+// fpos = the inverse of fperm: the column-sorted position of every entry
+__global__ void k_tc_inverse(const uint32_t *__restrict__ fperm, int64_t n, uint32_t *__restrict__ fpos) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+        fpos[fperm[k]] = (uint32_t)k;
+}
+
 __global__ void k_tc_count(const uint32_t *__restrict__ ckey, int64_t n, uint32_t *__restrict__ count) {
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
         atomicAdd(count + ckey[q], 1u);
@@ -751,6 +757,16 @@ int ensure_tc(cgb_op *op) {
         cu(cudaDeviceSynchronize(), "tensor-core layout");
         cudaFree(fk);
         cudaFree(fc);
+        // the adjoint writes each term at its column-sorted position (fpos), so the fibre
+        // pass reads every column's terms contiguously; fperm is not needed after this
+        cu(cudaMalloc((void **)&op->tc_fpos, (size_t)nent * sizeof(uint32_t)), "cudaMalloc");
+        if (rc == CGB_OK) {
+            k_tc_inverse<<<grid_of(nent, op->nsm), 256>>>(op->tc_fperm, nent, op->tc_fpos);
+            cu(cudaGetLastError(), "k_tc_inverse");
+            cu(cudaDeviceSynchronize(), "tensor-core layout");
+        }
+        cudaFree(op->tc_fperm);
+        op->tc_fperm = nullptr;
         cu(cudaMalloc((void **)&op->tc_abimg, (size_t)R * KBS * 2 * 128 * 64 * sizeof(__nv_bfloat16)), "cudaMalloc");
         if (rc == CGB_OK) {
             k_tca_bimg<<<grid_of((int64_t)R * KBS * 2 * 128 * 64, op->nsm), 256>>>(P, R, KBS, NKB, nkbd,
