@@ -463,17 +463,13 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
 }
 
 // x[c] = eval[c] * sum of IC column c's terms (stored contiguously at [fptr[c], fptr[c+1])),
-// one warp per column, each warp over a contiguous run of columns (so it streams through
-// one region of the term array): lane l sums terms l, l + 32, ... in FP64, then a fixed
-// butterfly adds the lanes (deterministic); coalesced 128-byte loads
+// one warp per column: lane l sums terms l, l + 32, ... in FP64, then a fixed butterfly adds
+// the lanes (deterministic); coalesced 128-byte loads
 __global__ void k_fibre_sum_entries(const uint32_t *__restrict__ fptr, const float *__restrict__ terms,
                                     const uint32_t *__restrict__ eval, int64_t ncols, double *__restrict__ xout) {
     const int lane = threadIdx.x & 31;
     const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
-    const int64_t w = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
-    const int64_t per = (ncols + nw - 1) / nw;
-    const int64_t c0 = w * per, c1 = c0 + per < ncols ? c0 + per : ncols;
-    for (int64_t c = c0; c < c1; ++c) {
+    for (int64_t c = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); c < ncols; c += nw) {
         const uint32_t b = fptr[c], e = fptr[c + 1];
         double s = 0.0;
         uint32_t k = b + (uint32_t)lane;
