@@ -181,6 +181,7 @@ struct cgb_op {
     uint32_t *tc_fptr, *tc_fperm;   // adjoint: CSR offsets per IC column; entry positions grouped by column
                                     // (layout only)
     uint32_t *tc_fpos;              // adjoint: column-sorted position of every IC entry (where its term goes)
+    uint32_t *tc_ford;              // adjoint: IC columns by their first entry position (fibre-pass order)
     __nv_bfloat16 *tc_abimg;        // adjoint LUT images
     float *tc_terms;                // adjoint IC terms in entry order
     float *tc_ax;                   // A x rows for the gradient (FISTA), on demand

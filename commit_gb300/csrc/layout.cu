@@ -296,7 +296,7 @@ static void free_op(cgb_op *op) {
                     op->iso_col, op->seg_o, op->ec_o, op->seg_l, op->scratch, op->scratch32, op->partials,
                     op->dscal, op->d_in, op->d_out, op->d_x64, op->fib_slab, op->fib_acc, op->d_xmax,
                     op->tc_ptr, op->tc_co, op->tc_l, op->tc_vl, op->tc_bimg, op->tc_xe, op->tc_err,
-                    op->tc_fptr, op->tc_fperm, op->tc_abimg, op->tc_terms, op->tc_ax, op->tc_rows16, op->tc_fpos};
+                    op->tc_fptr, op->tc_fperm, op->tc_abimg, op->tc_terms, op->tc_ax, op->tc_rows16, op->tc_ford, op->tc_fpos};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (op->h_scal) cudaFreeHost(op->h_scal);

@@ -462,29 +462,26 @@ __global__ void __launch_bounds__(kAThreads, 1) k_adjoint_tc(const TcAdjArgs A) 
     if (warp == 0) tc::tmem_dealloc(tmem, 512);
 }
 
-// x[c] = eval[c] * sum of IC column c's terms (stored contiguously at [fptr[c], fptr[c+1])),
-// one warp per column: lane l sums terms l, l + 32, ... in FP64, then a fixed butterfly adds
-// the lanes (deterministic); coalesced 128-byte loads
-__global__ void k_fibre_sum_entries(const uint32_t *__restrict__ fptr, const float *__restrict__ terms,
-                                    const uint32_t *__restrict__ eval, int64_t ncols, double *__restrict__ xout) {
-    const int lane = threadIdx.x & 31;
-    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t c = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); c < ncols; c += nw) {
-        const uint32_t b = fptr[c], e = fptr[c + 1];
+// x[c] = eval[c] * sum of IC column c's terms (stored contiguously, in entry order, at
+// [fptr[c], fptr[c + 1])), FP64 sums; the columns in the order of their first entry (ford)
+__global__ void k_fibre_sum_entries(const uint32_t *__restrict__ fptr, const uint32_t *__restrict__ ford,
+                                    const float *__restrict__ terms, const uint32_t *__restrict__ eval, int64_t ncols,
+                                    double *__restrict__ xout) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < ncols;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t c = ford[q];
+        const uint32_t e = fptr[c + 1];
+        uint32_t k = fptr[c];
         double s = 0.0;
-        uint32_t k = b + (uint32_t)lane;
-        for (; k + 96 < e; k += 128) {
-            const float t0 = __ldg(terms + k), t1 = __ldg(terms + k + 32), t2 = __ldg(terms + k + 64),
-                        t3 = __ldg(terms + k + 96);
-            s += (double)t0;
-            s += (double)t1;
-            s += (double)t2;
-            s += (double)t3;
-        }
-        for (; k < e; k += 32) s += (double)__ldg(terms + k);
+        for (; k + 8 <= e; k += 8) {
+            float t[8];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) xout[c] = s * (double)eval[c];
+            for (int u = 0; u < 8; ++u) t[u] = __ldg(terms + k + u);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) s += (double)t[u];
+        }
+        for (; k < e; ++k) s += (double)__ldg(terms + k);
+        xout[c] = s * (double)eval[c];
     }
 }
 
@@ -551,9 +548,9 @@ int adjoint_tc(cgb_op *op, int mode, const float *yin, const float *axa, const f
     CGB_CUDA(cudaGetLastError());
     const int64_t nic = (int64_t)op->nF * op->nIC;
     if (nic > 0) {
-        int64_t gw = (nic + 7) / 8;  // 8 warps (columns) per block
-        if (gw > (int64_t)op->nsm * 32) gw = (int64_t)op->nsm * 32;
-        k_fibre_sum_entries<<<(int)gw, 256, 0, st>>>(op->tc_fptr, op->tc_terms, op->eval, nic, xout);
+        int64_t gb = (nic + 255) / 256;
+        if (gb > (int64_t)op->nsm * 16) gb = (int64_t)op->nsm * 16;
+        k_fibre_sum_entries<<<(int)gb, 256, 0, st>>>(op->tc_fptr, op->tc_ford, op->tc_terms, op->eval, nic, xout);
         CGB_CUDA(cudaGetLastError());
     }
     if (grid) *grid = g;

@@ -530,6 +530,17 @@ __global__ void k_tc_fib_keys(const uint32_t *__restrict__ co, int64_t n, uint32
     }
 }
 
+// IC columns keyed by the entry position of their first term (nent without terms), for the
+// fibre pass order
+__global__ void k_tc_first(const uint32_t *__restrict__ fptr, const uint32_t *__restrict__ fperm, int64_t ncols,
+                           uint32_t nent, uint32_t *__restrict__ key, uint32_t *__restrict__ col) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < ncols;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        key[q] = fptr[q] < fptr[q + 1] ? fperm[fptr[q]] : nent;
+        col[q] = (uint32_t)q;
+    }
+}
+
 // fpos = the inverse of fperm: the column-sorted position of every entry
 __global__ void k_tc_inverse(const uint32_t *__restrict__ fperm, int64_t n, uint32_t *__restrict__ fpos) {
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
@@ -719,6 +730,33 @@ int ensure_tc(cgb_op *op) {
             cu(cudaMalloc(&tmp, tmp_bytes), "cudaMalloc");
         }
         cu(cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, count, op->tc_fptr, nic_cols + 1), "cub scan");
+        // columns in the order of their first entry: neighbouring threads of the fibre pass
+        // gather neighbouring terms
+        uint32_t *fk = nullptr, *fk2 = nullptr, *fc = nullptr;
+        cu(cudaMalloc((void **)&fk, nic_cols * 2 * sizeof(uint32_t)), "cudaMalloc");
+        cu(cudaMalloc((void **)&fc, nic_cols * sizeof(uint32_t)), "cudaMalloc");
+        cu(cudaMalloc((void **)&op->tc_ford, nic_cols * sizeof(uint32_t)), "cudaMalloc");
+        if (rc == CGB_OK) {
+            fk2 = fk + nic_cols;
+            k_tc_first<<<grid_of(nic_cols, op->nsm), 256>>>(op->tc_fptr, op->tc_fperm, nic_cols, (uint32_t)nent, fk, fc);
+            cu(cudaGetLastError(), "k_tc_first");
+            int ebits = 1;
+            while (ebits < 32 && (((uint64_t)nent) >> ebits) != 0) ++ebits;
+            size_t fneed = 0;
+            cu(cub::DeviceRadixSort::SortPairs(nullptr, fneed, fk, fk2, fc, op->tc_ford, nic_cols, 0, ebits),
+               "cub sort");
+            if (fneed > tmp_bytes) {
+                cudaFree(tmp);
+                tmp = nullptr;
+                tmp_bytes = fneed;
+                cu(cudaMalloc(&tmp, tmp_bytes), "cudaMalloc");
+            }
+            cu(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, fk, fk2, fc, op->tc_ford, nic_cols, 0, ebits),
+               "cub sort");
+        }
+        cu(cudaDeviceSynchronize(), "tensor-core layout");
+        cudaFree(fk);
+        cudaFree(fc);
         // the adjoint writes each term at its column-sorted position (fpos), so the fibre
         // pass reads every column's terms contiguously; fperm is not needed after this
         cu(cudaMalloc((void **)&op->tc_fpos, (size_t)nent * sizeof(uint32_t)), "cudaMalloc");
@@ -753,7 +791,7 @@ int ensure_tc(cgb_op *op) {
     op->tc_rounds = R;
     op->tc_nent = nent;
     op->bytes += nent * 7 + (nkeys + 1) * 4 + (size_t)NKB * Np * kTcKB * 2 + (size_t)op->ncols * 4 + nent * 8 +
-                 (size_t)(nic_cols + 1) * 4 + (size_t)R * KBS * 2 * 128 * 64 * 2 +
+                 (size_t)(nic_cols + 1) * 4 + (size_t)nic_cols * 4 + (size_t)R * KBS * 2 * 128 * 64 * 2 +
                  (size_t)(nec_rows + niso_rows) * Np * 2;
     op->tc_ready = 1;
     return CGB_OK;
