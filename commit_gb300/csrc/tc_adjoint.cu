@@ -9,10 +9,9 @@
 // in shared memory (K-major, 64 samples per K-block), and multiplies them with the BF16
 // LUT rows, 256 rows per round, into one half of tensor memory while the previous round's
 // half is read back: for each IC item of the round's rows the drain warps form l * G[v, k]
-// and write it to a term array in entry order (the tile-ordered entry stream of
-// tc_forward.cu).  The IC columns are then the sums of their terms, gathered per fibre in
-// entry order through an entry-order fibre index (deterministic, FP64 sums, as the
-// CUDA-core path).  The EC and ISO items (one or two per voxel) are dot products of the
+// and write it to the term array at the item's column-sorted position (fpos: the items of
+// a column are contiguous there, in entry order).  The IC columns are then the sums of
+// their contiguous terms (deterministic, FP64 sums, as the CUDA-core path).  The EC and ISO items (one or two per voxel) are dot products of the
 // same BF16 rows of z with their BF16 LUT rows on the CUDA cores, written straight to
 // their column of x.
 //
