@@ -222,7 +222,7 @@ class LinearOperator:
 
     def tensor_cores(self, mode: int | None = None) -> bool:
         """Reduced-precision BF16 A*x and A'*y on the tensor cores: mode 0 (default) when the
-        shape allows it and the operator has at least 64 IC segments per voxel, 1 CUDA cores
+        shape allows it and the operator has at least 32 IC segments per voxel, 1 CUDA cores
         only, 2 required; None only reads.  Returns whether it is in use."""
         out = ctypes.c_int32()
         check(lib().cgb_op_tensor_cores(self._h.ptr, -1 if mode is None else int(mode), ctypes.byref(out)))

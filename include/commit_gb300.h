@@ -216,9 +216,9 @@ int cgb_op_adjoint_noalloc(int nS, int ndirs, int nF, int64_t n, int nE, int nV,
  * of the input rows (A') with the BF16 LUT, FP32 accumulation in tensor memory; the EC and
  * ISO items run on the CUDA cores in the same kernels.  mode 0 (the default) uses it when
  * the shape allows it (an IC compartment, nS <= 320, fewer than 2^26 columns) and the IC
- * segments are dense enough for the dense product to pay, at least 64 per voxel on
- * average (measured on GB300: at 212 per voxel it is 1.65x faster than the CUDA-core
- * kernels, at 21 per voxel slower); 1 keeps the CUDA-core kernels; 2 requires it
+ * segments are dense enough for the dense product to pay, at least 32 per voxel on
+ * average (measured on GB300: 1.5x faster than the CUDA-core kernels at 62 per voxel,
+ * 1.9x at 212, slower at 21); 1 keeps the CUDA-core kernels; 2 requires it
  * (CGB_ERR_UNSUPPORTED when the shape does not allow it); a negative mode only reads.
  * *out (may be NULL) receives 1 when the tensor-core kernels are in use.  The first use on
  * a handle builds its tile-ordered entry stream and LUT images (about 6 bytes per
