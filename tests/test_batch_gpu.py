@@ -30,6 +30,7 @@ def test_dot_batch_matches_single_vector(nvec, width):
     from commit_gb300.operator import LinearOperator
     D, K, P, _ = _demo()
     A = LinearOperator(D, K, None)
+    A.tensor_cores(1)  # the batched passes are CUDA-core BF16: compare with the same single-vector kernels
     A.batch_width(width)
     rng = np.random.default_rng(nvec)
     xs32 = [torch.from_numpy(rng.uniform(0, 1, P.nCOLS).astype(np.float32)).cuda() for _ in range(nvec)]
@@ -79,6 +80,7 @@ def test_batched_path_tracks_sequential_solves(reuse):
     from commit_gb300.operator import LinearOperator
     D, K, P, y = _demo()
     A = LinearOperator(D, K, None)
+    A.tensor_cores(1)  # the batched passes are CUDA-core BF16: compare with the same single-vector kernels
     fracs = [1e-4, 1e-3, 3e-3, 1e-2, 3e-2]   # 5 problems: a 4-vector pass and a single one
     regs = _path_regs(A, D, K, y, fracs)
     out = solvers.solve_batch(y, A, regs, tol_fun=1e-5, tol_x=1e-7, max_iter=150, momentum_reuse=reuse)
@@ -187,6 +189,7 @@ def test_batch_voxel_shapes_agree(shape):
     from commit_gb300.operator import LinearOperator
     D, K, P, y = _demo('demo_5k', n_b0=18, shells=[(1000.0, 90), (2000.0, 90), (3000.0, 90)], n_fibers=2000)
     A = LinearOperator(D, K, None)
+    A.tensor_cores(1)  # the batched passes are CUDA-core BF16: compare with the same single-vector kernels
     A.batch_width(4)
     A.batch_shape(shape)
     rng = np.random.default_rng(8)
@@ -213,6 +216,7 @@ def test_batch_single_and_three_problems():
     from commit_gb300.operator import LinearOperator
     D, K, P, y = _demo()
     A = LinearOperator(D, K, None)
+    A.tensor_cores(1)  # the batched passes are CUDA-core BF16: compare with the same single-vector kernels
     A.batch_width(4)
     for fr in ([1e-3], [1e-4, 1e-3, 1e-2]):
         regs = _path_regs(A, D, K, y, fr)
