@@ -318,9 +318,10 @@ def solve_mixed(y, A, tol_fun=1e-4, tol_x=1e-6, max_iter=1000, verbose=0, x0=Non
 
     Phase 1 runs FISTA with the operator in ``arith`` ('bf16', 'fp16' or 'f32': LUT in
     that format, FP16 lengths, FP32 accumulation; FISTA vectors, the Lipschitz estimate
-    and every objective / stopping reduction in FP64).  The default is FP16: as fast as BF16
-    on GB300 (65 vs 69 operator pairs/s at 1M streamlines) with a tenth of its error
-    (solution within 4e-4 instead of 4e-3 of the FP64 one on the demo case).  Phase 2 restarts the plain FP64
+    and every objective / stopping reduction in FP64).  The default is FP16, with a tenth of
+    BF16's error (solution within 4e-4 instead of 4e-3 of the FP64 one on the demo case);
+    BF16 is the faster choice on dense dictionaries, where it runs on the tensor cores (141
+    against 65 operator pairs/s for FP16 at 1M streamlines).  Phase 2 restarts the plain FP64
     solver (float-float by default) from the phase-1 solution, which removes the bias of
     the reduced-precision operator.  Returns (x, details) with details['mixed'] and
     details['refine'] holding each phase's opt_details.  restart applies the function-value

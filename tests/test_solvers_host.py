@@ -72,3 +72,37 @@ def test_solve_batches_raises_a_job_error(fake_cuda, monkeypatch):
     for n in (1, 3):
         with pytest.raises(RuntimeError, match='job b failed'):
             solvers.solve_batches(_jobs(), n_streams=n)
+
+
+def test_solve_mixed_joins_the_phases(monkeypatch):
+    """solve_mixed: phase 2 starts from phase 1's x with the refinement settings, the
+    iterations add up, and with x_ref the two traces (seconds, |x - x_ref| / |x_ref|, cost)
+    join into one, phase 2's times shifted by phase 1's duration."""
+    import numpy as np
+    from commit_gb300 import solvers
+    calls = []
+
+    def fake_solve(y, A, At, tol_fun, tol_x, max_iter, verbose, x0, regularisation, confidence_array, arith, x_ref,
+                   restart):
+        calls.append(dict(x0=x0, arith=arith, max_iter=max_iter, tol_fun=tol_fun, restart=restart))
+        n = 3 if len(calls) == 1 else 2
+        tr = np.array([[0.1 * (k + 1), 1.0 / (k + 2), 10.0 - k] for k in range(n)])
+        return np.full(4, float(len(calls))), {'iterations': n, 'trace': tr, 'cost_function': 1.0}
+
+    monkeypatch.setattr(solvers, 'solve', fake_solve)
+
+    class _A:
+        T = None
+
+    x, det = solvers.solve_mixed(None, _A(), tol_fun=1e-4, max_iter=7, arith='bf16', refine_max_iter=5,
+                                 refine_tol_fun=1e-6, x_ref=np.ones(4), restart=True)
+    assert calls[0]['arith'] == 'bf16' and calls[0]['x0'] is None and calls[0]['max_iter'] == 7
+    assert calls[1]['arith'] is None and np.array_equal(calls[1]['x0'], np.full(4, 1.0))
+    assert calls[1]['max_iter'] == 5 and calls[1]['tol_fun'] == 1e-6 and calls[1]['restart']
+    assert det['iterations'] == 5 and np.array_equal(x, np.full(4, 2.0))
+    tr = det['trace']
+    assert tr.shape == (5, 3)
+    shift = tr[3:, 0] - det['refine']['trace'][:, 0]  # phase 1's duration, added to phase 2's times
+    assert shift[0] > 0 and np.allclose(shift, shift[0])
+    assert np.array_equal(tr[:3], det['mixed']['trace'])
+    assert np.allclose(tr[3:, 1:], det['refine']['trace'][:, 1:])
